@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Throughput of the point-driven dynamic-topology path on one GB300.
+
+Workload (the particle-fluid frames): 4,194,304 FP32 particles, seed 1, dam-break
+layout (0.5-voxel lattice over [0,128)x[0,256)x[0,128), jitter U(+-0.1), 5%
+scattered in a 512^3 domain), velocities N(0,1), frames advected by 0.5*v
+(10-frame cycle, positions precomputed on the device).  One step = one frame:
+
+  RebuildTopology(r=4) -> UpdateAtlas -> InsertPointsSubcell(4, R=4)
+  -> GatherLevelSet(rho=2) into an FP32 channel -> UpdateApron(0, 3.0)
+
+through the C ABI of libgbvdb.so, grid (3,3,3,4).  Metric: points/s
+(input particles per frame / frame time).  `e2e` repeats the frame with the
+positions copied from pinned host memory each step and the FP64 checksum read
+back.  `--impl reference` times the reference algorithm's CPU restatement
+(oracle/, all host threads) on a bounded sample of the same frames.
+
+Multi-GPU (torchrun): every rank runs its own independent grid (replicas, weak
+scaling); value = all ranks' points / the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gvdb-voxels_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "points/s rebuild+gather+apron (fluid frame, 4,194,304 particles)"
+N_FLUID = 4_194_304
+FRAMES = 10
+LOG2DIMS = (3, 3, 3, 4)
+R_TOPO, R_INSERT, RHO, BOUND = 4.0, 4.0, 2.0, 3.0
+SAMPLE_BOX = ((0.0, 0.0, 0.0), (32.0, 512.0, 512.0))  # CPU sample: the x < 32 slab of each frame
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def fluid_frames(seed):
+    import datasets
+
+    pos, vel = datasets.fluid(N_FLUID, seed=seed)
+    return pos, vel
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[4 + k].lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per gather launch from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "gather_fluid_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def run_frame(grid, n):
+    grid.rebuild_topology(n, R_TOPO)
+    grid.update_atlas()
+    _, ln = grid.insert_points_subcell(4, n, R_INSERT)
+    grid.gather_levelset(4, n, RHO, (0, 0, 0), ln)
+    grid.update_apron(0, BOUND)
+    return ln
+
+
+def cpu_sample_points(pos, vel, frame):
+    import datasets
+
+    p = (pos + 0.5 * (frame + 1) * vel).astype(np.float32)
+    return datasets.crop(p, *SAMPLE_BOX)
+
+
+def cpu_frame(og, pts):
+    og.rebuild_topology(pts, R_TOPO)
+    og.update_atlas()
+    og.insert_points_subcell(pts, R_INSERT)
+    og.gather_levelset(RHO)
+    og.update_apron(0, BOUND)
+
+
+def cpu_baseline(pos, vel, steps=2):
+    """the oracle (CPU restatement of the reference path) on the x < 32 slab, all host threads"""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    og = oracle.OracleGrid(LOG2DIMS)
+    og.add_channel(0)
+    pts0 = cpu_sample_points(pos, vel, 0)
+    cpu_frame(og, pts0)  # warm-up (full rebuild)
+    tot_pts, tot_t = 0, 0.0
+    for k in range(1, steps + 1):
+        pts = cpu_sample_points(pos, vel, k)
+        t0 = time.perf_counter()
+        cpu_frame(og, pts)
+        tot_t += time.perf_counter() - t0
+        tot_pts += pts.shape[0]
+    cores = os.cpu_count()
+    return {"value": tot_pts / tot_t, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": "fluid frames 2-%d cropped to x < 32 (%d points/frame, density-preserving), FP64 oracle, "
+                      "OpenMP %d threads" % (steps + 1, pts0.shape[0], cores)}
+
+
+def bench_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    pos, vel = fluid_frames(1)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    og = oracle.OracleGrid(LOG2DIMS)
+    og.add_channel(0)
+    frame = 0
+    for _ in range(args.warmup):
+        cpu_frame(og, cpu_sample_points(pos, vel, frame % FRAMES))
+        frame += 1
+    tot_pts, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        pts = cpu_sample_points(pos, vel, frame % FRAMES)
+        if frame % FRAMES == 0:
+            og.request_full_rebuild(True)
+        t0 = time.perf_counter()
+        cpu_frame(og, pts)
+        tot_t += time.perf_counter() - t0
+        tot_pts += pts.shape[0]
+        frame += 1
+    v = tot_pts / tot_t
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "fluid frames, 4,194,304 particles, grid (3,3,3,4), r=R=4, rho=2 level set",
+                   "sample": "x < 32 slab per frame"},
+        "cpu_baseline": {"value": v, "unit": "points/s", "cores": cores, "kind": "port",
+                         "sample": "x < 32 slab of each fluid frame (%d points avg), CPU restatement of the "
+                                   "reference algorithm, OpenMP %d threads" % (tot_pts // args.steps, cores)},
+        "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def bench_ours(args):
+    import torch
+
+    import gbvdb
+
+    rank, local, world = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import build_lib
+
+    build_lib.build()
+    dev = torch.device("cuda", local)
+    pos, vel = fluid_frames(1 + rank)
+    dpos = torch.from_numpy(pos).to(dev)
+    dvel = torch.from_numpy(vel).to(dev)
+    frames = [(dpos + 0.5 * (f + 1) * dvel).contiguous() for f in range(FRAMES)]
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    grid = gbvdb.Grid(local, LOG2DIMS, stream=stream)
+    grid.add_channel(0, gbvdb.T_FLOAT)
+
+    state = {"frame": 0}
+
+    def step(src=None):
+        f = state["frame"] % FRAMES
+        if f == 0:
+            grid.request_full_rebuild(True)
+        buf = frames[f] if src is None else src(f)
+        n = grid.set_points(buf)
+        run_frame(grid, n)
+        state["frame"] += 1
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    l0 = grid.stats()["launches"]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    dev_ms = ev0.elapsed_time(ev1)
+    launches = grid.stats()["launches"] - l0
+    ms = dev_ms / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * N_FLUID / (ms / 1000.0)
+
+    # end to end: host positions -> device, frame, checksum -> host
+    host = [frames[f].cpu().pin_memory() for f in range(FRAMES)]
+    staging = torch.empty_like(frames[0])
+    checks = []
+
+    def from_host(f):
+        staging.copy_(host[f], non_blocking=True)
+        return staging
+
+    for _ in range(2):
+        step(from_host)
+        checks.append(grid.checksum(0))
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step(from_host)
+        checks.append(grid.checksum(0))
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * N_FLUID / (e2e_ms / 1000.0), "unit": "points/s",
+           "h2d_bytes_per_step": N_FLUID * 12, "d2h_bytes_per_step": 8}
+
+    # per-stage times and the gather roofline (separate pass: profiling synchronizes per call)
+    grid.set_profile(True)
+    stage_names = ["rebuild", "atlas", "insert", "gather", "apron"]
+    stage_ms = {k: 0.0 for k in stage_names}
+    gather_ms, sc_len, bricks = [], [], []
+    nprof = FRAMES
+    for _ in range(nprof):
+        f = state["frame"] % FRAMES
+        if f == 0:
+            grid.request_full_rebuild(True)
+        n = grid.set_points(frames[f])
+        for name, fn in (("rebuild", lambda: grid.rebuild_topology(n, R_TOPO)),
+                         ("atlas", lambda: grid.update_atlas()),
+                         ("insert", lambda: state.__setitem__("ln", grid.insert_points_subcell(4, n, R_INSERT)[1])),
+                         ("gather", lambda: grid.gather_levelset(4, n, RHO, (0, 0, 0), state["ln"])),
+                         ("apron", lambda: grid.update_apron(0, BOUND))):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            stage_ms[name] += 1000.0 * (time.perf_counter() - a) / nprof
+            if name == "gather":
+                gather_ms.append(sum(grid.stage_times()))
+                st = grid.stats()
+                sc_len.append(st["sc_len"])
+                bricks.append(st["bricks"])
+        state["frame"] += 1
+    grid.set_profile(False)
+    g_ms = float(np.mean(gather_ms))
+    S, B = float(np.mean(sc_len)), float(np.mean(bricks))
+    alg_bytes = 12.0 * S + 8.0 * 64.0 * B + 4.0 * 4096.0 * B
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (g_ms / 1000.0) / 1e9
+    traffic = profile_traffic()
+    roofline = {"kernel": "k_gather<float> (GatherLevelSet)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": g_ms,
+                "bytes_formula": "12*S + 8*64*B + 4*4096*B (S = subcell list length, B = linked bricks)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "fluid frames: 4,194,304 particles seed 1, dam-break 0.5-voxel lattice + 5% "
+                               "scattered in 512^3, 10-frame cycle of p += 0.5 v",
+                   "grid_log2dims": list(LOG2DIMS), "topology_radius": R_TOPO, "insert_radius": R_INSERT,
+                   "gather": "levelset rho=2 FP32", "apron_boundval": BOUND, "parallelism": "replicas",
+                   "l2": "inputs larger than L2 (per-frame working set about 1 GB, 10 rotating position buffers)",
+                   "subcell_list_len": S, "linked_bricks": B},
+        "e2e": e2e, "roofline": roofline, "gpu_launches": launches, "wall_s": wall, "clocks": clk.summary(),
+        "stage_ms": stage_ms, "checksum_last": checks[-1],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(pos, vel)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    grid.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

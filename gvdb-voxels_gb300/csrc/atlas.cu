@@ -1,0 +1,221 @@
+// atlas.cu -- atlas slot assignment, apron update, atlas export and reductions.
+//
+// Replaces (reference file:line):
+//   UpdateAtlas: AtlasAlloc/getAtlasPos loop + ClearMapping/AssignMapping
+//       VG.cpp:2630-2704, 2557-2590; gvdb_allocator.cpp:692-715
+//   UpdateApron<T> / gvdbUpdateApronF   cuda_gvdb_operators.cuh:72-131, VG.cpp:4418-4457
+//
+// Atlas storage is brick-major and split in two arrays per channel:
+//   interior[slot][z][y][x]  16^3 voxels, the voxels gathers write
+//   apron[slot][k]           1736 apron voxels (record stride 1744), k = apron_index(x,y,z)
+// so that a gather writes whole 32-byte sectors and the apron pass writes its own
+// records.  The logical atlas coordinate of padded voxel (x,y,z) of slot s is the
+// reference's getAtlasPos(s) + (x,y,z) (gvdb_allocator.cpp:705-715).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "kernels.h"
+
+namespace gbvdb {
+
+namespace {
+
+__global__ void k_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    flag[i] = mode == 0 ? (nodes[i].flags ? 1u : 0u) : (nodes[i].parent != kUndef64 ? 1u : 0u);
+}
+
+// flagged leaves in pool order get consecutive slot ids (VG.cpp:2655-2662)
+__global__ void k_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Node* nd = leaves + i;
+    if (!nd->flags) return;
+    unsigned id = scan[i];
+    unsigned a2 = (unsigned)ax * (unsigned)ay;
+    int pz = (int)(id / a2);
+    unsigned rem = id - (unsigned)pz * a2;
+    int py = (int)(rem / (unsigned)ax);
+    int px = (int)(rem - (unsigned)py * ax);
+    nd->value[0] = px * kPad + 1;
+    nd->value[1] = py * kPad + 1;
+    nd->value[2] = pz * kPad + 1;
+    AtlasNode an;
+    an.pos[0] = nd->pos[0];
+    an.pos[1] = nd->pos[1];
+    an.pos[2] = nd->pos[2];
+    an.leaf = (int32_t)i;
+    amap[id] = an;
+}
+
+__global__ void k_fill_u32(uint32_t* p, long long n, uint32_t v) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// One block per assigned slot.  The 26 neighbour slots are looked up once per
+// brick (one tree traversal each, the reference does one per apron voxel); then
+// every apron voxel copies the matching interior voxel of its neighbour, or the
+// boundary value when no active brick contains that index-space position.
+template <typename T>
+__global__ void k_apron(TreeView t, const AtlasNode* __restrict__ amap, int ax, int ay, const T* __restrict__ interior,
+                        T* __restrict__ apron, T boundval) {
+    __shared__ int nslot[27];
+    const int s = blockIdx.x;
+    const AtlasNode an = amap[s];
+    if (an.leaf < 0) return;
+    if (threadIdx.x < 27) {
+        int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
+        int ns = -1;
+        if (dx | dy | dz) {
+            long long nl = get_leaf_at_voxel(t, an.pos[0] + 16 * dx, an.pos[1] + 16 * dy, an.pos[2] + 16 * dz);
+            if (nl >= 0) ns = slot_of_value(t.nodes[0][nl].value, ax, ay);
+        }
+        nslot[threadIdx.x] = ns;
+    }
+    __syncthreads();
+    T* out = apron + (size_t)s * kApronStride;
+    for (int k = threadIdx.x; k < kApronVox; k += blockDim.x) {
+        int x, y, z;
+        apron_coord(k, x, y, z);
+        int dx = x == 0 ? -1 : (x == 17 ? 1 : 0);
+        int dy = y == 0 ? -1 : (y == 17 ? 1 : 0);
+        int dz = z == 0 ? -1 : (z == 17 ? 1 : 0);
+        int ns = nslot[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
+        T v = boundval;
+        if (ns >= 0) {
+            int lx = (x - 1) & 15, ly = (y - 1) & 15, lz = (z - 1) & 15;
+            v = interior[(size_t)ns * 4096 + (lz << 8) + (ly << 4) + lx];
+        }
+        out[k] = v;
+    }
+}
+
+template <typename T>
+__global__ void k_export_bricks(const T* __restrict__ interior, const T* __restrict__ apron, int used, T* out) {
+    long long total = (long long)used * 5832;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int s = (int)(i / 5832);
+        int r = (int)(i - (long long)s * 5832);
+        int z = r / 324, y = (r / 18) % 18, x = r % 18;
+        T v;
+        if (x > 0 && x < 17 && y > 0 && y < 17 && z > 0 && z < 17)
+            v = interior[(size_t)s * 4096 + ((z - 1) << 8) + ((y - 1) << 4) + (x - 1)];
+        else
+            v = apron[(size_t)s * kApronStride + apron_index(x, y, z)];
+        out[i] = v;
+    }
+}
+
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <typename T>
+__global__ void k_checksum(const AtlasNode* __restrict__ amap, int used, const T* __restrict__ interior, double* out) {
+    double acc = 0;
+    long long total = (long long)used * 4096;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        int s = (int)(i >> 12);
+        if (amap[s].leaf < 0) continue;
+        acc += (double)to_f32(interior[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+        if (threadIdx.x == 0) atomicAdd(out, v);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T from_f32(float v);
+template <>
+__device__ __forceinline__ float from_f32<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __half from_f32<__half>(float v) { return __float2half_rn(v); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+template <typename T>
+__global__ void k_fill_interior(const AtlasNode* __restrict__ amap, int used, T* interior, float value) {
+    long long total = (long long)used * 4096;
+    T v = from_f32<T>(value);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        if (amap[i >> 12].leaf < 0) continue;
+        interior[i] = v;
+    }
+}
+
+inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+inline unsigned gs_blocks(long long n, int t) {
+    long long b = (n + t - 1) / t;
+    long long cap = 152LL * 16;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+}  // namespace
+
+void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag, cudaStream_t s) {
+    if (n <= 0) return;
+    k_node_flags<<<blocks_for(n, 256), 256, 0, s>>>(nodes, n, mode, flag);
+}
+void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
+                         cudaStream_t s) {
+    if (n <= 0) return;
+    k_assign_slots<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scan, ax, ay, amap);
+}
+void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s) {
+    if (n <= 0) return;
+    k_fill_u32<<<gs_blocks(n, 256), 256, 0, s>>>(p, n, v);
+}
+void launch_apron(const TreeView& t, const AtlasNode* amap, int used, int ax, int ay, int esize,
+                  const void* interior, void* apron, uint32_t boundbits, cudaStream_t s) {
+    if (used <= 0) return;
+    if (esize == 4) {
+        float b;
+        memcpy(&b, &boundbits, 4);
+        k_apron<float><<<used, 256, 0, s>>>(t, amap, ax, ay, (const float*)interior, (float*)apron, b);
+    } else {
+        uint16_t b16 = (uint16_t)boundbits;
+        __half_raw hr;
+        hr.x = b16;
+        k_apron<__half><<<used, 256, 0, s>>>(t, amap, ax, ay, (const __half*)interior, (__half*)apron, __half(hr));
+    }
+}
+void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out, cudaStream_t s) {
+    if (used <= 0) return;
+    long long total = (long long)used * 5832;
+    if (esize == 4)
+        k_export_bricks<float><<<gs_blocks(total, 256), 256, 0, s>>>((const float*)interior, (const float*)apron, used,
+                                                                     (float*)out);
+    else
+        k_export_bricks<__half><<<gs_blocks(total, 256), 256, 0, s>>>((const __half*)interior, (const __half*)apron,
+                                                                       used, (__half*)out);
+}
+void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* interior, double* out, cudaStream_t s) {
+    if (used <= 0) return;
+    long long total = (long long)used * 4096;
+    if (dtype == 3)
+        k_checksum<float><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const float*)interior, out);
+    else if (dtype == 100)
+        k_checksum<__half><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __half*)interior, out);
+    else
+        k_checksum<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, out);
+}
+void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value, cudaStream_t s) {
+    if (used <= 0) return;
+    long long total = (long long)used * 4096;
+    if (dtype == 3)
+        k_fill_interior<float><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (float*)interior, value);
+    else if (dtype == 100)
+        k_fill_interior<__half><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (__half*)interior, value);
+    else
+        k_fill_interior<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (__nv_bfloat16*)interior,
+                                                                            value);
+}
+
+}  // namespace gbvdb

@@ -1,0 +1,221 @@
+// common.cuh -- device-side types and helpers shared by the libgbvdb kernels.
+//
+// Node / pool layouts follow the reference byte for byte:
+//   Node            gvdb_node.h:27-40, cuda_gvdb_nodes.cuh:24-35 (64 bytes)
+//   Elem(grp,lev,n) gvdb_allocator.h:59-62
+//   child lists     res^3 u64 entries per node, 0xFF..FF = empty (VG.cpp:979-985)
+// The tree traversals restate getPosParent / getParent / getPosLeafParent /
+// getNode (cuda_gvdb_nodes.cuh:199-397) with one addition: a position outside
+// the node being descended is rejected instead of aliasing into a wrong child
+// slot (the reference has no bounds check there, ND.cuh:317-322).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbvdb {
+
+constexpr int kMaxLev = 10;
+constexpr unsigned long long kUndef64 = 0xFFFFFFFFFFFFFFFFull;
+constexpr unsigned long long kUndefL = 0xFFFFFFFFull;
+constexpr float kNoHit = 1.0e10f;
+constexpr int kBrick = 16;     // leaf resolution (log2dim[0] == 4)
+constexpr int kPad = 18;       // brick with a 1-voxel apron
+constexpr int kApronVox = 1736;  // 18^3 - 16^3
+constexpr int kApronStride = 1744;  // apron record length (multiple of 16 elements)
+
+struct __align__(16) Node {
+    uint8_t lev, flags, prio, pad;
+    int32_t pos[3];
+    int32_t value[3];
+    float vrange[3];
+    unsigned long long parent;
+    unsigned long long childlist;
+    unsigned long long mask;
+};
+static_assert(sizeof(Node) == 64, "node record is 64 bytes");
+
+struct __align__(16) AtlasNode {
+    int32_t pos[3];
+    int32_t leaf;
+};
+
+// Read-only view of the tree passed to kernels by value.
+struct TreeView {
+    int levs;
+    int top_lev;
+    int res[kMaxLev];
+    int lgres[kMaxLev];
+    int lgrange[kMaxLev];          // log2(range[l])
+    long long ncnt[kMaxLev];
+    Node* nodes[kMaxLev];
+    unsigned long long* clist[kMaxLev];
+};
+
+__host__ __device__ inline unsigned long long elem(int grp, int lev, unsigned long long ndx) {
+    return (unsigned long long)grp | ((unsigned long long)lev << 8) | (ndx << 16);
+}
+
+// ---- child-slot helpers -------------------------------------------------
+
+// slot of integer position p inside node (at level l, corner npos); -1 if outside
+__device__ __forceinline__ int child_slot(const TreeView& t, int l, const int32_t* npos, int px, int py, int pz) {
+    long long dx = (long long)px - npos[0], dy = (long long)py - npos[1], dz = (long long)pz - npos[2];
+    long long rg = 1ll << t.lgrange[l];
+    if (dx < 0 || dy < 0 || dz < 0 || dx >= rg || dy >= rg || dz >= rg) return -1;
+    int sh = t.lgrange[l] - t.lgres[l];  // log2 of the child range
+    int cx = (int)(dx >> sh), cy = (int)(dy >> sh), cz = (int)(dz >> sh);
+    return (cz << (2 * t.lgres[l])) | (cy << t.lgres[l]) | cx;
+}
+
+// getChild (ND.cuh:115-124): child index, -1 when empty
+__device__ __forceinline__ long long get_child(const TreeView& t, const Node* nd, int b) {
+    unsigned long long listid = nd->childlist;
+    if (listid == kUndefL) return -1;
+    int clev = (int)((listid >> 8) & 0xFF);
+    unsigned long long cndx = listid >> 16;
+    unsigned long long e = t.clist[clev][(cndx << (3 * t.lgres[clev])) + (unsigned)b];
+    if (e == kUndef64) return -1;
+    return (long long)(e >> 16);
+}
+
+// getPosParent (ND.cuh:303-348)
+__device__ inline long long get_pos_parent(const TreeView& t, int px, int py, int pz, int stop_lev) {
+    if (t.ncnt[t.top_lev] == 0) return -1;
+    const Node* nd = t.nodes[t.top_lev];
+    int l = nd->lev;
+    if (l == 0) return 0;
+    while (l > 0) {
+        int b = child_slot(t, l, nd->pos, px, py, pz);
+        if (b < 0) return -1;
+        long long c = get_child(t, nd, b);
+        l--;
+        if (c < 0) return -1;
+        if (l == stop_lev) return c;
+        nd = t.nodes[l] + c;
+    }
+    return -1;
+}
+
+// getParent (ND.cuh:350-397)
+__device__ inline long long get_parent(const TreeView& t, int stop_lev, int px, int py, int pz) {
+    const Node* nd = t.nodes[t.top_lev];
+    if (!nd->flags) return 0;
+    int l = nd->lev;
+    if (l == stop_lev) return 0;
+    while (l > stop_lev) {
+        int b = child_slot(t, l, nd->pos, px, py, pz);
+        if (b < 0) return -1;
+        l--;
+        long long c = get_child(t, nd, b);
+        if (c < 0) return -1;
+        if (l == stop_lev) return c;
+        nd = t.nodes[l] + c;
+    }
+    return -1;
+}
+
+// getPosLeafParent (ND.cuh:255-288); single-leaf trees check containment
+__device__ inline long long get_pos_leaf(const TreeView& t, int px, int py, int pz) {
+    if (t.ncnt[t.top_lev] == 0) return -1;
+    const Node* nd = t.nodes[t.top_lev];
+    int l = nd->lev;
+    if (l == 0) {
+        long long dx = (long long)px - nd->pos[0], dy = (long long)py - nd->pos[1], dz = (long long)pz - nd->pos[2];
+        long long rg = 1ll << t.lgrange[0];
+        if (dx < 0 || dy < 0 || dz < 0 || dx >= rg || dy >= rg || dz >= rg) return -1;
+        return 0;
+    }
+    while (true) {
+        int b = child_slot(t, l, nd->pos, px, py, pz);
+        if (b < 0) return -1;
+        long long c = get_child(t, nd, b);
+        if (c < 0) return -1;
+        l--;
+        if (l == 0) return c;
+        nd = t.nodes[l] + c;
+    }
+}
+
+// getNode(float pos) as used by UpdateApron (ND.cuh:199-253) for integer voxel w
+__device__ inline long long get_leaf_at_voxel(const TreeView& t, int wx, int wy, int wz) {
+    if (t.ncnt[t.top_lev] == 0) return -1;
+    int lev = t.top_lev;
+    const Node* nd = t.nodes[lev];
+    long long id = 0;
+    while (lev > 0) {
+        int b = child_slot(t, lev, nd->pos, wx, wy, wz);
+        if (b < 0) return -1;
+        lev--;
+        long long c = get_child(t, nd, b);
+        if (c < 0) return -1;
+        id = c;
+        nd = t.nodes[lev] + c;
+    }
+    long long dx = (long long)wx - nd->pos[0], dy = (long long)wy - nd->pos[1], dz = (long long)wz - nd->pos[2];
+    long long rg = 1ll << t.lgrange[0];
+    if (dx < 0 || dy < 0 || dz < 0 || dx >= rg || dy >= rg || dz >= rg) return -1;
+    return id;
+}
+
+// atlas slot from mValue (inverse of getAtlasPos, gvdb_allocator.cpp:705-715)
+__device__ __forceinline__ int slot_of_value(const int32_t* v, int ax, int ay) {
+    if (v[0] < 0) return -1;
+    return ((v[2] / kPad) * ay + v[1] / kPad) * ax + v[0] / kPad;
+}
+
+// ---- exact float helpers (no contraction) ------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// GetCoveringNode float version (PT.cuh:88-100) as a node coordinate
+__device__ __forceinline__ int cover_coord(float w, int lgrange) {
+    float fr = (float)(1 << lgrange);
+    float np = __fmul_rn(ceilf(__fdiv_rn(w, fr)), fr);
+    int ni = (int)np;
+    if (w < (float)ni) ni -= (1 << lgrange);
+    return ni >> lgrange;  // ni >= 0 for w >= 0
+}
+
+// ordered-int encoding of floats for atomicMin/Max
+__device__ __forceinline__ int f2o(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__host__ __device__ inline float o2f(int i) {
+#ifdef __CUDA_ARCH__
+    return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF);
+#else
+    int j = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    memcpy(&f, &j, 4);
+    return f;
+#endif
+}
+
+__device__ __forceinline__ void load_pos(const char* base, long long i, int stride, int off, float& x, float& y, float& z) {
+    const float* q = reinterpret_cast<const float*>(base + i * (long long)stride + off);
+    x = __ldg(q);
+    y = __ldg(q + 1);
+    z = __ldg(q + 2);
+}
+
+// padded-brick coordinate (x,y,z in [0,18)) on the apron shell -> apron record index
+__host__ __device__ inline int apron_index(int x, int y, int z) {
+    if (z == 0) return y * 18 + x;
+    if (z == 17) return 324 + y * 18 + x;
+    if (y == 0) return 648 + (z - 1) * 18 + x;
+    if (y == 17) return 936 + (z - 1) * 18 + x;
+    if (x == 0) return 1224 + (z - 1) * 16 + (y - 1);
+    return 1480 + (z - 1) * 16 + (y - 1);  // x == 17
+}
+// inverse of apron_index
+__host__ __device__ inline void apron_coord(int i, int& x, int& y, int& z) {
+    if (i < 324) { z = 0; y = i / 18; x = i % 18; return; }
+    if (i < 648) { i -= 324; z = 17; y = i / 18; x = i % 18; return; }
+    if (i < 936) { i -= 648; y = 0; z = 1 + i / 18; x = i % 18; return; }
+    if (i < 1224) { i -= 936; y = 17; z = 1 + i / 18; x = i % 18; return; }
+    if (i < 1480) { i -= 1224; x = 0; z = 1 + i / 16; y = 1 + i % 16; return; }
+    i -= 1480; x = 17; z = 1 + i / 16; y = 1 + i % 16;
+}
+
+}  // namespace gbvdb

@@ -1,0 +1,1139 @@
+// grid.cu -- host orchestration of the point-driven path and the C ABI (include/gbvdb.h).
+//
+// One gbvdb_grid is the state a nvdb::VolumeGVDB object holds for this path
+// (source/gvdb_library/src/gvdb_volume_gvdb.h:319-901): grid configuration, node
+// pools, the atlas channels and the subcell binning of the last insert.  All
+// device work is issued on the grid's stream; the host reads back only the few
+// counters it needs to size allocations (bounding box, unique key counts, used
+// leaf count, subcell-list length), each as one small pinned copy.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gbvdb.h"
+#include "kernels.h"
+
+using namespace gbvdb;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct Channel {
+    bool used = false;
+    int dtype = GBVDB_T_FLOAT;
+    int apron = 1;
+    int esize = 4;
+    DevBuf interior, apron_buf;
+    long long cap_slots = 0;
+};
+
+struct StatusError {
+    gbvdb_status st;
+    std::string msg;
+};
+
+uint16_t f2h_bits(float f) {  // round to nearest even, float -> IEEE half
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    int32_t exp = (int32_t)((x >> 23) & 0xFF) - 127 + 15;
+    uint32_t mant = x & 0x7FFFFFu;
+    if (((x >> 23) & 0xFF) == 0xFF) return (uint16_t)(sign | 0x7C00u | (mant ? 0x200u : 0));
+    if (exp >= 31) return (uint16_t)(sign | 0x7C00u);
+    if (exp <= 0) {
+        if (exp < -10) return (uint16_t)sign;
+        mant |= 0x800000u;
+        uint32_t shift = (uint32_t)(14 - exp);
+        uint32_t h = mant >> shift;
+        uint32_t rem = mant & ((1u << shift) - 1), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1))) h++;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = ((uint32_t)exp << 10) | (mant >> 13);
+    uint32_t rem = mant & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1))) h++;
+    return (uint16_t)(sign | h);
+}
+uint16_t f2bf_bits(float f) {
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    if ((x & 0x7F800000u) == 0x7F800000u && (x & 0x7FFFFFu)) return (uint16_t)((x >> 16) | 0x40);
+    uint32_t r = x + 0x7FFFu + ((x >> 16) & 1u);
+    return (uint16_t)(r >> 16);
+}
+
+}  // namespace
+
+struct gbvdb_grid_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+
+    // configuration (Configure, VG.cpp:2380-2434)
+    bool configured = false;
+    int levs = 0;
+    int log2dim[kMaxLev] = {0};
+    int res[kMaxLev] = {0};
+    long long range[kMaxLev] = {0};
+    int lgrange[kMaxLev] = {0};
+
+    // pools
+    DevBuf nodes[kMaxLev], clist[kMaxLev];
+    long long ncnt[kMaxLev] = {0}, nused[kMaxLev] = {0};
+    int rebuild_topo = 1;
+    int curr_depth = -1;
+    int last_depth = 0;
+    int root_lev = -1;
+    int root_pos[3] = {0, 0, 0};
+    float posmin[3] = {0, 0, 0}, posmax[3] = {0, 0, 0};
+    int bounds[6] = {0, 0, 0, 0, 0, 0};
+
+    // points (SetPoints, VG.cpp:4900-4908)
+    PointSrc pts{nullptr, 0, 12, 0};
+    const void* vel = nullptr;
+    const void* clr = nullptr;
+
+    // atlas
+    int def_ax = 16, def_ay = 16, def_az = 1;  // SetChannelDefault(16,16,1), VG.cpp:2348
+    int ax = 0, ay = 0, az = 0;
+    int atlas_last = 0;
+    Channel ch[8];
+    DevBuf amap;
+    long long amap_slots = 0;
+
+    // subcells of the last InsertPointsSubcell
+    bool sc_valid = false;
+    float sc_R = 0.f;
+    float3 sc_trans{0, 0, 0};
+    PointSrc sc_pts{nullptr, 0, 12, 0};
+    long long sc_nleaf = 0, sc_nbricks = 0, sc_len = 0, sc_orphans = 0;
+    bool lists_valid = false;
+    DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted;
+    DevBuf list_cnt, list_off, list_pts;
+
+    // scratch
+    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer;
+    unsigned char* pinned = nullptr;
+
+    // profiling
+    bool profile = false;
+    std::vector<double> stage_ms;
+
+    // ---------------------------------------------------------------- helpers
+    void check(cudaError_t e, const char* what) {
+        if (e != cudaSuccess) throw StatusError{GBVDB_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e)};
+    }
+    long long n_launch = 0, n_readback = 0;
+    void check_launch(const char* what) {
+        n_launch++;
+        check(cudaGetLastError(), what);
+    }
+    void sync() { check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
+
+    void grow(DevBuf& b, size_t bytes, size_t preserve = 0) {
+        if (bytes <= b.cap) return;
+        size_t cap = std::max(bytes, b.cap + b.cap / 2);
+        cap = (cap + 255) & ~size_t(255);
+        void* np = nullptr;
+        cudaError_t e = cudaMallocAsync(&np, cap, stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw StatusError{GBVDB_OUT_OF_MEMORY, "device allocation of " + std::to_string(cap) + " bytes failed"};
+        }
+        if (b.p) {
+            if (preserve) check(cudaMemcpyAsync(np, b.p, std::min(preserve, b.cap), cudaMemcpyDeviceToDevice, stream),
+                                "preserve copy");
+            check(cudaFreeAsync(b.p, stream), "cudaFreeAsync");
+        }
+        b.p = np;
+        b.cap = cap;
+    }
+    void release(DevBuf& b) {
+        if (b.p) cudaFreeAsync(b.p, stream);
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    template <typename T>
+    T* ptr(DevBuf& b) { return reinterpret_cast<T*>(b.p); }
+
+    void readback(void* host, const void* dev, size_t bytes) {
+        n_readback++;
+        check(cudaMemcpyAsync(pinned, dev, bytes, cudaMemcpyDeviceToHost, stream), "readback");
+        sync();
+        memcpy(host, pinned, bytes);
+    }
+    void upload(void* dev, const void* host, size_t bytes) {
+        // staged through a device-side copy of pageable memory: small control data only
+        check(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, stream), "upload");
+    }
+
+    int top_lev() const {
+        int t = 1;
+        for (int n = levs - 1; n >= 0; n--)
+            if (ncnt[n] == 1) t = n;
+        return t;
+    }
+    TreeView view() {
+        TreeView t{};
+        t.levs = levs;
+        t.top_lev = top_lev();
+        for (int l = 0; l < kMaxLev; l++) {
+            t.res[l] = l < levs ? res[l] : 1;
+            t.lgres[l] = l < levs ? log2dim[l] : 0;
+            t.lgrange[l] = l < levs ? lgrange[l] : 0;
+            t.ncnt[l] = ncnt[l];
+            t.nodes[l] = ptr<Node>(nodes[l]);
+            t.clist[l] = ptr<unsigned long long>(clist[l]);
+        }
+        return t;
+    }
+    long long cl_len(int lev) const { return lev >= 1 ? (1ll << (3 * log2dim[lev])) : 0; }
+
+    void ensure_pool(int lev, long long need) {
+        grow(nodes[lev], (size_t)need * sizeof(Node), (size_t)ncnt[lev] * sizeof(Node));
+        if (lev >= 1)
+            grow(clist[lev], (size_t)(need * cl_len(lev)) * 8, (size_t)(ncnt[lev] * cl_len(lev)) * 8);
+    }
+
+    void clear_topology() {  // Clear (VG.cpp:2487-2503)
+        for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
+        atlas_last = 0;
+        rebuild_topo = 1;
+        sc_valid = false;
+        lists_valid = false;
+    }
+
+    // ---------------------------------------------------------- stage timing
+    cudaEvent_t ev[64];
+    int nev = 0;
+    void mark() {
+        if (!profile || nev >= 64) return;
+        cudaEventRecord(ev[nev++], stream);
+    }
+    void stage_begin() {
+        nev = 0;
+        mark();
+    }
+    void stage_end() {
+        if (!profile) return;
+        sync();
+        stage_ms.clear();
+        for (int i = 1; i < nev; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
+            stage_ms.push_back(ms);
+        }
+    }
+
+    // ------------------------------------------------------------ topology
+    int determine_depth(int out_root[3]) const {  // DetermineDepth (VG.cpp:821-837)
+        int pmin[3], pmax[3];
+        for (int a = 0; a < 3; a++) { pmin[a] = (int)posmin[a]; pmax[a] = (int)posmax[a]; }
+        for (int lev = 0; lev < levs; lev++) {
+            long long rg = range[lev];
+            bool same = true;
+            for (int a = 0; a < 3; a++)
+                if (pmin[a] / rg != pmax[a] / rg) same = false;
+            if (same) {
+                for (int a = 0; a < 3; a++) out_root[a] = (int)((pmin[a] / rg) * rg);
+                return lev;
+            }
+        }
+        return -1;
+    }
+
+    void compute_bbox(long long n, float3 orig) {  // GetBoundingBox (VG.cpp:5404-5467)
+        int init[6];
+        for (int a = 0; a < 3; a++) { init[a] = 0x7F800000; init[3 + a] = (int)(0xFF800000u ^ 0x7FFFFFFFu); }
+        grow(misc, 256);
+        int* d6 = ptr<int>(misc);
+        memcpy(pinned, init, sizeof(init));
+        check(cudaMemcpyAsync(d6, pinned, sizeof(init), cudaMemcpyHostToDevice, stream), "bbox init");
+        PointSrc p = pts;
+        p.n = n;
+        launch_bbox(p, orig, d6, stream);
+        check_launch("bbox");
+        int out[6];
+        readback(out, d6, sizeof(out));
+        for (int a = 0; a < 3; a++) {
+            float mn = o2f(out[a]), mx = o2f(out[3 + a]);
+            float lo = mn - 1.0f, hi = mx + 2.0f;
+            posmin[a] = 0 > lo ? 0 : lo;
+            posmax[a] = 0 > hi ? 0 : hi;
+        }
+    }
+
+    // key domains of levels [0, depth): node coordinates that any pass can emit,
+    // clipped to the root node's extent
+    KeyDomains domains(int depth, float margin, const int rpos[3], int rlev, long long* total_bits) {
+        KeyDomains kd{};
+        long long bit = 0;
+        long long rg_root = range[rlev];
+        for (int l = 0; l < depth; l++) {
+            KeyDomain& d = kd.d[l];
+            for (int a = 0; a < 3; a++) {
+                double lo = std::max(0.0, (double)posmin[a] - margin);
+                double hi = (double)posmax[a] + margin;
+                long long clo = (long long)std::floor(lo) >> lgrange[l];
+                long long chi = (long long)std::floor(hi) >> lgrange[l];
+                long long rlo = (long long)rpos[a] >> lgrange[l];
+                long long rhi = ((long long)rpos[a] + rg_root - 1) >> lgrange[l];
+                clo = std::max(clo, rlo);
+                chi = std::min(chi, rhi);
+                if (chi < clo) chi = clo;
+                d.lo[a] = (int)clo;
+                d.dim[a] = (int)(chi - clo + 1);
+            }
+            d.bitbase = bit;
+            d.nbits = (long long)d.dim[0] * d.dim[1] * d.dim[2];
+            bit += (d.nbits + 31) & ~31ll;
+        }
+        *total_bits = bit;
+        return kd;
+    }
+
+    // dedup keys of one pass (bitmap already filled) and append the new nodes to the pools
+    // in ascending key order; returns the number of new nodes
+    long long allocate_from_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
+        long long nwords = total_bits / 32;
+        grow(pcnt, (size_t)(nwords + 1) * 4);
+        grow(pscan, (size_t)(nwords + 1) * 4);
+        grow(scan_tmp, scan_tmp_bytes(nwords));
+        launch_popc(ptr<uint32_t>(bitmap), nwords, ptr<uint32_t>(pcnt), stream);
+        check_launch("popc");
+        scan_exclusive_u32(ptr<uint32_t>(pcnt), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
+        check_launch("scan");
+        // per-level totals: prefix at each level's first word, and the grand total
+        std::vector<uint32_t> at(depth + 1);
+        for (int l = 0; l <= depth; l++) {
+            long long w = l < depth ? kd.d[l].bitbase / 32 : nwords;
+            check(cudaMemcpyAsync(pinned + 4 * l, ptr<uint32_t>(pscan) + w, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        }
+        int errflag = 0;
+        check(cudaMemcpyAsync(pinned + 4 * (depth + 1), ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        sync();
+        memcpy(at.data(), pinned, 4 * (depth + 1));
+        memcpy(&errflag, pinned + 4 * (depth + 1), 4);
+        if (errflag) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
+        long long added = 0;
+        for (int l = 0; l < depth; l++) {
+            long long cnt = (long long)at[l + 1] - (long long)at[l];
+            if (cnt <= 0) continue;
+            long long base = ncnt[l];
+            ensure_pool(l, base + cnt);
+            long long w0 = kd.d[l].bitbase / 32;
+            long long nw = ((kd.d[l].nbits + 31) / 32);
+            launch_alloc_nodes(ptr<uint32_t>(bitmap), ptr<uint32_t>(pscan), w0, nw, l, lgrange[l], kd.d[l], base,
+                               ptr<Node>(nodes[l]), stream);
+            check_launch("alloc_nodes");
+            if (l >= 1)
+                check(cudaMemsetAsync(ptr<unsigned long long>(clist[l]) + base * cl_len(l), 0xFF,
+                                      (size_t)(cnt * cl_len(l)) * 8, stream),
+                      "childlist init");
+            ncnt[l] = base + cnt;
+            nused[l] += cnt;
+            added += cnt;
+        }
+        return added;
+    }
+
+    void link_all(int depth) {
+        TreeView t = view();
+        for (int lev = depth - 1; lev >= 0; lev--) {
+            launch_link(t, lev, ncnt[lev], stream);
+            check_launch("link");
+        }
+    }
+
+    void clear_bitmap(long long total_bits) {
+        grow(bitmap, (size_t)(total_bits / 8) + 64);
+        check(cudaMemsetAsync(bitmap.p, 0, (size_t)(total_bits / 8), stream), "bitmap clear");
+        grow(misc, 256);
+        check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
+    }
+
+    static constexpr long long kMaxBits = 1ll << 34;
+
+    void activate_full(long long n, float radius, float3 orig, int D, const int rpos[3]) {
+        // root first (VG.cpp:1288-1300)
+        ensure_pool(D, 1);
+        Node root{};
+        root.lev = (uint8_t)D;
+        root.flags = 1;
+        for (int a = 0; a < 3; a++) { root.pos[a] = rpos[a]; root.value[a] = -1; }
+        root.parent = kUndefL;
+        root.childlist = elem(1, D, 0);
+        launch_write_node(ptr<Node>(nodes[D]), root, stream);
+        check_launch("write root");
+        check(cudaMemsetAsync(clist[D].p, 0xFF, (size_t)cl_len(D) * 8, stream), "root childlist");
+        ncnt[D] = 1;
+        nused[D] = 1;
+        root_lev = D;
+        for (int a = 0; a < 3; a++) root_pos[a] = rpos[a];
+        long long bits = 0;
+        float margin = 2.0f * std::max(radius, 0.0f) + 4.0f;
+        KeyDomains kd = domains(D, margin, rpos, D, &bits);
+        if (bits > kMaxBits) throw StatusError{GBVDB_NOT_SUPPORTED, "point extent too sparse for the key bitmap"};
+        PointSrc p = pts;
+        p.n = n;
+        // pass 1 (ActivateBricksGPU, VG.cpp:1229-1413)
+        clear_bitmap(bits);
+        TreeView t = view();
+        launch_keys_pass1(t, p, orig, D, kd, ptr<uint32_t>(bitmap), ptr<int>(misc) + 8, stream);
+        check_launch("keys_pass1");
+        allocate_from_bitmap(D, kd, bits);
+        mark();
+        link_all(D);
+        mark();
+        // pass 2 (ActivateExtraBricksGPU, VG.cpp:931-1016), only if radius >= 1 (VG.cpp:1207)
+        if (radius >= 1) {
+            clear_bitmap(bits);
+            t = view();
+            int rlo[3], rhi[3];
+            for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
+            launch_keys_box(t, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), nullptr, ptr<int>(misc) + 8,
+                            stream);
+            check_launch("keys_extra");
+            allocate_from_bitmap(D, kd, bits);
+            mark();
+            link_all(D);
+            mark();
+        }
+    }
+
+    void activate_incremental(long long n, float radius, float3 orig, int D, bool accum) {
+        long long nleaf = ncnt[0];
+        if (nleaf == 0) return;  // VG.cpp:1022
+        grow(markers, (size_t)nleaf * 4);
+        launch_init_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), accum ? 1 : 0, stream);
+        check_launch("init_markers");
+        long long bits = 0;
+        float margin = 2.0f * std::max(radius, 0.0f) + 4.0f;
+        int rl = root_lev >= 0 ? root_lev : D;
+        KeyDomains kd = domains(D, margin, root_pos, rl, &bits);
+        if (bits > kMaxBits) throw StatusError{GBVDB_NOT_SUPPORTED, "point extent too sparse for the key bitmap"};
+        clear_bitmap(bits);
+        PointSrc p = pts;
+        p.n = n;
+        TreeView t = view();
+        int rlo[3], rhi[3];
+        for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
+        launch_keys_box(t, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), ptr<int>(markers),
+                        ptr<int>(misc) + 8, stream);
+        check_launch("keys_incr");
+        // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
+        long long nwords = bits / 32;
+        grow(pcnt, (size_t)(nwords + 1) * 4);
+        grow(pscan, (size_t)(nwords + 1) * 4);
+        grow(scan_tmp, scan_tmp_bytes(nwords));
+        launch_popc(ptr<uint32_t>(bitmap), nwords, ptr<uint32_t>(pcnt), stream);
+        scan_exclusive_u32(ptr<uint32_t>(pcnt), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
+        check_launch("incr scan");
+        uint32_t total = 0;
+        readback(&total, ptr<uint32_t>(pscan) + nwords, 4);
+        mark();
+        if (total == 0) return;
+        launch_apply_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), stream);
+        check_launch("apply_markers");
+        allocate_from_bitmap(D, kd, bits);
+        link_all(D);
+        t = view();
+        launch_delink_leaf(t, ncnt[0], stream);
+        check_launch("delink_leaf");
+        for (int lev = 1; lev < D; lev++) {
+            launch_delink_upper(t, lev, ncnt[lev], stream);
+            check_launch("delink_upper");
+        }
+        // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148)
+        check(cudaMemsetAsync(ptr<char>(misc) + 64, 0, 8, stream), "count clear");
+        launch_count_flags(ptr<Node>(nodes[0]), ncnt[0], reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 64),
+                           stream);
+        check_launch("count_flags");
+        unsigned long long used = 0;
+        readback(&used, ptr<char>(misc) + 64, 8);
+        nused[0] = (long long)used;
+        mark();
+    }
+
+    gbvdb_status rebuild(long long n, float radius, float3 orig, bool accumulate, int min_depth) {
+        if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
+        if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
+        if (n <= 0) return GBVDB_NOOP;
+        if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
+        stage_begin();
+        compute_bbox(n, orig);
+        mark();
+        int rpos[3];
+        int D = determine_depth(rpos);
+        if (accumulate && D >= 0 && D < min_depth) D = min_depth;
+        if (D <= 0 || D > 5 || D >= levs)
+            throw StatusError{GBVDB_DEPTH_UNSUPPORTED, D == 0 ? "point extents smaller than 1 brick"
+                                                              : "point extents exceed the configured levels"};
+        if (accumulate) {  // AccumulateTopology (VG.cpp:1158-1178)
+            if (rebuild_topo) return rebuild(n, radius, orig, false, 0);
+            last_depth = D;
+            activate_incremental(n, radius, orig, D, true);
+            sc_valid = false;
+            stage_end();
+            return GBVDB_OK;
+        }
+        if (rebuild_topo) {
+            clear_topology();
+        } else if (D != curr_depth) {  // VG.cpp:1198-1203
+            clear_topology();
+            rebuild_topo = 1;
+            curr_depth = D;
+        }
+        last_depth = D;
+        if (rebuild_topo) {
+            activate_full(n, radius, orig, D, rpos);
+            rebuild_topo = 0;
+        } else {
+            activate_incremental(n, radius, orig, D, false);
+        }
+        sc_valid = false;
+        lists_valid = false;
+        stage_end();
+        return GBVDB_OK;
+    }
+
+    // ------------------------------------------------------------- atlas
+    void resize_channels(long long slots) {
+        for (int c = 0; c < 8; c++) {
+            Channel& C = ch[c];
+            if (!C.used || C.cap_slots >= slots) continue;
+            grow(C.interior, (size_t)slots * 4096 * C.esize, (size_t)C.cap_slots * 4096 * C.esize);
+            grow(C.apron_buf, (size_t)slots * kApronStride * C.esize, (size_t)C.cap_slots * kApronStride * C.esize);
+            C.cap_slots = slots;
+        }
+    }
+
+    gbvdb_status update_atlas() {  // UpdateAtlas (VG.cpp:2630-2704)
+        if (!ch[0].used) throw StatusError{GBVDB_INVALID_ARG, "no atlas channel"};
+        long long total = ncnt[0];
+        long long used = nused[0];
+        atlas_last = 0;
+        long long layer = (long long)ax * ay;
+        if (used > layer * az) az = (int)std::ceil((double)((float)used / (float)layer));
+        long long F = 0;
+        if (total > 0) {
+            grow(flags, (size_t)(total + 1) * 4);
+            grow(flags_scan, (size_t)(total + 1) * 4);
+            grow(scan_tmp, scan_tmp_bytes(total));
+            launch_node_flags(ptr<Node>(nodes[0]), total, 0, ptr<uint32_t>(flags), stream);
+            scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(flags_scan), total, scan_tmp.p, stream);
+            check_launch("atlas scan");
+            uint32_t f = 0;
+            readback(&f, ptr<uint32_t>(flags_scan) + total, 4);
+            F = f;
+        }
+        if (F > layer * az) az = (int)std::ceil((double)((float)F / (float)layer));  // AtlasAlloc growth, AL.cpp:695-698
+        long long slots = layer * az;
+        resize_channels(slots);
+        grow(amap, (size_t)slots * sizeof(AtlasNode));
+        amap_slots = slots;
+        launch_fill_u32(ptr<uint32_t>(amap), slots * 4, 0xFFFFFFFFu, stream);
+        if (total > 0)
+            launch_assign_slots(ptr<Node>(nodes[0]), total, ptr<uint32_t>(flags_scan), ax, ay, ptr<AtlasNode>(amap),
+                                stream);
+        check_launch("assign_slots");
+        atlas_last = (int)F;
+        return GBVDB_OK;
+    }
+
+    // -------------------------------------------------------- subcells
+    void build_linked() {
+        long long nleaf = ncnt[0];
+        grow(flags, (size_t)(nleaf + 1) * 4);
+        grow(scmap, (size_t)(nleaf + 1) * 4);
+        grow(scan_tmp, scan_tmp_bytes(nleaf));
+        launch_node_flags(ptr<Node>(nodes[0]), nleaf, 1, ptr<uint32_t>(flags), stream);
+        scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(scmap), nleaf, scan_tmp.p, stream);
+        check_launch("scmap");
+        uint32_t nb = 0;
+        readback(&nb, ptr<uint32_t>(scmap) + nleaf, 4);
+        sc_nbricks = nb;
+        grow(linked, (size_t)(nb + 1) * 4);
+        launch_linked_list(ptr<Node>(nodes[0]), nleaf, ptr<uint32_t>(scmap), ptr<int>(linked), stream);
+        check_launch("linked");
+    }
+
+    gbvdb_status insert_subcell(int sc, long long n, float R, float3 trans, long long* out_len) {
+        if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
+        if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
+        if (sc != 4 || log2dim[0] != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 with 16^3 bricks only"};
+        if (!(R >= 0)) throw StatusError{GBVDB_INVALID_ARG, "negative radius"};
+        if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
+        if (nused[0] == 0) return GBVDB_NOOP;  // VG.cpp:4973-4977
+        stage_begin();
+        build_linked();
+        mark();
+        long long nbins = sc_nbricks * 64;
+        grow(bin_cnt, (size_t)(nbins + 1) * 4);
+        grow(bin_off, (size_t)(nbins + 1) * 4);
+        check(cudaMemsetAsync(bin_cnt.p, 0, (size_t)(nbins + 1) * 4, stream), "bin clear");
+        PointSrc p = pts;
+        p.n = std::max(n, 0ll);
+        grow(bin_of, (size_t)std::max(p.n, 1ll) * 4);
+        grow(rank_of, (size_t)std::max(p.n, 1ll) * 4);
+        grow(misc, 256);
+        unsigned long long* totals = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 128);
+        check(cudaMemsetAsync(totals, 0, 16, stream), "totals clear");
+        TreeView t = view();
+        launch_bin_count(t, p, trans, R, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
+                         ptr<uint32_t>(rank_of), totals, stream);
+        check_launch("bin_count");
+        grow(scan_tmp, scan_tmp_bytes(nbins));
+        scan_exclusive_u32(ptr<uint32_t>(bin_cnt), ptr<uint32_t>(bin_off), nbins, scan_tmp.p, stream);
+        check_launch("bin scan");
+        unsigned long long tot[2];
+        uint32_t binned = 0;
+        check(cudaMemcpyAsync(pinned, totals, 16, cudaMemcpyDeviceToHost, stream), "rb");
+        check(cudaMemcpyAsync(pinned + 16, ptr<uint32_t>(bin_off) + nbins, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        sync();
+        memcpy(tot, pinned, 16);
+        memcpy(&binned, pinned + 16, 4);
+        mark();
+        grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
+        launch_bin_scatter(p, trans, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
+                           ptr<float4>(sorted), stream);
+        check_launch("bin_scatter");
+        mark();
+        sc_valid = true;
+        lists_valid = false;
+        sc_R = R;
+        sc_trans = trans;
+        sc_pts = p;
+        sc_nleaf = ncnt[0];
+        sc_len = (long long)tot[0];
+        sc_orphans = (long long)tot[1];
+        if (out_len) *out_len = sc_len;
+        stage_end();
+        return GBVDB_OK;
+    }
+
+    // materialize the reference-shaped subcell lists (export and the fallback gather)
+    void materialize_lists() {
+        if (lists_valid) return;
+        if (sc_len > 0xFFFFFFFFll) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell lists exceed 2^32 entries"};
+        long long nsub = sc_nbricks * 64;
+        grow(list_cnt, (size_t)(nsub + 1) * 4);
+        grow(list_off, (size_t)(nsub + 1) * 4);
+        grow(list_pts, (size_t)std::max(sc_len, 1ll) * 12);
+        check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
+        TreeView t = view();
+        launch_list_count(t, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt), stream);
+        grow(scan_tmp, scan_tmp_bytes(nsub));
+        scan_exclusive_u32(ptr<uint32_t>(list_cnt), ptr<uint32_t>(list_off), nsub, scan_tmp.p, stream);
+        check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
+        launch_list_fill(t, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
+                         ptr<uint32_t>(list_cnt), ptr<float>(list_pts), stream);
+        check_launch("lists");
+        lists_valid = true;
+    }
+
+    static uint32_t bits_of(float f) {
+        uint32_t u;
+        memcpy(&u, &f, 4);
+        return u;
+    }
+    static float next_up(float f) {
+        uint32_t u = bits_of(f);
+        u += 1;
+        float r;
+        memcpy(&r, &u, 4);
+        return r;
+    }
+
+    gbvdb_status gather(int mode, int sc, float rho, long long sc_len_arg, int chan, int clr_chan, bool accum) {
+        (void)clr_chan;
+        if (sc != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 only"};
+        if (chan < 0 || chan >= 8 || !ch[chan].used) throw StatusError{GBVDB_INVALID_ARG, "bad channel"};
+        if (ch[chan].dtype != GBVDB_T_FLOAT && ch[chan].dtype != GBVDB_T_HALF && ch[chan].dtype != GBVDB_T_BFLOAT16)
+            throw StatusError{GBVDB_NOT_SUPPORTED, "gathers write float, half or bfloat16 channels"};
+        if (clr) throw StatusError{GBVDB_NOT_SUPPORTED, "colour gathers are not implemented"};
+        if (nused[0] == 0) return GBVDB_NOOP;                       // VG.cpp:5321-5322, 5350-5351
+        if (mode == 0 && sc_len_arg == 0) return GBVDB_NOOP;        // VG.cpp:5321
+        if (!sc_valid || sc_nleaf != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "InsertPointsSubcell is stale"};
+        stage_begin();
+        GatherParams gp{};
+        gp.mode = mode;
+        gp.accum = accum ? 1 : 0;
+        gp.rho = rho;
+        gp.R = sc_R;
+        gp.dtype = ch[chan].dtype;
+        gp.ax = ax;
+        gp.ay = ay;
+        // static cutoff T: any d^2 >= T leaves the voxel at its initial value
+        float T = INFINITY;
+        if (!accum) {
+            if (mode == 0) {
+                T = (float)((double)rho * rho);
+                if (!(rho > 0)) T = 0.0f;
+                while (!(std::sqrt(T) >= rho)) T = next_up(T);
+            } else {
+                double r3 = (double)rho + 3.0;
+                T = r3 > 0 ? (float)(r3 * r3) : 0.0f;
+                while (!((float)(std::sqrt(T) - rho) >= 3.0f) && T < 3.0e38f) T = next_up(T);
+            }
+        }
+        gp.tbits = bits_of(T);
+        gp.lo_off = (int)std::floor((-1.0 - sc_R) / 4.0) - 1;
+        gp.hi_off = (int)std::ceil((4.0 + sc_R) / 4.0);
+        int span = 4 + gp.hi_off - gp.lo_off;
+        TreeView t = view();
+        void* interior = ch[chan].interior.p;
+        if (sc_orphans > 0 || span > 12) {
+            materialize_lists();
+            launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
+                                interior, stream);
+        } else {
+            launch_gather(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
+                          ptr<float4>(sorted), gp, interior, stream);
+        }
+        check_launch("gather");
+        mark();
+        stage_end();
+        return GBVDB_OK;
+    }
+
+    gbvdb_status update_apron(int chan, float boundval) {  // UpdateApron (VG.cpp:4418-4457)
+        if (chan < 0 || chan >= 8 || !ch[chan].used) throw StatusError{GBVDB_INVALID_ARG, "bad channel"};
+        if (ch[chan].apron == 0) return GBVDB_NOOP;
+        if (ncnt[0] == 0 || atlas_last == 0) return GBVDB_NOOP;
+        stage_begin();
+        uint32_t bb;
+        if (ch[chan].esize == 4) bb = bits_of(boundval);
+        else if (ch[chan].dtype == GBVDB_T_HALF) bb = f2h_bits(boundval);
+        else bb = f2bf_bits(boundval);
+        TreeView t = view();
+        launch_apron(t, ptr<AtlasNode>(amap), atlas_last, ax, ay, ch[chan].esize, ch[chan].interior.p,
+                     ch[chan].apron_buf.p, bb, stream);
+        check_launch("apron");
+        mark();
+        stage_end();
+        return GBVDB_OK;
+    }
+};
+
+// ------------------------------------------------------------------ C ABI
+
+#define GBVDB_GUARD(g)                                    \
+    if (!(g)) return GBVDB_INVALID_ARG;                   \
+    std::lock_guard<std::mutex> _lk((g)->mu);             \
+    try {                                                 \
+        cudaSetDevice((g)->device);
+#define GBVDB_END(g)                                      \
+    }                                                     \
+    catch (const StatusError& e) {                        \
+        (g)->err = e.msg;                                 \
+        return e.st;                                      \
+    }                                                     \
+    catch (const std::exception& e) {                     \
+        (g)->err = e.what();                              \
+        return GBVDB_OUT_OF_MEMORY;                       \
+    }
+
+extern "C" {
+
+gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
+    if (!out) return GBVDB_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return GBVDB_CUDA_ERROR;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return GBVDB_CUDA_ERROR;
+    gbvdb_grid g = new (std::nothrow) gbvdb_grid_s();
+    if (!g) return GBVDB_OUT_OF_MEMORY;
+    g->device = device;
+    if (cudaMallocHost(&g->pinned, 1 << 16) != cudaSuccess) {
+        delete g;
+        return GBVDB_OUT_OF_MEMORY;
+    }
+    for (int i = 0; i < 64; i++) cudaEventCreate(&g->ev[i]);
+    *out = g;
+    return GBVDB_OK;
+}
+
+gbvdb_status gbvdb_destroy(gbvdb_grid g) {
+    if (!g) return GBVDB_INVALID_ARG;
+    cudaSetDevice(g->device);
+    DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer};
+    for (DevBuf* b : bufs) g->release(*b);
+    for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
+    for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
+    cudaStreamSynchronize(g->stream);
+    for (int i = 0; i < 64; i++) cudaEventDestroy(g->ev[i]);
+    cudaFreeHost(g->pinned);
+    delete g;
+    return GBVDB_OK;
+}
+
+gbvdb_status gbvdb_set_stream(gbvdb_grid g, void* stream) {
+    GBVDB_GUARD(g)
+    g->sync();
+    g->stream = reinterpret_cast<cudaStream_t>(stream);
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+const char* gbvdb_last_error(gbvdb_grid g) { return g ? g->err.c_str() : "null grid"; }
+
+gbvdb_status gbvdb_configure(gbvdb_grid g, int levs, const int* log2dim) {
+    GBVDB_GUARD(g)
+    if (levs < 2 || levs > kMaxLev || !log2dim) return GBVDB_INVALID_ARG;
+    long long rg = 1;
+    int lg = 0;
+    for (int l = 0; l < levs; l++) {
+        int d = log2dim[l] == 0 ? 1 : log2dim[l];  // VG.cpp:2394
+        if (d < 1 || d > 6) return GBVDB_INVALID_ARG;
+        lg += d;
+        if (lg > 30) return GBVDB_NOT_SUPPORTED;
+        g->log2dim[l] = d;
+        g->res[l] = 1 << d;
+        rg <<= d;
+        g->range[l] = rg;
+        g->lgrange[l] = lg;
+    }
+    for (int l = levs; l < kMaxLev; l++) { g->log2dim[l] = 0; g->res[l] = 1; g->range[l] = rg; g->lgrange[l] = lg; }
+    g->levs = levs;
+    g->configured = true;
+    g->clear_topology();  // Configure ends with Clear (VG.cpp:2431)
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_configure5(gbvdb_grid g, int q4, int q3, int q2, int q1, int q0) {
+    int r[5] = {q0, q1, q2, q3, q4};
+    return gbvdb_configure(g, 5, r);
+}
+
+gbvdb_status gbvdb_set_channel_default(gbvdb_grid g, int ax, int ay, int az) {
+    GBVDB_GUARD(g)
+    if (ax <= 0 || ay <= 0 || az <= 0) return GBVDB_INVALID_ARG;
+    g->def_ax = ax;
+    g->def_ay = ay;
+    g->def_az = az;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron, int ax, int ay, int az) {
+    GBVDB_GUARD(g)
+    if (!g->configured) return GBVDB_INVALID_ARG;
+    if (chan < 0 || chan >= 8) return GBVDB_INVALID_ARG;
+    if (apron != 1) return GBVDB_NOT_SUPPORTED;  // the reference's apron kernels assume 1 (VG.cpp:4448)
+    if (g->log2dim[0] != 4) return GBVDB_NOT_SUPPORTED;
+    int es;
+    if (dtype == GBVDB_T_FLOAT) es = 4;
+    else if (dtype == GBVDB_T_HALF || dtype == GBVDB_T_BFLOAT16) es = 2;
+    else return GBVDB_NOT_SUPPORTED;
+    if (ax == 0 && ay == 0 && az == 0) {  // VG.cpp:2441-2444
+        if (chan == 0) { ax = g->def_ax; ay = g->def_ay; az = g->def_az; }
+        else { ax = g->ax; ay = g->ay; az = g->az; }
+    }
+    if (ax <= 0 || ay <= 0 || az <= 0) return GBVDB_INVALID_ARG;
+    if (chan == 0) { g->ax = ax; g->ay = ay; g->az = az; }
+    else if (ax != g->ax || ay != g->ay) return GBVDB_NOT_SUPPORTED;  // all channels share the slot layout
+    Channel& C = g->ch[chan];
+    C.used = true;
+    C.dtype = dtype;
+    C.apron = apron;
+    C.esize = es;
+    long long slots = (long long)g->ax * g->ay * g->az;
+    C.cap_slots = 0;
+    g->release(C.interior);
+    g->release(C.apron_buf);
+    g->grow(C.interior, (size_t)slots * 4096 * es);
+    g->grow(C.apron_buf, (size_t)slots * kApronStride * es);
+    g->check(cudaMemsetAsync(C.interior.p, 0, (size_t)slots * 4096 * es, g->stream), "channel clear");
+    g->check(cudaMemsetAsync(C.apron_buf.p, 0, (size_t)slots * kApronStride * es, g->stream), "channel clear");
+    C.cap_slots = slots;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off, int stride, const void* vel,
+                              int vel_off, int vel_stride, const void* clr, int clr_off, int clr_stride) {
+    GBVDB_GUARD(g)
+    (void)vel_off; (void)vel_stride; (void)clr_off; (void)clr_stride;
+    if (!pos || n < 0 || stride < 12 || off < 0 || (off % 4) || (stride % 4)) return GBVDB_INVALID_ARG;
+    g->pts.base = reinterpret_cast<const char*>(pos);
+    g->pts.n = n;
+    g->pts.off = off;
+    g->pts.stride = stride;
+    g->vel = vel;
+    g->clr = clr;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+static float3 f3(const float* v) { return v ? make_float3(v[0], v[1], v[2]) : make_float3(0, 0, 0); }
+
+gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3]) {
+    GBVDB_GUARD(g)
+    return g->rebuild(n, radius, f3(orig), false, 0);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3], int min_depth) {
+    GBVDB_GUARD(g)
+    return g->rebuild(n, radius, f3(orig), true, min_depth);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_request_full_rebuild(gbvdb_grid g, int tf) {
+    GBVDB_GUARD(g)
+    g->rebuild_topo = tf ? 1 : 0;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bounds) {
+    GBVDB_GUARD(g)
+    (void)commit_pool;  // pools live on the device only; nothing to commit
+    if (compute_bounds && g->ncnt[0] > 0) {  // ComputeBounds (VG.cpp:1792-1816)
+        int init[6] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000, (int)0x80000000};
+        g->grow(g->misc, 256);
+        int* d6 = g->ptr<int>(g->misc) + 16;
+        memcpy(g->pinned, init, sizeof(init));
+        g->check(cudaMemcpyAsync(d6, g->pinned, sizeof(init), cudaMemcpyHostToDevice, g->stream), "bounds init");
+        launch_leaf_bounds(g->ptr<Node>(g->nodes[0]), g->ncnt[0], g->lgrange[0], d6, g->stream);
+        g->check_launch("bounds");
+        g->readback(g->bounds, d6, sizeof(g->bounds));
+    }
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_update_atlas(gbvdb_grid g) {
+    GBVDB_GUARD(g)
+    return g->update_atlas();
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
+                                         int64_t* out_len) {
+    GBVDB_GUARD(g)
+    long long len = 0;
+    gbvdb_status st = g->insert_subcell(sc, n, radius, f3(trans), &len);
+    if (st == GBVDB_OK && out_len) *out_len = len;
+    return st;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_gather_density(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3], int64_t sc_len,
+                                  int chan, int clr_chan, int accum) {
+    GBVDB_GUARD(g)
+    (void)n; (void)trans;
+    return g->gather(0, sc, radius, sc_len, chan, clr_chan, accum != 0);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_gather_levelset(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
+                                   int64_t sc_len, int chan, int clr_chan, int accum) {
+    GBVDB_GUARD(g)
+    (void)n; (void)trans;
+    return g->gather(1, sc, radius, sc_len, chan, clr_chan, accum != 0);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval) {
+    GBVDB_GUARD(g)
+    return g->update_apron(chan, boundval);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
+    if (g->atlas_last == 0) return GBVDB_NOOP;
+    Channel& C = g->ch[chan];
+    launch_fill_interior(g->ptr<AtlasNode>(g->amap), g->atlas_last, C.dtype, C.interior.p, value, g->stream);
+    uint32_t bb = C.esize == 4 ? gbvdb_grid_s::bits_of(value)
+                               : (C.dtype == GBVDB_T_HALF ? f2h_bits(value) : f2bf_bits(value));
+    long long n = (long long)g->atlas_last * kApronStride;
+    if (C.esize == 4) {
+        launch_fill_u32(g->ptr<uint32_t>(C.apron_buf), n, bb, g->stream);
+    } else {
+        launch_fill_u32(g->ptr<uint32_t>(C.apron_buf), n / 2, bb | (bb << 16), g->stream);
+    }
+    g->check_launch("fill");
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_depth(gbvdb_grid g, int* depth, int* top_lev) {
+    GBVDB_GUARD(g)
+    if (depth) *depth = g->last_depth;
+    if (top_lev) *top_lev = g->top_lev();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used) {
+    GBVDB_GUARD(g)
+    for (int l = 0; l < kMaxLev; l++) {
+        if (total) total[l] = g->ncnt[l];
+        if (used) used[l] = g->nused[l];
+    }
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_point_bounds(gbvdb_grid g, float* out6) {
+    GBVDB_GUARD(g)
+    if (!out6) return GBVDB_INVALID_ARG;
+    for (int a = 0; a < 3; a++) { out6[a] = g->posmin[a]; out6[3 + a] = g->posmax[a]; }
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_nodes(gbvdb_grid g, int lev, void* host_out, int64_t cap) {
+    GBVDB_GUARD(g)
+    if (lev < 0 || lev >= kMaxLev || !host_out) return GBVDB_INVALID_ARG;
+    if (cap < g->ncnt[lev]) return GBVDB_CAPACITY;
+    if (g->ncnt[lev] == 0) return GBVDB_OK;
+    g->check(cudaMemcpyAsync(host_out, g->nodes[lev].p, (size_t)g->ncnt[lev] * sizeof(Node), cudaMemcpyDeviceToHost,
+                             g->stream), "export nodes");
+    g->sync();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_childlist(gbvdb_grid g, int lev, uint64_t* host_out, int64_t cap) {
+    GBVDB_GUARD(g)
+    if (lev < 1 || lev >= g->levs || !host_out) return GBVDB_INVALID_ARG;
+    long long n = g->ncnt[lev] * g->cl_len(lev);
+    if (cap < n) return GBVDB_CAPACITY;
+    if (n == 0) return GBVDB_OK;
+    g->check(cudaMemcpyAsync(host_out, g->clist[lev].p, (size_t)n * 8, cudaMemcpyDeviceToHost, g->stream),
+             "export childlist");
+    g->sync();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_atlas_info(gbvdb_grid g, int chan, int* info) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !info || !g->ch[chan].used) return GBVDB_INVALID_ARG;
+    info[0] = g->ax; info[1] = g->ay; info[2] = g->az; info[3] = g->atlas_last;
+    info[4] = g->ch[chan].dtype; info[5] = g->ch[chan].apron; info[6] = kPad; info[7] = g->ch[chan].esize;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_atlas_bricks(gbvdb_grid g, int chan, void* host_out, int64_t cap_bytes) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !host_out) return GBVDB_INVALID_ARG;
+    Channel& C = g->ch[chan];
+    long long bytes = (long long)g->atlas_last * 5832 * C.esize;
+    if (cap_bytes < bytes) return GBVDB_CAPACITY;
+    if (bytes == 0) return GBVDB_OK;
+    g->grow(g->xfer, (size_t)bytes);
+    launch_export_bricks(C.interior.p, C.apron_buf.p, g->atlas_last, C.esize, g->xfer.p, g->stream);
+    g->check_launch("export bricks");
+    g->check(cudaMemcpyAsync(host_out, g->xfer.p, (size_t)bytes, cudaMemcpyDeviceToHost, g->stream), "export atlas");
+    g->sync();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_atlas_map(gbvdb_grid g, void* host_out, int64_t cap) {
+    GBVDB_GUARD(g)
+    if (!host_out) return GBVDB_INVALID_ARG;
+    if (cap < g->amap_slots) return GBVDB_CAPACITY;
+    if (g->amap_slots == 0) return GBVDB_OK;
+    g->check(cudaMemcpyAsync(host_out, g->amap.p, (size_t)g->amap_slots * 16, cudaMemcpyDeviceToHost, g->stream),
+             "export map");
+    g->sync();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int64_t cap_offsets, float* points,
+                                   int64_t cap_points) {
+    GBVDB_GUARD(g)
+    if (!g->sc_valid) return GBVDB_INVALID_ARG;
+    long long nsub = g->sc_nbricks * 64;
+    if (cap_offsets < nsub + 1 || cap_points < g->sc_len) return GBVDB_CAPACITY;
+    g->materialize_lists();
+    std::vector<uint32_t> off((size_t)nsub + 1);
+    g->check(cudaMemcpyAsync(off.data(), g->list_off.p, (size_t)(nsub + 1) * 4, cudaMemcpyDeviceToHost, g->stream),
+             "export offsets");
+    if (g->sc_len > 0 && points)
+        g->check(cudaMemcpyAsync(points, g->list_pts.p, (size_t)g->sc_len * 12, cudaMemcpyDeviceToHost, g->stream),
+                 "export points");
+    g->sync();
+    if (offsets)
+        for (long long i = 0; i <= nsub; i++) offsets[i] = off[(size_t)i];
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !out) return GBVDB_INVALID_ARG;
+    g->grow(g->misc, 256);
+    double* d = reinterpret_cast<double*>(g->ptr<char>(g->misc) + 192);
+    g->check(cudaMemsetAsync(d, 0, 8, g->stream), "checksum clear");
+    launch_checksum(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p, d,
+                    g->stream);
+    g->check_launch("checksum");
+    g->readback(out, d, 8);
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
+    if (interior) *interior = g->ch[chan].interior.p;
+    if (apron) *apron = g->ch[chan].apron_buf.p;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable) {
+    GBVDB_GUARD(g)
+    g->profile = enable != 0;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4) {
+    GBVDB_GUARD(g)
+    if (!out4) return GBVDB_INVALID_ARG;
+    out4[0] = g->n_launch;
+    out4[1] = g->n_readback;
+    out4[2] = g->sc_len;
+    out4[3] = g->sc_nbricks;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap) {
+    GBVDB_GUARD(g)
+    if (!ms) return GBVDB_INVALID_ARG;
+    int n = std::min<int>(cap, (int)g->stage_ms.size());
+    for (int i = 0; i < n; i++) ms[i] = g->stage_ms[(size_t)i];
+    for (int i = n; i < cap; i++) ms[i] = -1;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+// kernels.h -- host-side launchers of the libgbvdb kernels (one declaration per launcher).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace gbvdb {
+
+// Key-domain of one level: node coordinates [lo, lo+dim) per axis, bit offset into
+// the level bitmaps (x-major linear index so that bit order == key sort order).
+struct KeyDomain {
+    int lo[3];
+    int dim[3];
+    long long bitbase;   // first bit of this level
+    long long nbits;
+};
+struct KeyDomains {
+    KeyDomain d[kMaxLev];
+};
+
+struct PointSrc {
+    const char* base;
+    long long n;
+    int stride;
+    int off;
+};
+
+// ---- scan.cu
+size_t scan_tmp_bytes(long long n);
+// exclusive scan of n u32 into out[0..n]; out[n] = total.  tmp: scan_tmp_bytes(n) bytes
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+
+// ---- topology.cu
+void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s);
+void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
+                       uint32_t* bitmap, int* err, cudaStream_t s);
+void launch_keys_box(const TreeView& t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
+                     int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
+                     int* err, cudaStream_t s);
+void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s);
+void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
+                        int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
+void launch_write_node(Node* dst, const Node& v, cudaStream_t s);
+void launch_link(const TreeView& t, int lev, long long count, cudaStream_t s);
+void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s);
+void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s);
+void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s);
+void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s);
+void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s);
+void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s);
+
+// ---- atlas.cu
+// flag[i] = (mode 0: node.flags != 0, mode 1: node.parent != UNDEF64)
+void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag, cudaStream_t s);
+void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
+                         cudaStream_t s);
+void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s);
+void launch_apron(const TreeView& t, const AtlasNode* amap, int used, int ax, int ay, int esize,
+                  const void* interior, void* apron, uint32_t boundbits, cudaStream_t s);
+void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out,
+                          cudaStream_t s);
+void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* interior, double* out,
+                     cudaStream_t s);
+void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value,
+                          cudaStream_t s);
+
+// ---- points.cu
+void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s);
+void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                      uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals,
+                      cudaStream_t s);
+void launch_bin_scatter(PointSrc p, float3 trans, const int* bin_of, const uint32_t* rank_of,
+                        const uint32_t* bin_off, float4* sorted, cudaStream_t s);
+
+struct GatherParams {
+    int mode;          // 0 density, 1 level set
+    int accum;
+    float rho;         // gather radius
+    float R;           // subcell insert radius (membership)
+    uint32_t tbits;    // static cutoff on squared distance (float bits)
+    int dtype;         // storage type
+    int ax, ay;        // atlas axis counts
+    int lo_off, hi_off;  // home-bin offset range H - S (subcell units)
+};
+void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
+                   const uint32_t* bin_off, const float4* pts, const GatherParams& gp, void* interior,
+                   cudaStream_t s);
+// materialized subcell lists (export and the fallback gather)
+void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                       uint32_t* cnt, cudaStream_t s);
+void launch_list_fill(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                      const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s);
+void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
+                         const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s);
+
+}  // namespace gbvdb

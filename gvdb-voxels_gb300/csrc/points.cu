@@ -1,0 +1,432 @@
+// points.cu -- InsertPointsSubcell binning and the GatherDensity / GatherLevelSet kernels.
+//
+// Replaces (reference file:line):
+//   gvdbSetFlagSubcell + PrefixSum (sc_mapping)       PT.cuh:109-118, VG.cpp:4988-4996
+//   gvdbCountSubcell / gvdbInsertSubcell              PT.cuh:218-315
+//   gvdbCalcSubcellPos                                PT.cuh:677-694
+//   gvdbGatherDensity / gvdbGatherLevelSet            PT.cuh:696-773
+//
+// Subcell membership is the reference's rule: point w (after +trans, all
+// coordinates >= 0, z != NOHIT) belongs to subcell S of a linked leaf iff on every
+// axis  int(w - R)/4*4 <= S <= int(w + 1 + R)/4*4  (C truncation, FP32).
+// The reference copies each point into every member subcell's list (~34 copies
+// at R = 4) and then re-reads those lists.  Here each point is binned once, by
+// its home subcell (the subcell containing floor(w)), with a counting sort; the
+// gather of a brick pulls the home bins of its 3x3x3 brick neighbourhood and
+// applies the membership rule per (point, subcell).  The value of a voxel is a
+// max / min over its subcell's members, so it does not depend on visiting order:
+//   density   max(0, max_j (rho - |p_j - v|)) = max(0, rho - sqrt(min_j d_j^2))
+//   level set min(3, min_j (|p_j - v| - rho)) = min(3, sqrt(min_j d_j^2) - rho)
+// (sqrt and the subtraction are monotonic under round-to-nearest, so both forms
+// round identically).  The kernels reduce min d^2 per voxel.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "kernels.h"
+
+namespace gbvdb {
+
+namespace {
+
+constexpr int kSc = 4;  // subcell size (voxels)
+
+__device__ __forceinline__ void sc_range(float w, float R, int& lo, int& hi) {
+    lo = ((int)fsub(w, R)) / kSc * kSc;
+    hi = ((int)fadd(fadd(w, 1.0f), R)) / kSc * kSc;
+}
+
+__device__ __forceinline__ bool load_valid(PointSrc p, long long i, float3 trans, float& x, float& y, float& z) {
+    load_pos(p.base, i, p.stride, p.off, x, y, z);
+    if (z == kNoHit) return false;  // PT.cuh:282, tested before +trans
+    x = fadd(x, trans.x);
+    y = fadd(y, trans.y);
+    z = fadd(z, trans.z);
+    return !(x < 0 || y < 0 || z < 0);
+}
+
+__global__ void k_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (leaves[i].parent != kUndef64) linked[scmap[i]] = (int)i;
+}
+
+__device__ __forceinline__ long long linked_leaf(const TreeView& t, int x, int y, int z) {
+    long long l = get_pos_leaf(t, x, y, z);
+    if (l < 0 || t.nodes[0][l].parent == kUndef64) return -1;
+    return l;
+}
+
+// Home-subcell counting pass + total subcell-list length (the reference's
+// pSCPntsLength) + orphans (valid points whose home leaf is not linked).
+__global__ void k_bin_count(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* __restrict__ scmap,
+                           uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
+    unsigned long long members = 0, orphans = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float w[3];
+        if (!load_valid(p, i, trans, w[0], w[1], w[2])) { bin_of[i] = -1; continue; }
+        int h[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) h[a] = ((int)w[a]) & ~(kSc - 1);
+        long long leaf = linked_leaf(t, h[0], h[1], h[2]);
+        if (leaf < 0) {
+            bin_of[i] = -2;
+            orphans++;
+        } else {
+            const Node& nd = t.nodes[0][leaf];
+            int loc = (((h[2] - nd.pos[2]) >> 2) << 4) | (((h[1] - nd.pos[1]) >> 2) << 2) | ((h[0] - nd.pos[0]) >> 2);
+            unsigned bin = scmap[leaf] * 64u + (unsigned)loc;
+            rank_of[i] = atomicAdd(bin_cnt + bin, 1u);
+            bin_of[i] = (int)bin;
+        }
+        // number of (subcell, point) list entries this point creates
+        int lo[3], hi[3];
+        bool any = true;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            sc_range(w[a], R, lo[a], hi[a]);
+            if (lo[a] < 0) lo[a] = 0;  // guard: negative subcells are skipped
+            if (hi[a] < lo[a]) any = false;
+        }
+        if (!any) continue;
+        for (int bx = lo[0] >> 4; bx <= hi[0] >> 4; bx++) {
+            int x0 = max(lo[0], bx << 4), x1 = min(hi[0], (bx << 4) + 12);
+            for (int by = lo[1] >> 4; by <= hi[1] >> 4; by++) {
+                int y0 = max(lo[1], by << 4), y1 = min(hi[1], (by << 4) + 12);
+                for (int bz = lo[2] >> 4; bz <= hi[2] >> 4; bz++) {
+                    int z0 = max(lo[2], bz << 4), z1 = min(hi[2], (bz << 4) + 12);
+                    if (linked_leaf(t, bx << 4, by << 4, bz << 4) < 0) continue;
+                    members += (unsigned long long)(((x1 - x0) >> 2) + 1) * (((y1 - y0) >> 2) + 1) * (((z1 - z0) >> 2) + 1);
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        members += __shfl_down_sync(0xFFFFFFFFu, members, o);
+        orphans += __shfl_down_sync(0xFFFFFFFFu, orphans, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (members) atomicAdd(totals, members);
+        if (orphans) atomicAdd(totals + 1, orphans);
+    }
+}
+
+__global__ void k_bin_scatter(PointSrc p, float3 trans, const int* __restrict__ bin_of, const uint32_t* __restrict__ rank_of,
+                              const uint32_t* __restrict__ bin_off, float4* __restrict__ sorted) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        int b = bin_of[i];
+        if (b < 0) continue;
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        sorted[bin_off[b] + rank_of[i]] = make_float4(fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z), 0.f);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ float ld_f32(const T* p);
+template <>
+__device__ __forceinline__ float ld_f32<float>(const float* p) { return *p; }
+template <>
+__device__ __forceinline__ float ld_f32<__half>(const __half* p) { return __half2float(*p); }
+template <>
+__device__ __forceinline__ float ld_f32<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+template <typename T>
+__device__ __forceinline__ T cvt_out(float v);
+template <>
+__device__ __forceinline__ float cvt_out<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __half cvt_out<__half>(float v) { return __float2half_rn(v); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 cvt_out<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// final voxel value from min squared distance m
+__device__ __forceinline__ float finish(const GatherParams& gp, float m, float old) {
+    float c = __fsqrt_rn(m);
+    if (gp.mode == 0) {
+        float base = gp.accum ? old : 0.0f;
+        return fmaxf(base, fsub(gp.rho, c));
+    }
+    float base = gp.accum ? old : 3.0f;
+    return fminf(base, fsub(c, gp.rho));
+}
+
+// write the brick's 4096 voxel values from the min-d^2 tile (coalesced, 4 voxels per access)
+template <typename T>
+__device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out) {
+    for (int v4 = threadIdx.x; v4 < 1024; v4 += blockDim.x) {
+        float r[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int v = v4 * 4 + k;
+            float old = gp.accum ? ld_f32<T>(out + v) : 0.f;
+            r[k] = finish(gp, __uint_as_float(tile[v]), old);
+        }
+        if constexpr (sizeof(T) == 4) {
+            reinterpret_cast<float4*>(out)[v4] = make_float4(r[0], r[1], r[2], r[3]);
+        } else {
+            T h[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) h[k] = cvt_out<T>(r[k]);
+            uint2 pk;
+            pk.x = (uint32_t)(*reinterpret_cast<uint16_t*>(&h[0])) | ((uint32_t)(*reinterpret_cast<uint16_t*>(&h[1])) << 16);
+            pk.y = (uint32_t)(*reinterpret_cast<uint16_t*>(&h[2])) | ((uint32_t)(*reinterpret_cast<uint16_t*>(&h[3])) << 16);
+            reinterpret_cast<uint2*>(out)[v4] = pk;
+        }
+    }
+}
+
+constexpr int kGatherThreads = 256;
+constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 15 -> offsets within +-1 brick)
+
+// One block per linked leaf.  Candidate home bins of the 3x3x3 brick
+// neighbourhood are collected in shared memory; warps take bins, lanes take 32
+// points of a bin at a time, and for every point every lane evaluates 2 voxels
+// of each member subcell of this brick, reducing min d^2 into a shared tile
+// with shared-memory atomics.  One coalesced write of the brick at the end.
+template <typename T>
+__global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int* __restrict__ linked,
+                                                           const uint32_t* __restrict__ scmap,
+                                                           const uint32_t* __restrict__ bin_off,
+                                                           const float4* __restrict__ pts, GatherParams gp,
+                                                           T* __restrict__ interior) {
+    __shared__ uint32_t tile[4096];
+    __shared__ int nrank[27];
+    __shared__ uint32_t cb_beg[kMaxBins];
+    __shared__ uint32_t cb_cnt[kMaxBins];
+    __shared__ int ncb;
+    __shared__ int cursor;
+
+    const int leaf = linked[blockIdx.x];
+    const Node nd = t.nodes[0][leaf];
+    const int slot = slot_of_value(nd.value, gp.ax, gp.ay);
+    if (slot < 0) return;
+    const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+
+    for (int v = threadIdx.x; v < 4096; v += blockDim.x) tile[v] = gp.tbits;
+    if (threadIdx.x < 27) {
+        int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
+        int r = -1;
+        if ((dx | dy | dz) == 0) {
+            r = (int)scmap[leaf];
+        } else {
+            int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
+            if (px >= 0 && py >= 0 && pz >= 0) {
+                long long l = linked_leaf(t, px, py, pz);
+                if (l >= 0) r = (int)scmap[l];
+            }
+        }
+        nrank[threadIdx.x] = r;
+    }
+    if (threadIdx.x == 0) { ncb = 0; cursor = 0; }
+    __syncthreads();
+
+    // candidate home bins: H (in subcells) within [S + lo_off, S + hi_off] of some S of this brick
+    const int sx0 = ox >> 2, sy0 = oy >> 2, sz0 = oz >> 2;
+    const int span = 4 + gp.hi_off - gp.lo_off;  // candidates per axis
+    const int ncand = span * span * span;
+    for (int c = threadIdx.x; c < ncand; c += blockDim.x) {
+        int cx = c % span, cy = (c / span) % span, cz = c / (span * span);
+        int hx = sx0 + gp.lo_off + cx, hy = sy0 + gp.lo_off + cy, hz = sz0 + gp.lo_off + cz;
+        if (hx < 0 || hy < 0 || hz < 0) continue;
+        int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
+        if (bx < -1 || bx > 1 || by < -1 || by > 1 || bz < -1 || bz > 1) continue;
+        int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
+        if (r < 0) continue;
+        unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
+        uint32_t b = bin_off[bin], e = bin_off[bin + 1];
+        if (e > b) {
+            int k = atomicAdd(&ncb, 1);
+            cb_beg[k] = b;
+            cb_cnt[k] = e - b;
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int vx = lane & 3, vy = (lane >> 2) & 3, vz = lane >> 4;
+    const float fvx = (float)vx, fvy = (float)vy;
+    const int nb = ncb;
+    while (true) {
+        int e = 0;
+        if (lane == 0) e = atomicAdd(&cursor, 1);
+        e = __shfl_sync(0xFFFFFFFFu, e, 0);
+        if (e >= nb) break;
+        const uint32_t beg = cb_beg[e], cnt = cb_cnt[e];
+        for (uint32_t base = 0; base < cnt; base += 32) {
+            const int nv = (int)min(32u, cnt - base);
+            float4 q = make_float4(0, 0, 0, 0);
+            int box = 0;  // packed member range of this brick: lx0,lx1,ly0,ly1,lz0,lz1 (2 bits each), bit 12 = empty
+            if (lane < nv) {
+                q = pts[beg + base + lane];
+                int lo, hi, rng[6];
+                bool empty = false;
+                const float w3[3] = {q.x, q.y, q.z};
+                const int o3[3] = {ox, oy, oz};
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    sc_range(w3[a], gp.R, lo, hi);
+                    int l0 = lo <= o3[a] ? 0 : (lo - o3[a]) >> 2;
+                    int l1 = hi < o3[a] ? -1 : min(3, (hi - o3[a]) >> 2);
+                    if (l0 > 3 || l1 < l0) empty = true;
+                    rng[2 * a] = l0;
+                    rng[2 * a + 1] = l1;
+                }
+                box = empty ? (1 << 12)
+                            : (rng[0] | (rng[1] << 2) | (rng[2] << 4) | (rng[3] << 6) | (rng[4] << 8) | (rng[5] << 10));
+            } else {
+                box = 1 << 12;
+            }
+            unsigned live = __ballot_sync(0xFFFFFFFFu, (box & (1 << 12)) == 0);
+            while (live) {
+                const int j = __ffs(live) - 1;
+                live &= live - 1;
+                const float px = __shfl_sync(0xFFFFFFFFu, q.x, j);
+                const float py = __shfl_sync(0xFFFFFFFFu, q.y, j);
+                const float pz = __shfl_sync(0xFFFFFFFFu, q.z, j);
+                const int bxv = __shfl_sync(0xFFFFFFFFu, box, j);
+                const int lx0 = bxv & 3, lx1 = (bxv >> 2) & 3, ly0 = (bxv >> 4) & 3, ly1 = (bxv >> 6) & 3;
+                const int lz0 = (bxv >> 8) & 3, lz1 = (bxv >> 10) & 3;
+                for (int lz = lz0; lz <= lz1; lz++) {
+                    const float z0 = (float)(oz + 4 * lz + vz), z1 = (float)(oz + 4 * lz + vz + 2);
+                    const float dz0 = fsub(pz, z0), dz1 = fsub(pz, z1);
+                    for (int ly = ly0; ly <= ly1; ly++) {
+                        const float dy = fsub(py, (float)(oy + 4 * ly) + fvy);
+                        for (int lx = lx0; lx <= lx1; lx++) {
+                            const float dx = fsub(px, (float)(ox + 4 * lx) + fvx);
+                            const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                            const float d0 = __fmaf_rn(dz0, dz0, dxy);
+                            const float d1 = __fmaf_rn(dz1, dz1, dxy);
+                            const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
+                            const uint32_t b0 = __float_as_uint(d0), b1 = __float_as_uint(d1);
+                            if (b0 < gp.tbits) atomicMin(&tile[v0], b0);
+                            if (b1 < gp.tbits) atomicMin(&tile[v0 + 512], b1);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    write_tile<T>(gp, tile, interior + (size_t)slot * 4096);
+}
+
+// ---- materialized subcell lists (reference-shaped; export + fallback) ----
+
+template <bool kFill>
+__device__ void list_points(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                            uint32_t* cnt, const uint32_t* off, float* out3) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float w[3];
+        if (!load_valid(p, i, trans, w[0], w[1], w[2])) continue;
+        int lo[3], hi[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) sc_range(w[a], R, lo[a], hi[a]);
+        for (int sx = lo[0]; sx <= hi[0]; sx += kSc)
+            for (int sy = lo[1]; sy <= hi[1]; sy += kSc)
+                for (int sz = lo[2]; sz <= hi[2]; sz += kSc) {
+                    if (sx < 0 || sy < 0 || sz < 0) continue;
+                    long long leaf = linked_leaf(t, sx, sy, sz);
+                    if (leaf < 0) continue;
+                    const Node& nd = t.nodes[0][leaf];
+                    int loc = (((sz - nd.pos[2]) >> 2) << 4) | (((sy - nd.pos[1]) >> 2) << 2) | ((sx - nd.pos[0]) >> 2);
+                    unsigned idx = scmap[leaf] * 64u + (unsigned)loc;
+                    unsigned k = atomicAdd(cnt + idx, 1u);
+                    if (kFill) {
+                        float* o = out3 + 3ull * (off[idx] + k);
+                        o[0] = w[0];
+                        o[1] = w[1];
+                        o[2] = w[2];
+                    }
+                }
+    }
+}
+__global__ void k_list_count(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* cnt) {
+    list_points<false>(t, p, trans, R, scmap, cnt, nullptr, nullptr);
+}
+__global__ void k_list_fill(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* scmap, const uint32_t* off,
+                            uint32_t* cursor, float* out3) {
+    list_points<true>(t, p, trans, R, scmap, cursor, off, out3);
+}
+
+// reference-shaped gather over materialized lists: one block per linked leaf,
+// thread per voxel (16 voxels per thread), each voxel scans its subcell's list
+template <typename T>
+__global__ void k_gather_lists(TreeView t, const int* __restrict__ linked, const uint32_t* __restrict__ off,
+                               const float* __restrict__ pts3, GatherParams gp, T* __restrict__ interior) {
+    __shared__ uint32_t tile[4096];
+    const int leaf = linked[blockIdx.x];
+    const Node nd = t.nodes[0][leaf];
+    const int slot = slot_of_value(nd.value, gp.ax, gp.ay);
+    if (slot < 0) return;
+    for (int v = threadIdx.x; v < 4096; v += blockDim.x) {
+        int x = v & 15, y = (v >> 4) & 15, z = v >> 8;
+        int s = ((z >> 2) << 4) | ((y >> 2) << 2) | (x >> 2);
+        unsigned idx = blockIdx.x * 64u + (unsigned)s;
+        float fx = (float)(nd.pos[0] + x), fy = (float)(nd.pos[1] + y), fz = (float)(nd.pos[2] + z);
+        uint32_t m = gp.tbits;
+        for (uint32_t j = off[idx]; j < off[idx + 1]; j++) {
+            float dx = fsub(pts3[3ull * j], fx), dy = fsub(pts3[3ull * j + 1], fy), dz = fsub(pts3[3ull * j + 2], fz);
+            float d = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            m = min(m, __float_as_uint(d));
+        }
+        tile[v] = m;
+    }
+    __syncthreads();
+    write_tile<T>(gp, tile, interior + (size_t)slot * 4096);
+}
+
+inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+inline unsigned gs_blocks(long long n, int t) {
+    long long b = (n + t - 1) / t;
+    long long cap = 152LL * 16;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+}  // namespace
+
+void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s) {
+    if (n <= 0) return;
+    k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
+}
+void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* bin_cnt,
+                      int* bin_of, uint32_t* rank_of, unsigned long long* totals, cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, p, trans, R, scmap, bin_cnt, bin_of, rank_of, totals);
+}
+void launch_bin_scatter(PointSrc p, float3 trans, const int* bin_of, const uint32_t* rank_of, const uint32_t* bin_off,
+                        float4* sorted, cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, bin_of, rank_of, bin_off, sorted);
+}
+void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
+                   const uint32_t* bin_off, const float4* pts, const GatherParams& gp, void* interior, cudaStream_t s) {
+    if (nbricks <= 0) return;
+    if (gp.dtype == 3)
+        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp, (float*)interior);
+    else if (gp.dtype == 100)
+        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp, (__half*)interior);
+    else
+        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp,
+                                                                            (__nv_bfloat16*)interior);
+}
+void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* cnt,
+                       cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, p, trans, R, scmap, cnt);
+}
+void launch_list_fill(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, const uint32_t* off,
+                      uint32_t* cursor, float* out3, cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, p, trans, R, scmap, off, cursor, out3);
+}
+void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
+                         const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s) {
+    if (nbricks <= 0) return;
+    if (gp.dtype == 3)
+        k_gather_lists<float><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp, (float*)interior);
+    else if (gp.dtype == 100)
+        k_gather_lists<__half><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp, (__half*)interior);
+    else
+        k_gather_lists<__nv_bfloat16><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp,
+                                                                       (__nv_bfloat16*)interior);
+}
+
+}  // namespace gbvdb

@@ -1,0 +1,337 @@
+// topology.cu -- bounding box, per-level node keys, node allocation, linking.
+//
+// Replaces (reference file:line):
+//   GetBoundingBox + gvdbSplitPos + 6 Thrust min/max   VG.cpp:5404-5467, ND.cuh:507-517
+//   gvdbCalcBrickId + Thrust sort + FindUnique/Compact  PT.cuh:352-382, 336-350, 934-943
+//   gvdbCalcExtraBrickId                                PT.cuh:467-512
+//   gvdbCalcIncreExtraBrickId (+ node markers)          PT.cuh:420-465
+//   host node-allocation loop                           VG.cpp:1288-1332, 958-989, 1087-1112
+//   gvdbLinkBricks / gvdbDelinkLeafBricks / gvdbDelinkBricks  ND.cuh:401-505
+//
+// Keys are deduplicated in per-level bitmaps over the key domain instead of a
+// 64-bit sort: bit i of a level's bitmap is node coordinate (x,y,z) with
+// i = ((x-lo)*ny + (y-lo))*nz + (z-lo), so ascending bit order equals the
+// reference's ascending u64 key order {lev, x, y, z} and a popcount prefix sum
+// gives each unique key its pool slot directly.
+#include "kernels.h"
+
+namespace gbvdb {
+
+namespace {
+
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    return v;
+}
+
+__global__ void k_bbox(PointSrc p, float3 orig, int* out6) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
+#pragma unroll
+        for (int a = 0; a < 3; a++) { mn[a] = fminf(mn[a], w[a]); mx[a] = fmaxf(mx[a], w[a]); }
+    }
+    __shared__ float red[6][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; a++) { mn[a] = warp_min(mn[a]); mx[a] = warp_max(mx[a]); }
+    if (lane == 0)
+        for (int a = 0; a < 3; a++) { red[a][warp] = mn[a]; red[3 + a][warp] = mx[a]; }
+    __syncthreads();
+    if (warp == 0) {
+        for (int a = 0; a < 3; a++) {
+            float v0 = lane < nw ? red[a][lane] : INFINITY;
+            float v1 = lane < nw ? red[3 + a][lane] : -INFINITY;
+            v0 = warp_min(v0);
+            v1 = warp_max(v1);
+            if (lane == 0) {
+                atomicMin(out6 + a, f2o(v0));
+                atomicMax(out6 + 3 + a, f2o(v1));
+            }
+        }
+    }
+}
+
+// set bit `idx` of the bitmap, skipping the atomic when the bit is already visible
+__device__ __forceinline__ void set_bit(uint32_t* bm, long long idx) {
+    uint32_t* w = bm + (idx >> 5);
+    uint32_t bit = 1u << (idx & 31);
+    if ((__ldcg(w) & bit) == 0) atomicOr(w, bit);
+}
+
+__device__ __forceinline__ long long key_bit(const KeyDomain& d, int x, int y, int z) {
+    int rx = x - d.lo[0], ry = y - d.lo[1], rz = z - d.lo[2];
+    if (rx < 0 || ry < 0 || rz < 0 || rx >= d.dim[0] || ry >= d.dim[1] || rz >= d.dim[2]) return -1;
+    return d.bitbase + ((long long)rx * d.dim[1] + ry) * d.dim[2] + rz;
+}
+
+// gvdbCalcBrickId (PT.cuh:352-382): key of every level below the root for every
+// point whose coordinates are all >= 0
+__global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom, TreeView tv, uint32_t* bm, int* err) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        float w0 = fadd(x, orig.x), w1 = fadd(y, orig.y), w2 = fadd(z, orig.z);
+        if (w0 < 0 || w1 < 0 || w2 < 0) continue;
+        for (int lev = 0; lev < depth; lev++) {
+            int lg = tv.lgrange[lev];
+            long long b = key_bit(dom.d[lev], cover_coord(w0, lg), cover_coord(w1, lg), cover_coord(w2, lg));
+            if (b < 0) { atomicOr(err, 1); continue; }
+            set_bit(bm, b);
+        }
+    }
+}
+
+// gvdbCalcExtraBrickId (hi_mul = 2, PT.cuh:467-512) and gvdbCalcIncreExtraBrickId
+// (hi_mul = 1, PT.cuh:420-465): every node position in the point's box that is not
+// reachable from the root becomes a key; reachable leaves are marked (incremental).
+__global__ void k_keys_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
+                           int3 rlo, int3 rhi, KeyDomains dom, uint32_t* bm, int* markers, int* err) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
+        if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
+        int bmin[3], bmax[3];
+        float hr = hi_mul == 2 ? __fmul_rn(2.0f, radius) : radius;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            float fi = (float)(int)w[a];
+            bmin[a] = (int)fsub(fi, radius);
+            bmax[a] = (int)fadd(fi, hr);
+        }
+        for (int lev = 0; lev < depth; lev++) {
+            int rr = 1 << t.lgrange[lev];
+            int lo[3], hi[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                lo[a] = bmin[a] / rr * rr;
+                hi[a] = bmax[a] / rr * rr;
+            }
+            for (int nx = lo[0]; nx <= hi[0]; nx += rr)
+                for (int ny = lo[1]; ny <= hi[1]; ny += rr)
+                    for (int nz = lo[2]; nz <= hi[2]; nz += rr) {
+                        // guard: positions outside the root (the reference aliases them)
+                        if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
+                        long long pid = get_pos_parent(t, nx, ny, nz, lev);
+                        if (pid < 0) {
+                            long long b = key_bit(dom.d[lev], nx >> t.lgrange[lev], ny >> t.lgrange[lev], nz >> t.lgrange[lev]);
+                            if (b < 0) { atomicOr(err, 1); continue; }
+                            set_bit(bm, b);
+                        } else if (lev == 0 && markers) {
+                            markers[pid] = 1;
+                        }
+                    }
+        }
+    }
+}
+
+__global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32_t* __restrict__ cnt) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += (long long)gridDim.x * blockDim.x)
+        cnt[i] = __popc(bm[i]);
+}
+
+// one thread per bitmap word of one level; every set bit becomes a node record
+// (SetupNode, VG.cpp:2512-2524) at pool index base + rank
+__global__ void k_alloc_nodes(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ prefix, long long word0,
+                              long long nwords, int lev, int lgrange, KeyDomain d, long long base, Node* nodes) {
+    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nwords) return;
+    uint32_t bits = bm[word0 + w];
+    if (!bits) return;
+    long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0];
+    long long level_bit0 = d.bitbase;  // bitbase is word aligned
+    while (bits) {
+        int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        long long li = (word0 + w) * 32 + b - level_bit0;
+        int rz = (int)(li % d.dim[2]);
+        long long q = li / d.dim[2];
+        int ry = (int)(q % d.dim[1]);
+        int rx = (int)(q / d.dim[1]);
+        long long idx = base + rank;
+        rank++;
+        Node n;
+        n.lev = (uint8_t)lev;
+        n.flags = 1;
+        n.prio = 0;
+        n.pad = 0;
+        n.pos[0] = (d.lo[0] + rx) << lgrange;
+        n.pos[1] = (d.lo[1] + ry) << lgrange;
+        n.pos[2] = (d.lo[2] + rz) << lgrange;
+        n.value[0] = n.value[1] = n.value[2] = -1;
+        n.vrange[0] = n.vrange[1] = n.vrange[2] = 0.f;
+        n.parent = kUndefL;
+        n.childlist = lev > 0 ? elem(1, lev, (unsigned long long)idx) : kUndefL;
+        n.mask = 0;
+        nodes[idx] = n;
+    }
+}
+
+__global__ void k_write_node(Node* dst, Node v) { *dst = v; }
+
+// gvdbLinkBricks (ND.cuh:470-505)
+__global__ void k_link(TreeView t, int lev, long long count) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    Node* node = t.nodes[lev] + i;
+    if (!node->flags) return;
+    long long pid = get_parent(t, lev + 1, node->pos[0], node->pos[1], node->pos[2]);
+    if (pid < 0) return;
+    const Node* pn = t.nodes[lev + 1] + pid;
+    int sh = t.lgrange[lev + 1] - t.lgres[lev + 1];
+    int r = t.res[lev + 1];
+    long long px = ((long long)node->pos[0] - pn->pos[0]) >> sh;
+    long long py = ((long long)node->pos[1] - pn->pos[1]) >> sh;
+    long long pz = ((long long)node->pos[2] - pn->pos[2]) >> sh;
+    if (px > r || px < 0 || py > r || py < 0 || pz > r || pz < 0) return;
+    int b = (int)((pz * r + py) * r + px);
+    node->parent = ((unsigned long long)pid << 16) | ((unsigned long long)(lev + 1) << 8);
+    unsigned long long cndx = pn->childlist >> 16;
+    if ((long long)cndx >= t.ncnt[lev + 1]) return;
+    t.clist[lev + 1][(cndx << (3 * t.lgres[lev + 1])) + b] = ((unsigned long long)i << 16) | ((unsigned long long)lev << 8);
+}
+
+__global__ void k_init_markers(const Node* leaves, long long n, int* markers, int accum) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) markers[i] = accum ? (int)leaves[i].flags : 0;
+}
+
+__global__ void k_apply_markers(Node* leaves, long long n, const int* markers) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) leaves[i].flags = (uint8_t)markers[i];
+}
+
+// gvdbDelinkLeafBricks (ND.cuh:401-429)
+__global__ void k_delink_leaf(TreeView t, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Node* node = t.nodes[0] + i;
+    if (node->flags) return;
+    if (node->parent == kUndef64) return;
+    long long pid = get_parent(t, 1, node->pos[0], node->pos[1], node->pos[2]);
+    if (pid < 0) { node->parent = kUndef64; return; }
+    const Node* pn = t.nodes[1] + pid;
+    int sh = t.lgrange[1] - t.lgres[1];
+    int r = t.res[1];
+    long long px = ((long long)node->pos[0] - pn->pos[0]) >> sh;
+    long long py = ((long long)node->pos[1] - pn->pos[1]) >> sh;
+    long long pz = ((long long)node->pos[2] - pn->pos[2]) >> sh;
+    int b = (int)((pz * r + py) * r + px);
+    node->parent = kUndef64;
+    unsigned long long cndx = pn->childlist >> 16;
+    t.clist[1][(cndx << (3 * t.lgres[1])) + b] = kUndef64;
+}
+
+// gvdbDelinkBricks (ND.cuh:431-467)
+__global__ void k_delink_upper(TreeView t, int lev, long long n) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Node* node = t.nodes[lev] + i;
+    if (node->parent == kUndef64) { node->flags = 0; return; }
+    const unsigned long long* cl = t.clist[lev] + ((unsigned long long)i << (3 * t.lgres[lev]));
+    const int len = 1 << (3 * t.lgres[lev]);
+    for (int k = 0; k < len; k++)
+        if (cl[k] != kUndef64) { node->flags = 1; return; }
+    node->flags = 0;
+    long long pid = get_parent(t, lev + 1, node->pos[0], node->pos[1], node->pos[2]);
+    if (pid < 0) { node->parent = kUndef64; return; }
+    const Node* pn = t.nodes[lev + 1] + pid;
+    int sh = t.lgrange[lev + 1] - t.lgres[lev + 1];
+    int r = t.res[lev + 1];
+    long long px = ((long long)node->pos[0] - pn->pos[0]) >> sh;
+    long long py = ((long long)node->pos[1] - pn->pos[1]) >> sh;
+    long long pz = ((long long)node->pos[2] - pn->pos[2]) >> sh;
+    int b = (int)((pz * r + py) * r + px);
+    node->parent = kUndef64;
+    unsigned long long cndx = pn->childlist >> 16;
+    t.clist[lev + 1][(cndx << (3 * t.lgres[lev + 1])) + b] = kUndef64;
+}
+
+__global__ void k_count_flags(const Node* nodes, long long n, unsigned long long* out) {
+    unsigned c = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        c += nodes[i].flags ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+}
+
+// ComputeBounds (VG.cpp:1792-1816): min corner / max corner of flagged leaves
+__global__ void k_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !leaves[i].flags) return;
+    for (int a = 0; a < 3; a++) {
+        atomicMin(out6 + a, leaves[i].pos[a]);
+        atomicMax(out6 + 3 + a, leaves[i].pos[a] + (1 << lgrange0));
+    }
+}
+
+inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+inline unsigned grid_stride_blocks(long long n, int t) {
+    long long b = (n + t - 1) / t;
+    long long cap = 152LL * 16;
+    return (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+}  // namespace
+
+void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s) {
+    k_bbox<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, out6);
+}
+void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
+                       uint32_t* bitmap, int* err, cudaStream_t s) {
+    k_keys_pass1<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, depth, dom, t, bitmap, err);
+}
+void launch_keys_box(const TreeView& t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
+                     int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
+                     int* err, cudaStream_t s) {
+    int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
+    int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
+    k_keys_box<<<grid_stride_blocks(p.n, 128), 128, 0, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
+                                                             bitmap, markers, err);
+}
+void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s) {
+    if (nwords <= 0) return;
+    k_popc<<<grid_stride_blocks(nwords, 256), 256, 0, s>>>(bm, nwords, cnt);
+}
+void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
+                        int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
+    if (nwords <= 0) return;
+    k_alloc_nodes<<<blocks_for(nwords, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
+}
+void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<1, 1, 0, s>>>(dst, v); }
+void launch_link(const TreeView& t, int lev, long long count, cudaStream_t s) {
+    if (count <= 0) return;
+    k_link<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count);
+}
+void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s) {
+    if (n <= 0) return;
+    k_init_markers<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, markers, accum);
+}
+void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s) {
+    if (n <= 0) return;
+    k_apply_markers<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, markers);
+}
+void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_delink_leaf<<<blocks_for(n, 256), 256, 0, s>>>(t, n);
+}
+void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_delink_upper<<<blocks_for(n, 128), 128, 0, s>>>(t, lev, n);
+}
+void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_count_flags<<<grid_stride_blocks(n, 256), 256, 0, s>>>(nodes, n, out);
+}
+void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s) {
+    if (n <= 0) return;
+    k_leaf_bounds<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, lgrange0, out6);
+}
+
+}  // namespace gbvdb

@@ -1,0 +1,302 @@
+"""ctypes binding of libgbvdb.so (include/gbvdb.h).
+
+`Grid` mirrors the reference class nvdb::VolumeGVDB for the point-driven path
+(source/gvdb_library/src/gvdb_volume_gvdb.h:387-557): same method names,
+argument meaning and order.  Point buffers are device tensors (torch) or raw
+device pointers.  There is no CPU fallback: loading fails loudly if the
+library is missing, and every failing call raises GbvdbError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgbvdb.so")
+
+OK, INVALID_ARG, OUT_OF_MEMORY, CUDA_ERROR, DEPTH_UNSUPPORTED, CAPACITY, TIMEOUT, NOT_SUPPORTED, NOOP = range(9)
+STATUS_NAMES = ["OK", "INVALID_ARG", "OUT_OF_MEMORY", "CUDA_ERROR", "DEPTH_UNSUPPORTED", "CAPACITY", "TIMEOUT",
+                "NOT_SUPPORTED", "NOOP"]
+T_UCHAR, T_FLOAT, T_HALF, T_BFLOAT16 = 0, 3, 100, 101
+
+NODE_DTYPE = np.dtype([
+    ("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "u1"),
+    ("pos", "<i4", 3), ("value", "<i4", 3), ("vrange", "<f4", 3),
+    ("parent", "<u8"), ("childlist", "<u8"), ("mask", "<u8"),
+])
+AMAP_DTYPE = np.dtype([("pos", "<i4", 3), ("leaf", "<i4")])
+
+# every symbol declared in include/gbvdb.h
+EXPORTS = [
+    "gbvdb_create", "gbvdb_destroy", "gbvdb_set_stream", "gbvdb_last_error", "gbvdb_configure",
+    "gbvdb_configure5", "gbvdb_set_channel_default", "gbvdb_add_channel", "gbvdb_set_points",
+    "gbvdb_rebuild_topology", "gbvdb_accumulate_topology", "gbvdb_request_full_rebuild",
+    "gbvdb_finish_topology", "gbvdb_update_atlas", "gbvdb_insert_points_subcell", "gbvdb_gather_density",
+    "gbvdb_gather_levelset", "gbvdb_update_apron", "gbvdb_fill_channel", "gbvdb_get_depth",
+    "gbvdb_get_node_counts", "gbvdb_get_point_bounds", "gbvdb_export_nodes", "gbvdb_export_childlist",
+    "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
+    "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
+    "gbvdb_get_stats",
+]
+
+
+class GbvdbError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libgbvdb.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libgbvdb.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    vp, i32, i64, f32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+    fp = ctypes.POINTER(ctypes.c_float)
+    for name in EXPORTS:
+        getattr(L, name).restype = i32
+    L.gbvdb_last_error.restype = ctypes.c_char_p
+    L.gbvdb_create.argtypes = [i32, ctypes.POINTER(vp)]
+    L.gbvdb_destroy.argtypes = [vp]
+    L.gbvdb_set_stream.argtypes = [vp, vp]
+    L.gbvdb_last_error.argtypes = [vp]
+    L.gbvdb_configure.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int)]
+    L.gbvdb_configure5.argtypes = [vp, i32, i32, i32, i32, i32]
+    L.gbvdb_set_channel_default.argtypes = [vp, i32, i32, i32]
+    L.gbvdb_add_channel.argtypes = [vp, i32, i32, i32, i32, i32, i32]
+    L.gbvdb_set_points.argtypes = [vp, vp, i64, i32, i32, vp, i32, i32, vp, i32, i32]
+    L.gbvdb_rebuild_topology.argtypes = [vp, i64, f32, fp]
+    L.gbvdb_accumulate_topology.argtypes = [vp, i64, f32, fp, i32]
+    L.gbvdb_request_full_rebuild.argtypes = [vp, i32]
+    L.gbvdb_finish_topology.argtypes = [vp, i32, i32]
+    L.gbvdb_update_atlas.argtypes = [vp]
+    L.gbvdb_insert_points_subcell.argtypes = [vp, i32, i64, f32, fp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_gather_density.argtypes = [vp, i32, i64, f32, fp, i64, i32, i32, i32]
+    L.gbvdb_gather_levelset.argtypes = [vp, i32, i64, f32, fp, i64, i32, i32, i32]
+    L.gbvdb_update_apron.argtypes = [vp, i32, f32]
+    L.gbvdb_fill_channel.argtypes = [vp, i32, f32]
+    L.gbvdb_get_depth.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.gbvdb_get_node_counts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_get_point_bounds.argtypes = [vp, fp]
+    L.gbvdb_export_nodes.argtypes = [vp, i32, vp, i64]
+    L.gbvdb_export_childlist.argtypes = [vp, i32, vp, i64]
+    L.gbvdb_get_atlas_info.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int)]
+    L.gbvdb_export_atlas_bricks.argtypes = [vp, i32, vp, i64]
+    L.gbvdb_export_atlas_map.argtypes = [vp, vp, i64]
+    L.gbvdb_export_subcells.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), i64, vp, i64]
+    L.gbvdb_checksum.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_double)]
+    L.gbvdb_get_atlas_device.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.gbvdb_set_profile.argtypes = [vp, i32]
+    L.gbvdb_get_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
+    L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    _lib = L
+    return L
+
+
+def _f3(v):
+    return (ctypes.c_float * 3)(*[float(x) for x in (v if v is not None else (0, 0, 0))])
+
+
+def _dev_ptr(points):
+    """(pointer, n, stride_bytes) of a device point buffer: torch tensor (N, >=3) float32."""
+    if hasattr(points, "data_ptr"):
+        if not points.is_cuda:
+            raise ValueError("points must be a CUDA tensor")
+        if points.dtype.itemsize != 4 or points.dim() != 2 or points.shape[1] < 3 or points.stride(1) != 1:
+            raise ValueError("points must be float32 (N, >=3) with unit inner stride")
+        return points.data_ptr(), points.shape[0], points.stride(0) * 4
+    ptr, n, stride = points
+    return int(ptr), int(n), int(stride)
+
+
+class Grid:
+    """One GVDB grid on one GPU.  `log2dims` is top -> leaf, as Configure(q4..q0)."""
+
+    def __init__(self, device=0, log2dims=(3, 3, 3, 4), stream=None):
+        self.L = load()
+        h = ctypes.c_void_p()
+        self._check(self.L.gbvdb_create(int(device), ctypes.byref(h)), "create", handle=None)
+        self._h = h
+        self.levs = len(log2dims)
+        self.configure(log2dims)
+        if stream is not None:
+            self.set_stream(stream)
+        self._points = None
+
+    def _check(self, st, what, handle="self", allow_noop=True):
+        if st == OK or (allow_noop and st == NOOP):
+            return st
+        msg = ""
+        if handle == "self":
+            msg = (self.L.gbvdb_last_error(self._h) or b"").decode()
+        raise GbvdbError(st, "%s failed: %s" % (what, msg))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.L.gbvdb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- configuration -----------------------------------------------------
+    def set_stream(self, stream):
+        ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        self._check(self.L.gbvdb_set_stream(self._h, ctypes.c_void_p(ptr)), "set_stream")
+
+    def configure(self, log2dims):
+        leaf_first = list(reversed(log2dims))
+        arr = (ctypes.c_int * len(leaf_first))(*leaf_first)
+        self._check(self.L.gbvdb_configure(self._h, len(leaf_first), arr), "configure")
+        self.levs = len(leaf_first)
+        self._leaf_first = [d if d else 1 for d in leaf_first]
+
+    def set_channel_default(self, ax, ay, az):
+        self._check(self.L.gbvdb_set_channel_default(self._h, ax, ay, az), "set_channel_default")
+
+    def add_channel(self, chan=0, dtype=T_FLOAT, apron=1, axiscnt=(0, 0, 0)):
+        self._check(self.L.gbvdb_add_channel(self._h, chan, dtype, apron, *axiscnt), "add_channel")
+
+    def set_points(self, points, n=None):
+        ptr, cnt, stride = _dev_ptr(points)
+        self._points = points  # keep the buffer alive
+        self._check(self.L.gbvdb_set_points(self._h, ctypes.c_void_p(ptr), cnt if n is None else n, 0, stride,
+                                            None, 0, 0, None, 0, 0), "set_points")
+        return cnt
+
+    # -- topology ------------------------------------------------------------
+    def rebuild_topology(self, n, radius, orig=(0, 0, 0)):
+        return self._check(self.L.gbvdb_rebuild_topology(self._h, n, radius, _f3(orig)), "rebuild_topology")
+
+    def accumulate_topology(self, n, radius, orig=(0, 0, 0), min_depth=1):
+        return self._check(self.L.gbvdb_accumulate_topology(self._h, n, radius, _f3(orig), min_depth),
+                           "accumulate_topology")
+
+    def request_full_rebuild(self, tf=True):
+        self._check(self.L.gbvdb_request_full_rebuild(self._h, 1 if tf else 0), "request_full_rebuild")
+
+    def finish_topology(self, commit=False, bounds=True):
+        self._check(self.L.gbvdb_finish_topology(self._h, int(commit), int(bounds)), "finish_topology")
+
+    def update_atlas(self):
+        return self._check(self.L.gbvdb_update_atlas(self._h), "update_atlas")
+
+    # -- points to voxels ----------------------------------------------------
+    def insert_points_subcell(self, subcell, n, radius, trans=(0, 0, 0)):
+        out = ctypes.c_int64(-1)
+        st = self._check(self.L.gbvdb_insert_points_subcell(self._h, subcell, n, radius, _f3(trans),
+                                                            ctypes.byref(out)), "insert_points_subcell")
+        return st, int(out.value)
+
+    def gather_density(self, subcell, n, radius, trans, sc_len, chan=0, clr_chan=-1, accum=False):
+        return self._check(self.L.gbvdb_gather_density(self._h, subcell, n, radius, _f3(trans), sc_len, chan,
+                                                       clr_chan, int(accum)), "gather_density")
+
+    def gather_levelset(self, subcell, n, radius, trans, sc_len, chan=0, clr_chan=-1, accum=False):
+        return self._check(self.L.gbvdb_gather_levelset(self._h, subcell, n, radius, _f3(trans), sc_len, chan,
+                                                        clr_chan, int(accum)), "gather_levelset")
+
+    def update_apron(self, chan=0, boundval=0.0):
+        return self._check(self.L.gbvdb_update_apron(self._h, chan, boundval), "update_apron")
+
+    def fill_channel(self, chan, value):
+        return self._check(self.L.gbvdb_fill_channel(self._h, chan, value), "fill_channel")
+
+    # -- state / export ------------------------------------------------------
+    def depth(self):
+        d, t = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.gbvdb_get_depth(self._h, ctypes.byref(d), ctypes.byref(t)), "get_depth")
+        return d.value, t.value
+
+    def node_counts(self):
+        tot = (ctypes.c_int64 * 10)()
+        used = (ctypes.c_int64 * 10)()
+        self._check(self.L.gbvdb_get_node_counts(self._h, tot, used), "get_node_counts")
+        return list(tot), list(used)
+
+    def point_bounds(self):
+        out = (ctypes.c_float * 6)()
+        self._check(self.L.gbvdb_get_point_bounds(self._h, out), "get_point_bounds")
+        return np.array(out[:], dtype=np.float32)
+
+    def nodes(self, lev):
+        n = self.node_counts()[0][lev]
+        out = np.zeros(n, dtype=NODE_DTYPE)
+        if n:
+            self._check(self.L.gbvdb_export_nodes(self._h, lev, out.ctypes.data, n), "export_nodes")
+        return out
+
+    def childlist(self, lev):
+        n = self.node_counts()[0][lev]
+        if lev == 0 or n == 0:
+            return np.zeros((n, 0), dtype=np.uint64)
+        cl = 1 << (3 * self._leaf_first[lev])
+        out = np.zeros(n * cl, dtype=np.uint64)
+        self._check(self.L.gbvdb_export_childlist(self._h, lev, out.ctypes.data, n * cl), "export_childlist")
+        return out.reshape(n, cl)
+
+    def atlas_info(self, chan=0):
+        info = (ctypes.c_int * 8)()
+        self._check(self.L.gbvdb_get_atlas_info(self._h, chan, info), "get_atlas_info")
+        keys = ["ax", "ay", "az", "used", "dtype", "apron", "brick_res", "esize"]
+        return dict(zip(keys, info[:]))
+
+    def atlas_bricks(self, chan=0):
+        """Padded bricks of the assigned slots, shape (used, 18, 18, 18) [slot, z, y, x].
+        float32 channels return float32; half returns float16; bfloat16 returns raw uint16."""
+        info = self.atlas_info(chan)
+        used = info["used"]
+        dt = {T_FLOAT: np.float32, T_HALF: np.float16, T_BFLOAT16: np.uint16}[info["dtype"]]
+        out = np.zeros(used * 5832, dtype=dt)
+        if used:
+            self._check(self.L.gbvdb_export_atlas_bricks(self._h, chan, out.ctypes.data, out.nbytes),
+                        "export_atlas_bricks")
+        return out.reshape(used, 18, 18, 18)
+
+    def atlas_map(self):
+        info = self.atlas_info(0)
+        n = info["ax"] * info["ay"] * info["az"]
+        out = np.zeros(n, dtype=AMAP_DTYPE)
+        if n:
+            self._check(self.L.gbvdb_export_atlas_map(self._h, out.ctypes.data, n), "export_atlas_map")
+        return out
+
+    def subcells(self, total_len, nsub):
+        off = np.zeros(nsub + 1, dtype=np.int64)
+        pts = np.zeros((max(total_len, 0), 3), dtype=np.float32)
+        self._check(self.L.gbvdb_export_subcells(
+            self._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nsub + 1,
+            pts.ctypes.data if total_len > 0 else None, total_len), "export_subcells")
+        return off, pts
+
+    def checksum(self, chan=0):
+        out = ctypes.c_double()
+        self._check(self.L.gbvdb_checksum(self._h, chan, ctypes.byref(out)), "checksum")
+        return out.value
+
+    def set_profile(self, on=True):
+        self._check(self.L.gbvdb_set_profile(self._h, int(on)), "set_profile")
+
+    def stats(self):
+        out = (ctypes.c_int64 * 4)()
+        self._check(self.L.gbvdb_get_stats(self._h, out), "get_stats")
+        return {"launches": out[0], "readbacks": out[1], "sc_len": out[2], "bricks": out[3]}
+
+    def stage_times(self, cap=32):
+        out = (ctypes.c_double * cap)()
+        self._check(self.L.gbvdb_get_stage_times(self._h, out, cap), "get_stage_times")
+        return [v for v in out[:] if v >= 0]
+
+
+def bf16_to_f32(u16):
+    """Raw bfloat16 bits (uint16) -> float32."""
+    return (u16.astype(np.uint32) << 16).view(np.float32)

@@ -1,0 +1,154 @@
+/*
+ * gbvdb.h -- C ABI of the GB300-native point-driven dynamic-topology path of
+ * GVDB Voxels (libgbvdb.so).
+ *
+ * Each entry point replaces one method of the reference class nvdb::VolumeGVDB
+ * (source/gvdb_library/src/gvdb_volume_gvdb.h) for the path
+ *   RebuildTopology -> UpdateAtlas -> InsertPointsSubcell -> Gather* -> UpdateApron
+ * with the same argument meaning.  Signatures use plain pointers and sizes
+ * only.  Point buffers are borrowed DEVICE pointers (as DataPtr.gpu in the
+ * reference); the grid owns all other device memory.  Every call returns a
+ * gbvdb_status instead of printing and calling exit() (the reference's
+ * cudaCheck, gvdb_allocator.cpp:1006-1034).  All work is issued on the grid's
+ * stream (gbvdb_set_stream; default: the legacy NULL stream).
+ *
+ * Layouts kept from the reference:
+ *   - node records: 64 bytes, gvdb_node.h:27-40 (mLev, mFlags, mPriority, pad,
+ *     mPos int3, mValue int3, mVRange float3, mParent u64, mChildList u64, mMask u64);
+ *   - pool references Elem(grp,lev,ndx) = grp | lev<<8 | ndx<<16 (gvdb_allocator.h:59-62);
+ *   - child lists: res^3 u64 per node, 0xFF..FF = empty (no bitmasks);
+ *   - atlas addressing: slot id -> (id%ax, (id/ax)%ay, id/(ax*ay))*18 + apron
+ *     (gvdb_allocator.cpp:705-715), 16^3 bricks with a 1-voxel apron;
+ *   - atlas map entries {int3 pos, int leaf} (cuda_gvdb_nodes.cuh:38-41).
+ * The physical atlas storage is brick-major (see gbvdb_export_atlas_bricks);
+ * exported bricks are 18^3 with the apron, [z][y][x].
+ */
+#ifndef GBVDB_H
+#define GBVDB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBVDB_API __attribute__((visibility("default")))
+#else
+#define GBVDB_API
+#endif
+
+typedef struct gbvdb_grid_s* gbvdb_grid;
+
+typedef enum {
+    GBVDB_OK = 0,
+    GBVDB_INVALID_ARG = 1,        /* bad argument or call order */
+    GBVDB_OUT_OF_MEMORY = 2,      /* device or host allocation failed */
+    GBVDB_CUDA_ERROR = 3,         /* a CUDA runtime call failed; see gbvdb_last_error */
+    GBVDB_DEPTH_UNSUPPORTED = 4,  /* point extents < 1 brick or > 5 levels (VG.cpp:1187-1194) */
+    GBVDB_CAPACITY = 5,           /* a device capacity was exceeded; retry was not possible */
+    GBVDB_TIMEOUT = 6,            /* a bounded device wait gave up */
+    GBVDB_NOT_SUPPORTED = 7,      /* configuration outside what this build implements */
+    GBVDB_NOOP = 8                /* nothing to do (the reference returns early here) */
+} gbvdb_status;
+
+/* channel element types: the reference's T_* codes (gvdb_types.h) plus two storage extensions */
+#define GBVDB_T_UCHAR 0
+#define GBVDB_T_FLOAT 3
+#define GBVDB_T_HALF 100    /* extension: FP16 storage, FP32 accumulation */
+#define GBVDB_T_BFLOAT16 101 /* extension: BF16 storage, FP32 accumulation */
+
+/* --- lifetime ------------------------------------------------------------ */
+/* SetCudaDevice + Initialize (gvdb_volume_gvdb.cpp:240-334, 2320-2361) */
+GBVDB_API gbvdb_status gbvdb_create(int device, gbvdb_grid* out);
+GBVDB_API gbvdb_status gbvdb_destroy(gbvdb_grid g);
+/* all work of this grid goes to `stream` (a cudaStream_t) */
+GBVDB_API gbvdb_status gbvdb_set_stream(gbvdb_grid g, void* stream);
+/* message of the last failing call on this grid */
+GBVDB_API const char* gbvdb_last_error(gbvdb_grid g);
+
+/* --- configuration ------------------------------------------------------- */
+/* Configure(levs, r, numcnt) (gvdb_volume_gvdb.cpp:2380-2434); log2dim[0] = leaf */
+GBVDB_API gbvdb_status gbvdb_configure(gbvdb_grid g, int levs, const int* log2dim_leaf_first);
+/* Configure(q4, q3, q2, q1, q0) (gvdb_volume_gvdb.cpp:2364-2377) */
+GBVDB_API gbvdb_status gbvdb_configure5(gbvdb_grid g, int q4, int q3, int q2, int q1, int q0);
+/* SetChannelDefault (gvdb_volume_gvdb.h:390) */
+GBVDB_API gbvdb_status gbvdb_set_channel_default(gbvdb_grid g, int ax, int ay, int az);
+/* AddChannel(chan, dt, apron, filter, border, axiscnt) (gvdb_volume_gvdb.cpp:2437-2453);
+ * apron must be 1 (the reference's kernels assume it, VG.cpp:4448) */
+GBVDB_API gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron,
+                                         int ax, int ay, int az);
+/* SetPoints / SetDataGPU (gvdb_volume_gvdb.cpp:4900-4908, 4872-4880): position i is the
+ * float3 at pos + i*stride + off.  vel and clr may be NULL. */
+GBVDB_API gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* dev_pos, int64_t n, int off, int stride,
+                                        const void* dev_vel, int vel_off, int vel_stride,
+                                        const void* dev_clr, int clr_off, int clr_stride);
+
+/* --- topology ------------------------------------------------------------ */
+/* RebuildTopology(num_pnts, radius, orig) (gvdb_volume_gvdb.cpp:1181-1218) */
+GBVDB_API gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3]);
+/* AccumulateTopology(num_pnts, radius, orig, iDepth) (gvdb_volume_gvdb.cpp:1158-1178) */
+GBVDB_API gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3],
+                                                 int min_depth);
+/* RequestFullRebuild (gvdb_volume_gvdb.h:432) */
+GBVDB_API gbvdb_status gbvdb_request_full_rebuild(gbvdb_grid g, int tf);
+/* FinishTopology(commit, bounds) (gvdb_volume_gvdb.cpp:1579-1593): bounds of the active leaves */
+GBVDB_API gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bounds);
+/* UpdateAtlas (gvdb_volume_gvdb.cpp:2630-2704) */
+GBVDB_API gbvdb_status gbvdb_update_atlas(gbvdb_grid g);
+
+/* --- points to voxels ---------------------------------------------------- */
+/* InsertPointsSubcell(subcell_size, num_pnts, radius, trans, &len) (gvdb_volume_gvdb.cpp:4971-5092);
+ * *out_len receives the total subcell list length pSCPntsLength. */
+GBVDB_API gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int subcell_size, int64_t n, float radius,
+                                                   const float trans[3], int64_t* out_len);
+/* GatherDensity (gvdb_volume_gvdb.cpp:5318-5344): v = max(accum ? old : 0, max_j(radius - |p_j - v|)) */
+GBVDB_API gbvdb_status gbvdb_gather_density(gbvdb_grid g, int subcell_size, int64_t n, float radius,
+                                            const float trans[3], int64_t sc_len, int chan, int clr_chan,
+                                            int accum);
+/* GatherLevelSet (gvdb_volume_gvdb.cpp:5348-5373): v = min(accum ? old : 3, min_j(|p_j - v| - radius)) */
+GBVDB_API gbvdb_status gbvdb_gather_levelset(gbvdb_grid g, int subcell_size, int64_t n, float radius,
+                                             const float trans[3], int64_t sc_len, int chan, int clr_chan,
+                                             int accum);
+/* UpdateApron(chan, boundval) (gvdb_volume_gvdb.cpp:4418-4457, cuda_gvdb_operators.cuh:72-131) */
+GBVDB_API gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval);
+/* ClearChannel / FillChannel (gvdb_volume_gvdb.cpp:2456-2485) for the assigned slots */
+GBVDB_API gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value);
+
+/* --- state and export (for parity checks, VBX and consumers) -------------- */
+/* depth of the last build, traversal top level (VG.cpp:3957-3968) */
+GBVDB_API gbvdb_status gbvdb_get_depth(gbvdb_grid g, int* depth, int* top_lev);
+/* getNumTotalNodes / getNumUsedNodes per level (gvdb_volume_gvdb.h:637-641); arrays of 10 */
+GBVDB_API gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used);
+/* getBoundMin/Max (gvdb_volume_gvdb.h:563-564): 6 floats */
+GBVDB_API gbvdb_status gbvdb_get_point_bounds(gbvdb_grid g, float* out6);
+/* node pool of one level as 64-byte records (host buffer, `cap` records) */
+GBVDB_API gbvdb_status gbvdb_export_nodes(gbvdb_grid g, int lev, void* host_out, int64_t cap);
+/* child-list pool of one level (res^3 u64 per node) */
+GBVDB_API gbvdb_status gbvdb_export_childlist(gbvdb_grid g, int lev, uint64_t* host_out, int64_t cap);
+/* info[8] = {ax, ay, az, used_slots, dtype, apron, brick_res(18), bytes_per_voxel} */
+GBVDB_API gbvdb_status gbvdb_get_atlas_info(gbvdb_grid g, int chan, int* info8);
+/* padded bricks of slots [0, used): used * 18^3 voxels, [slot][z][y][x], storage type */
+GBVDB_API gbvdb_status gbvdb_export_atlas_bricks(gbvdb_grid g, int chan, void* host_out, int64_t cap_bytes);
+/* atlas map (16 bytes per slot, ax*ay*az entries) */
+GBVDB_API gbvdb_status gbvdb_export_atlas_map(gbvdb_grid g, void* host_out, int64_t cap);
+/* materialized subcell lists of the last InsertPointsSubcell: offsets[nsub+1] (nsub = 64 *
+ * linked leaves, subcells in reference order) and float3 points; the order inside one list
+ * is unspecified, as in the reference (PT.cuh:266 uses atomicAdd slots) */
+GBVDB_API gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int64_t cap_offsets,
+                                             float* points, int64_t cap_points);
+/* FP64 sum of the interior voxels of all assigned slots (total-mass check) */
+GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
+/* device pointers of the atlas storage (interior bricks, apron records) for consumers */
+GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron);
+/* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
+GBVDB_API gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable);
+GBVDB_API gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap);
+/* out4 = {kernel launches issued so far, host readbacks so far, last subcell-list length,
+ * linked leaves of the last insert} */
+GBVDB_API gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBVDB_H */

@@ -1,0 +1,197 @@
+"""GPU parity tests: the CUDA path (through the C ABI of libgbvdb.so) against the
+CPU oracle on the same seeded inputs.
+
+Rules (see tests/_helpers.py): node pools, child lists, atlas map and subcell
+membership bit-exact; gathered values within 1e-5 relative + 1e-6 absolute of
+the FP64 oracle; apron voxels bit-exact copies of the neighbour interior (or
+the boundary value) and within the same tolerance of the oracle.
+"""
+import numpy as np
+import pytest
+
+import _helpers as H
+import datasets
+
+pytestmark = pytest.mark.gpu
+
+
+def _mini_fluid(n=60000, seed=11):
+    pos, vel = datasets.fluid(n=n, seed=seed, box=(32, 64, 32), domain=128)
+    return pos, vel
+
+
+def _full_check(o, g, boundval, tol=None):
+    H.compare_topology(o, g)
+    H.compare_subcells(o, g)
+    err = H.compare_values(o, g) if tol is None else H.compare_values(o, g, *tol)
+    H.check_apron_self(g, boundval)
+    return err
+
+
+def test_shell_200k_density(gpu_lib):
+    """Plain path, small: the 200,000-point shell, grid (3,3,3,4), r = R = rho = 1."""
+    pts = datasets.shell(200_000, seed=0)
+    _, o = H.run_oracle(pts, radius=1.0, R=1.0, rho=1.0, mode="density", boundval=0.0)
+    _, g = H.run_gpu(pts, radius=1.0, R=1.0, rho=1.0, mode="density", boundval=0.0)
+    _full_check(o[0], g[0], 0.0)
+    assert abs(o[0]["checksum"] - g[0]["checksum"]) <= 1e-6 * max(1.0, abs(o[0]["checksum"]))
+
+
+def test_fluid_frames_levelset(gpu_lib):
+    """Dam-break frames: RebuildTopology(r=4), InsertPointsSubcell(R=4), GatherLevelSet(rho=2),
+    UpdateApron(3.0); frame 2 is a full rebuild (mCurrDepth quirk), frames 3+ incremental."""
+    pos, vel = _mini_fluid()
+    frames = []
+    p = pos.copy()
+    for f in range(4):
+        p = (p + 0.5 * vel).astype(np.float32)
+        frames.append(p.copy())
+    _, o = H.run_oracle(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    _, g = H.run_gpu(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    for k in range(len(frames)):
+        _full_check(o[k], g[k], 3.0)
+
+
+def test_accumulate_topology(gpu_lib):
+    pos, vel = _mini_fluid(n=20000, seed=5)
+    frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
+    frames = [np.maximum(f, 0.0).astype(np.float32) for f in frames]
+    _, o = H.run_oracle(None, frames=frames, radius=2.0, R=2.0, rho=1.5, accumulate=True)
+    _, g = H.run_gpu(None, frames=frames, radius=2.0, R=2.0, rho=1.5, accumulate=True)
+    for k in range(len(frames)):
+        _full_check(o[k], g[k], 0.0)
+
+
+@pytest.mark.parametrize("dtype,rtol", [("half", 1e-3), ("bf16", 8e-3)])
+def test_reduced_precision_storage(gpu_lib, dtype, rtol):
+    import gbvdb
+
+    dt = gbvdb.T_HALF if dtype == "half" else gbvdb.T_BFLOAT16
+    pts = datasets.shell(50_000, seed=7)
+    _, o = H.run_oracle(pts, radius=1.5, R=1.5, rho=1.5)
+    _, g = H.run_gpu(pts, radius=1.5, R=1.5, rho=1.5, dtype=dt)
+    H.compare_topology(o[0], g[0])
+    H.compare_subcells(o[0], g[0])
+    err = H.compare_values(o[0], g[0], rtol, 1e-3, dtype=dt)
+    assert err < 0.05
+
+
+def test_surface_depth3(gpu_lib):
+    """Sphere-surface points in a 4096^3 domain with grid (4,4,3,4): depth 3, default atlas."""
+    pts = datasets.sphere_surface(40_000, seed=21, domain=4096.0, nspheres=6)
+    pts = pts[np.all(pts >= 0, axis=1)]
+    _, o = H.run_oracle(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5)
+    _, g = H.run_gpu(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5)
+    assert o[0]["depth"] == 3
+    _full_check(o[0], g[0], 0.0)
+
+
+def test_strided_input_and_translation(gpu_lib):
+    """Positions read at pos + i*stride + off (DataPtr), with orig / trans offsets."""
+    import torch
+
+    import gbvdb
+
+    pts = datasets.shell(30_000, seed=3)
+    orig = (5.25, -3.5, 7.0)
+    _, o = H.run_oracle(pts, radius=1.0, R=1.0, rho=1.0, orig=orig)
+    # oracle insert/gather used trans = 0 on the raw points; run the same on the GPU
+    wide = np.zeros((pts.shape[0], 5), dtype=np.float32)
+    wide[:, :3] = pts
+    wide[:, 3:] = 123.0
+    d = torch.from_numpy(wide).cuda()
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0)
+    n = g.set_points(d)
+    g.rebuild_topology(n, 1.0, orig)
+    g.update_atlas()
+    st, ln = g.insert_points_subcell(4, n, 1.0)
+    g.gather_density(4, n, 1.0, (0, 0, 0), ln)
+    g.update_apron(0, 0.0)
+    s = H.snapshot_gpu(g, ln)
+    _full_check(o[0], s, 0.0)
+
+
+def test_orphan_points_use_the_list_path(gpu_lib):
+    """InsertPointsSubcell with points whose home brick is not in the topology: the
+    reference still lists them in neighbouring subcells; the result must match."""
+    import oracle
+    import torch
+
+    import gbvdb
+
+    base = datasets.shell(20_000, seed=1)
+    moved = (base + np.array([6.0, 0.0, 0.0], dtype=np.float32)).astype(np.float32)
+    og = oracle.OracleGrid((3, 3, 3, 4))
+    og.add_channel(0)
+    assert og.rebuild_topology(base, 1.0) == 0
+    og.update_atlas()
+    rc, ln_o = og.insert_points_subcell(moved, 2.0)
+    og.gather_density(2.0)
+    og.update_apron(0, 0.0)
+    o = H.snapshot_oracle(og, ln_o)
+
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0)
+    db = torch.from_numpy(base).cuda()
+    dm = torch.from_numpy(moved).cuda()
+    n = g.set_points(db)
+    g.rebuild_topology(n, 1.0)
+    g.update_atlas()
+    g.set_points(dm)
+    st, ln = g.insert_points_subcell(4, n, 2.0)
+    g.gather_density(4, n, 2.0, (0, 0, 0), ln)
+    g.update_apron(0, 0.0)
+    s = H.snapshot_gpu(g, ln)
+    _full_check(o, s, 0.0)
+
+
+def test_edge_cases(gpu_lib):
+    import torch
+
+    import gbvdb
+
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0)
+    # empty input: nothing to do
+    d = torch.zeros((0, 3), dtype=torch.float32, device="cuda")
+    g.set_points(d)
+    assert g.rebuild_topology(0, 1.0) == gbvdb.NOOP
+    # all points in one brick: depth 0 is an error (VG.cpp:1187-1190)
+    one = torch.tensor([[20.5, 20.5, 20.5]], dtype=torch.float32, device="cuda")
+    n = g.set_points(one)
+    with pytest.raises(gbvdb.GbvdbError) as e:
+        g.rebuild_topology(n, 1.0)
+    assert e.value.status == gbvdb.DEPTH_UNSUPPORTED
+    # extents beyond the configured levels
+    far = torch.tensor([[1.0, 1.0, 1.0], [60000.0, 1.0, 1.0]], dtype=torch.float32, device="cuda")
+    n = g.set_points(far)
+    with pytest.raises(gbvdb.GbvdbError) as e:
+        g.rebuild_topology(n, 1.0)
+    assert e.value.status == gbvdb.DEPTH_UNSUPPORTED
+    # all points negative except bbox-defining ones: negative points make no keys
+    pts = np.array([[-5.0, 10.0, 10.0], [30.5, 30.5, 30.5], [40.5, 40.5, 40.5], [-1.0, -1.0, -1.0]],
+                   dtype=np.float32)
+    _, o = H.run_oracle(pts, radius=1.0, R=1.0, rho=1.0)
+    _, s = H.run_gpu(pts, radius=1.0, R=1.0, rho=1.0)
+    _full_check(o[0], s[0], 0.0)
+    # NOHIT points are skipped by InsertPointsSubcell but still bound the box (PT.cuh:282)
+    # a single point per brick corner, ragged counts per brick
+    rng = np.random.default_rng(9)
+    ragged = np.concatenate([rng.uniform(0, 64, size=(500, 3)), rng.uniform(200, 203, size=(7, 3))]).astype(np.float32)
+    _, o = H.run_oracle(ragged, radius=2.0, R=3.0, rho=2.5, mode="levelset", boundval=3.0)
+    _, s = H.run_gpu(ragged, radius=2.0, R=3.0, rho=2.5, mode="levelset", boundval=3.0)
+    _full_check(o[0], s[0], 3.0)
+
+
+def test_insert_before_topology_is_noop(gpu_lib):
+    import torch
+
+    import gbvdb
+
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0)
+    d = torch.from_numpy(datasets.shell(1000, seed=2)).cuda()
+    n = g.set_points(d)
+    st, ln = g.insert_points_subcell(4, n, 1.0)
+    assert st == gbvdb.NOOP and ln == -1
