@@ -122,7 +122,7 @@ struct gbvdb_grid_s {
     DevBuf list_cnt, list_off, list_pts;
 
     // scratch
-    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer;
+    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     unsigned char* pinned = nullptr;
 
     // profiling
@@ -350,7 +350,10 @@ struct gbvdb_grid_s {
     void link_all(int depth) {
         TreeView t = view();
         for (int lev = depth - 1; lev >= 0; lev--) {
-            launch_link(t, lev, ncnt[lev], stream);
+            long long nslots = ncnt[lev + 1] * cl_len(lev + 1);
+            grow(link_tag, (size_t)std::max(nslots, 1ll) * 4);
+            grow(link_slot, (size_t)std::max(ncnt[lev], 1ll) * 8);
+            launch_link(t, lev, ncnt[lev], ptr<int>(link_tag), ptr<long long>(link_slot), stream);
             check_launch("link");
         }
     }
@@ -467,8 +470,8 @@ struct gbvdb_grid_s {
 
     gbvdb_status rebuild(long long n, float radius, float3 orig, bool accumulate, int min_depth) {
         if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
-        if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
         if (n <= 0) return GBVDB_NOOP;
+        if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
         if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
         stage_begin();
         compute_bbox(n, orig);
@@ -772,7 +775,8 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->bitmap, &g->pcnt, &g->pscan,
-                      &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer};
+                      &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
+                      &g->link_tag, &g->link_slot};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -871,7 +875,7 @@ gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off,
                               int vel_off, int vel_stride, const void* clr, int clr_off, int clr_stride) {
     GBVDB_GUARD(g)
     (void)vel_off; (void)vel_stride; (void)clr_off; (void)clr_stride;
-    if (!pos || n < 0 || stride < 12 || off < 0 || (off % 4) || (stride % 4)) return GBVDB_INVALID_ARG;
+    if ((!pos && n > 0) || n < 0 || stride < 12 || off < 0 || (off % 4) || (stride % 4)) return GBVDB_INVALID_ARG;
     g->pts.base = reinterpret_cast<const char*>(pos);
     g->pts.n = n;
     g->pts.off = off;

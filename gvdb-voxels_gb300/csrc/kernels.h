@@ -43,7 +43,8 @@ void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s);
-void launch_link(const TreeView& t, int lev, long long count, cudaStream_t s);
+// tag: ncnt[lev+1]*res^3 ints, slot_of: count long longs (scratch)
+void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s);
 void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s);
 void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s);
 void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s);

@@ -176,10 +176,15 @@ __global__ void k_alloc_nodes(const uint32_t* __restrict__ bm, const uint32_t* _
 
 __global__ void k_write_node(Node* dst, Node v) { *dst = v; }
 
-// gvdbLinkBricks (ND.cuh:470-505)
-__global__ void k_link(TreeView t, int lev, long long count) {
+// gvdbLinkBricks (ND.cuh:470-505), in two launches.  When two flagged nodes of
+// one level map to the same child slot (duplicates the reference creates after
+// its top-level quirk), the reference's single kernel races on that slot; here
+// the highest pool index wins, which is what a sequential pass over the nodes
+// leaves behind.  claim: set mParent, record the slot, atomicMax the index.
+__global__ void k_link_claim(TreeView t, int lev, long long count, int* tag, long long* slot_of) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
+    slot_of[i] = -1;
     Node* node = t.nodes[lev] + i;
     if (!node->flags) return;
     long long pid = get_parent(t, lev + 1, node->pos[0], node->pos[1], node->pos[2]);
@@ -195,7 +200,17 @@ __global__ void k_link(TreeView t, int lev, long long count) {
     node->parent = ((unsigned long long)pid << 16) | ((unsigned long long)(lev + 1) << 8);
     unsigned long long cndx = pn->childlist >> 16;
     if ((long long)cndx >= t.ncnt[lev + 1]) return;
-    t.clist[lev + 1][(cndx << (3 * t.lgres[lev + 1])) + b] = ((unsigned long long)i << 16) | ((unsigned long long)lev << 8);
+    long long slot = (long long)(cndx << (3 * t.lgres[lev + 1])) + b;
+    slot_of[i] = slot;
+    atomicMax(tag + slot, (int)i);
+}
+
+__global__ void k_link_write(TreeView t, int lev, long long count, const int* tag, const long long* slot_of) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    long long slot = slot_of[i];
+    if (slot < 0 || tag[slot] != (int)i) return;
+    t.clist[lev + 1][slot] = ((unsigned long long)i << 16) | ((unsigned long long)lev << 8);
 }
 
 __global__ void k_init_markers(const Node* leaves, long long n, int* markers, int accum) {
@@ -305,9 +320,12 @@ void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long wo
     k_alloc_nodes<<<blocks_for(nwords, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
 }
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<1, 1, 0, s>>>(dst, v); }
-void launch_link(const TreeView& t, int lev, long long count, cudaStream_t s) {
+void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s) {
     if (count <= 0) return;
-    k_link<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count);
+    long long nslots = t.ncnt[lev + 1] << (3 * t.lgres[lev + 1]);
+    cudaMemsetAsync(tag, 0xFF, (size_t)nslots * sizeof(int), s);
+    k_link_claim<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
+    k_link_write<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
 }
 void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s) {
     if (n <= 0) return;

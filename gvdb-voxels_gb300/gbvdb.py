@@ -237,9 +237,11 @@ class Grid:
 
     def childlist(self, lev):
         n = self.node_counts()[0][lev]
-        if lev == 0 or n == 0:
+        if lev == 0:
             return np.zeros((n, 0), dtype=np.uint64)
         cl = 1 << (3 * self._leaf_first[lev])
+        if n == 0:
+            return np.zeros((0, cl), dtype=np.uint64)
         out = np.zeros(n * cl, dtype=np.uint64)
         self._check(self.L.gbvdb_export_childlist(self._h, lev, out.ctypes.data, n * cl), "export_childlist")
         return out.reshape(n, cl)
