@@ -14,6 +14,9 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
+#include <mutex>
+
 #include "kernels.h"
 
 namespace gbvdb {
@@ -151,6 +154,51 @@ __global__ void k_fill_interior(const AtlasNode* __restrict__ amap, int used, T*
     }
 }
 
+// ---- allocation-free checksum ------------------------------------------
+// Scratch of gbvdb_checksum_noalloc: one FP64 partial sum per atlas slot, in a
+// file-scope device array (every GPU that loads the library holds it until the
+// process exits).  Host code must not pass `g_slot_partials` to a kernel: on the
+// host that name is only a stand-in; its device address comes from
+// cudaGetSymbolAddress, taken once per device (checksum_noalloc below).
+constexpr int kNoAllocMaxSlots = 65536;
+static __device__ __align__(256) double g_slot_partials[kNoAllocMaxSlots];
+
+// one block per slot (grid-stride over slots): fixed-order FP64 sum of the 4096 interior voxels
+template <typename T>
+__global__ void k_slot_sums(const AtlasNode* __restrict__ amap, int used, const T* __restrict__ interior,
+                            double* __restrict__ partials) {
+    __shared__ double red[32];
+    for (int s = blockIdx.x; s < used; s += gridDim.x) {
+        double acc = 0.0;
+        if (amap[s].leaf >= 0)
+            for (int v = threadIdx.x; v < 4096; v += blockDim.x) acc += (double)to_f32(interior[(size_t)s * 4096 + v]);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
+            if (threadIdx.x == 0) partials[s] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// single block: fixed-order sum of the per-slot partials
+__global__ void k_sum_partials(const double* __restrict__ partials, int used, double* __restrict__ out) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int s = threadIdx.x; s < used; s += blockDim.x) acc += partials[s];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
+        if (threadIdx.x == 0) *out = t;
+    }
+}
+
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 inline unsigned gs_blocks(long long n, int t) {
     long long b = (n + t - 1) / t;
@@ -216,6 +264,42 @@ void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* inte
     else
         k_fill_interior<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (__nv_bfloat16*)interior,
                                                                             value);
+}
+
+int noalloc_max_slots() { return kNoAllocMaxSlots; }
+
+cudaError_t checksum_noalloc(const AtlasNode* amap, int used, int dtype, const void* interior, double* dev_out,
+                             cudaStream_t s) {
+    // device address of the static scratch, taken once per device with that device current
+    static std::mutex mu;
+    static double* addr[128] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
+    double* partials = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!addr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_slot_partials);
+            if (e != cudaSuccess) return e;
+            addr[dev] = static_cast<double*>(p);
+        }
+        partials = addr[dev];
+    }
+    if (used < 0 || used > kNoAllocMaxSlots) return cudaErrorInvalidValue;
+    if (used > 0) {
+        unsigned blocks = (unsigned)std::min(used, 152 * 8);
+        if (dtype == 3)
+            k_slot_sums<float><<<blocks, 256, 0, s>>>(amap, used, (const float*)interior, partials);
+        else if (dtype == 100)
+            k_slot_sums<__half><<<blocks, 256, 0, s>>>(amap, used, (const __half*)interior, partials);
+        else
+            k_slot_sums<__nv_bfloat16><<<blocks, 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
+    }
+    k_sum_partials<<<1, 1024, 0, s>>>(partials, used, dev_out);
+    return cudaGetLastError();
 }
 
 }  // namespace gbvdb

@@ -1103,6 +1103,27 @@ gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
     GBVDB_END(g)
 }
 
+// Allocation-free variant of gbvdb_checksum: see include/gbvdb.h.  It reads the
+// grid's atlas and writes one double to dev_out on the grid's stream; its
+// scratch is the static per-slot array in atlas.cu, so it calls no allocator.
+gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !dev_out) return GBVDB_INVALID_ARG;
+    if (g->atlas_last > noalloc_max_slots()) {
+        g->err = "checksum_noalloc: " + std::to_string(g->atlas_last) + " atlas slots exceed the static scratch limit of " +
+                 std::to_string(noalloc_max_slots()) + " slots";
+        return GBVDB_CAPACITY;
+    }
+    cudaError_t e = checksum_noalloc(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype,
+                                     g->ch[chan].interior.p, dev_out, g->stream);
+    if (e != cudaSuccess) {
+        g->err = std::string("checksum_noalloc: ") + cudaGetErrorString(e);
+        return GBVDB_CUDA_ERROR;
+    }
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
 gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron) {
     GBVDB_GUARD(g)
     if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;

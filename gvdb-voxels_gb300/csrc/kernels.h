@@ -66,6 +66,10 @@ void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* int
                      cudaStream_t s);
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value,
                           cudaStream_t s);
+// allocation-free checksum: scratch in a static device array (max slots noalloc_max_slots())
+int noalloc_max_slots();
+cudaError_t checksum_noalloc(const AtlasNode* amap, int used, int dtype, const void* interior, double* dev_out,
+                             cudaStream_t s);
 
 // ---- points.cu
 void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s);

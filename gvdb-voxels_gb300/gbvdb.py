@@ -36,7 +36,7 @@ EXPORTS = [
     "gbvdb_get_node_counts", "gbvdb_get_point_bounds", "gbvdb_export_nodes", "gbvdb_export_childlist",
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
-    "gbvdb_get_stats",
+    "gbvdb_get_stats", "gbvdb_checksum_noalloc",
 ]
 
 
@@ -95,6 +95,7 @@ def load(path=LIB_PATH):
     L.gbvdb_set_profile.argtypes = [vp, i32]
     L.gbvdb_get_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
     L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
     _lib = L
     return L
 

@@ -139,6 +139,19 @@ GBVDB_API gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int
                                              float* points, int64_t cap_points);
 /* FP64 sum of the interior voxels of all assigned slots (total-mass check) */
 GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
+/* Allocation-free variant of gbvdb_checksum (no counterpart in the reference).
+ * For callers that may not allocate device memory: a host application that owns
+ * every device allocation and forbids its plugins to call cudaMalloc, or a
+ * serving loop admitting jobs against a fixed memory budget.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine and does not synchronize:
+ * the FP64 sum is written to the DEVICE pointer dev_out on the grid's stream.
+ * Scratch is a file-scope device array of 65,536 FP64 per-slot partial sums
+ * (512 KiB, held by every GPU that loads the library until exit); grids with
+ * more assigned atlas slots are rejected with GBVDB_CAPACITY.  The first call on
+ * a device looks up that array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (different streams or grids without ordering) race. */
+GBVDB_API gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out);
 /* device pointers of the atlas storage (interior bricks, apron records) for consumers */
 GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron);
 /* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
