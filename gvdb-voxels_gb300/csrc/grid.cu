@@ -7,6 +7,7 @@
 // counters it needs to size allocations (bounding box, unique key counts, used
 // leaf count, subcell-list length), each as one small pinned copy.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -120,6 +121,10 @@ struct gbvdb_grid_s {
     bool lists_valid = false;
     DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted;
     DevBuf list_cnt, list_off, list_pts;
+    DevBuf offs_buf;
+    int noffs = 0;
+    float offs_R = -1.f;
+    uint32_t offs_T = 0;
 
     // scratch
     DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
@@ -608,7 +613,7 @@ struct gbvdb_grid_s {
         memcpy(&binned, pinned + 16, 4);
         mark();
         grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
-        launch_bin_scatter(p, trans, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
+        launch_bin_scatter(p, trans, R, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
                            ptr<float4>(sorted), stream);
         check_launch("bin_scatter");
         mark();
@@ -643,6 +648,37 @@ struct gbvdb_grid_s {
                          ptr<uint32_t>(list_cnt), ptr<float>(list_pts), stream);
         check_launch("lists");
         lists_valid = true;
+    }
+
+    // candidate home-bin offsets d = H - S (subcell units) with their integer lower
+    // bound lb2 on the squared distance from any point of bin H to the voxels of
+    // subcell S, sorted ascending; offsets with lb2 >= T are dropped
+    void build_offsets(int lo_off, int hi_off, float T, float R) {
+        if (offs_R == R && offs_T == bits_of(T) && noffs > 0) return;
+        std::vector<std::array<int, 4>> v;
+        auto gap = [](int d) { return d > 0 ? 4 * d - 3 : (d < 0 ? -4 * d - 4 : 0); };
+        for (int dz = lo_off; dz <= hi_off; dz++)
+            for (int dy = lo_off; dy <= hi_off; dy++)
+                for (int dx = lo_off; dx <= hi_off; dx++) {
+                    int lb2 = gap(dx) * gap(dx) + gap(dy) * gap(dy) + gap(dz) * gap(dz);
+                    if (!((float)lb2 < T)) continue;
+                    v.push_back({dx, dy, dz, lb2});
+                }
+        std::stable_sort(v.begin(), v.end(), [](const std::array<int, 4>& a, const std::array<int, 4>& b) {
+            return a[3] < b[3];
+        });
+        noffs = (int)v.size();
+        grow(offs_buf, (size_t)std::max(noffs, 1) * 16);
+        if (noffs) {
+            std::vector<int> flat((size_t)noffs * 4);
+            for (int i = 0; i < noffs; i++)
+                for (int k = 0; k < 4; k++) flat[(size_t)i * 4 + k] = v[(size_t)i][(size_t)k];
+            memcpy(pinned, flat.data(), flat.size() * 4);
+            check(cudaMemcpyAsync(offs_buf.p, pinned, flat.size() * 4, cudaMemcpyHostToDevice, stream), "offsets");
+            sync();
+        }
+        offs_R = R;
+        offs_T = bits_of(T);
     }
 
     static uint32_t bits_of(float f) {
@@ -701,8 +737,10 @@ struct gbvdb_grid_s {
             launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
                                 interior, stream);
         } else {
+            gp.dense_min = 2048;
+            build_offsets(gp.lo_off, gp.hi_off, T, sc_R);
             launch_gather(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
-                          ptr<float4>(sorted), gp, interior, stream);
+                          ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, interior, stream);
         }
         check_launch("gather");
         mark();
@@ -774,7 +812,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot};
     for (DevBuf* b : bufs) g->release(*b);

@@ -76,7 +76,7 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
 void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                       uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals,
                       cudaStream_t s);
-void launch_bin_scatter(PointSrc p, float3 trans, const int* bin_of, const uint32_t* rank_of,
+void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s);
 
 struct GatherParams {
@@ -88,10 +88,12 @@ struct GatherParams {
     int dtype;         // storage type
     int ax, ay;        // atlas axis counts
     int lo_off, hi_off;  // home-bin offset range H - S (subcell units)
+    int dense_min;     // bricks with more candidate points use the gather form
 };
+// offs: candidate home-bin offsets {dx, dy, dz, lb2} (H - S, subcell units), ascending lb2
 void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
-                   const uint32_t* bin_off, const float4* pts, const GatherParams& gp, void* interior,
-                   cudaStream_t s);
+                   const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
+                   void* interior, cudaStream_t s);
 // materialized subcell lists (export and the fallback gather)
 void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                        uint32_t* cnt, cudaStream_t s);

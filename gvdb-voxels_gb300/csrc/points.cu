@@ -110,14 +110,36 @@ __global__ void k_bin_count(TreeView t, PointSrc p, float3 trans, float R, const
     }
 }
 
-__global__ void k_bin_scatter(PointSrc p, float3 trans, const int* __restrict__ bin_of, const uint32_t* __restrict__ rank_of,
-                              const uint32_t* __restrict__ bin_off, float4* __restrict__ sorted) {
+// Binned record of one point: position (after +trans) and, in .w, its subcell
+// membership range relative to its home subcell H = floor(w/4): six signed
+// nibbles lo_x, hi_x, lo_y, hi_y, lo_z, hi_z with lo = int(w-R)/4 - H and
+// hi = int(w+1+R)/4 - H (fits for R <= 11, the range the brick-tiled gather serves).
+__device__ __forceinline__ int pack_ranges(const float* w, float R) {
+    int packed = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int lo, hi;
+        sc_range(w[a], R, lo, hi);
+        int h = ((int)w[a]) >> 2;
+        int l = (lo >> 2) - h, u = (hi >> 2) - h;  // lo, hi are multiples of 4 (lo may be negative)
+        packed |= ((l & 15) << (8 * a)) | ((u & 15) << (8 * a + 4));
+    }
+    return packed;
+}
+__device__ __forceinline__ int nib(int packed, int k) {  // signed nibble k (0..5 in lo_x,hi_x,lo_y,...)
+    return (packed << (28 - 4 * k)) >> 28;
+}
+
+__global__ void k_bin_scatter(PointSrc p, float3 trans, float R, const int* __restrict__ bin_of,
+                              const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
+                              float4* __restrict__ sorted) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         int b = bin_of[i];
         if (b < 0) continue;
         float x, y, z;
         load_pos(p.base, i, p.stride, p.off, x, y, z);
-        sorted[bin_off[b] + rank_of[i]] = make_float4(fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z), 0.f);
+        float w[3] = {fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z)};
+        sorted[bin_off[b] + rank_of[i]] = make_float4(w[0], w[1], w[2], __int_as_float(pack_ranges(w, R)));
     }
 }
 
@@ -175,33 +197,48 @@ __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out)
 }
 
 constexpr int kGatherThreads = 256;
-constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 15 -> offsets within +-1 brick)
+constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 11 -> offsets within +-1 brick)
 
-// One block per linked leaf.  Candidate home bins of the 3x3x3 brick
-// neighbourhood are collected in shared memory; warps take bins, lanes take 32
-// points of a bin at a time, and for every point every lane evaluates 2 voxels
-// of each member subcell of this brick, reducing min d^2 into a shared tile
-// with shared-memory atomics.  One coalesced write of the brick at the end.
+// One block per linked leaf.  Setup: the 3x3x3 neighbour ranks and the
+// non-empty home bins that can hold members of this brick's subcells.  Then
+// one of two forms, chosen per brick by its candidate point count:
+//
+// scatter (sparse bricks): warps take bins, lanes take 32 points of a bin; for
+//   each point the warp visits the point's member subcells of this brick, 2
+//   voxels per lane per subcell, and reduces min d^2 into the shared tile with
+//   shared atomics (skipped when d^2 >= the static cutoff T).
+// gather (dense bricks): each warp owns whole subcells in turn (2 voxels per
+//   lane, min d^2 in registers).  It visits candidate home bins in ascending
+//   order of their lower-bound distance lb^2 to the subcell (host table) and
+//   stops at the first bin with lb^2 >= wmax, the largest current minimum of
+//   its 64 voxels; a point is evaluated only if it is a member and its own
+//   lower bound to the subcell's voxel box is below wmax.  Skipped points
+//   cannot lower any voxel's minimum, so the result is exact.
+//
+// One coalesced write of the brick from the tile at the end.
 template <typename T>
 __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int* __restrict__ linked,
                                                            const uint32_t* __restrict__ scmap,
                                                            const uint32_t* __restrict__ bin_off,
-                                                           const float4* __restrict__ pts, GatherParams gp,
-                                                           T* __restrict__ interior) {
+                                                           const float4* __restrict__ pts,
+                                                           const int4* __restrict__ offs, int noffs,
+                                                           GatherParams gp, T* __restrict__ interior) {
     __shared__ uint32_t tile[4096];
     __shared__ int nrank[27];
     __shared__ uint32_t cb_beg[kMaxBins];
     __shared__ uint32_t cb_cnt[kMaxBins];
+    __shared__ int cb_home[kMaxBins];
     __shared__ int ncb;
     __shared__ int cursor;
+    __shared__ unsigned int ncand;
 
     const int leaf = linked[blockIdx.x];
     const Node nd = t.nodes[0][leaf];
     const int slot = slot_of_value(nd.value, gp.ax, gp.ay);
     if (slot < 0) return;
     const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+    const int sx0 = ox >> 2, sy0 = oy >> 2, sz0 = oz >> 2;
 
-    for (int v = threadIdx.x; v < 4096; v += blockDim.x) tile[v] = gp.tbits;
     if (threadIdx.x < 27) {
         int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
         int r = -1;
@@ -216,14 +253,14 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int
         }
         nrank[threadIdx.x] = r;
     }
-    if (threadIdx.x == 0) { ncb = 0; cursor = 0; }
+    if (threadIdx.x == 0) { ncb = 0; cursor = 0; ncand = 0; }
     __syncthreads();
 
     // candidate home bins: H (in subcells) within [S + lo_off, S + hi_off] of some S of this brick
-    const int sx0 = ox >> 2, sy0 = oy >> 2, sz0 = oz >> 2;
-    const int span = 4 + gp.hi_off - gp.lo_off;  // candidates per axis
-    const int ncand = span * span * span;
-    for (int c = threadIdx.x; c < ncand; c += blockDim.x) {
+    const int span = 4 + gp.hi_off - gp.lo_off;
+    const int nc = span * span * span;
+    unsigned local_pts = 0;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
         int cx = c % span, cy = (c / span) % span, cz = c / (span * span);
         int hx = sx0 + gp.lo_off + cx, hy = sy0 + gp.lo_off + cy, hz = sz0 + gp.lo_off + cz;
         if (hx < 0 || hy < 0 || hz < 0) continue;
@@ -237,72 +274,136 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int
             int k = atomicAdd(&ncb, 1);
             cb_beg[k] = b;
             cb_cnt[k] = e - b;
+            cb_home[k] = ((hx - sx0 + 16) << 10) | ((hy - sy0 + 16) << 5) | (hz - sz0 + 16);  // relative, biased
+            local_pts += e - b;
         }
     }
+    for (int o = 16; o > 0; o >>= 1) local_pts += __shfl_down_sync(0xFFFFFFFFu, local_pts, o);
+    if ((threadIdx.x & 31) == 0 && local_pts) atomicAdd(&ncand, local_pts);
     __syncthreads();
 
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int vx = lane & 3, vy = (lane >> 2) & 3, vz = lane >> 4;
-    const float fvx = (float)vx, fvy = (float)vy;
-    const int nb = ncb;
-    while (true) {
-        int e = 0;
-        if (lane == 0) e = atomicAdd(&cursor, 1);
-        e = __shfl_sync(0xFFFFFFFFu, e, 0);
-        if (e >= nb) break;
-        const uint32_t beg = cb_beg[e], cnt = cb_cnt[e];
-        for (uint32_t base = 0; base < cnt; base += 32) {
-            const int nv = (int)min(32u, cnt - base);
-            float4 q = make_float4(0, 0, 0, 0);
-            int box = 0;  // packed member range of this brick: lx0,lx1,ly0,ly1,lz0,lz1 (2 bits each), bit 12 = empty
-            if (lane < nv) {
-                q = pts[beg + base + lane];
-                int lo, hi, rng[6];
-                bool empty = false;
-                const float w3[3] = {q.x, q.y, q.z};
-                const int o3[3] = {ox, oy, oz};
-#pragma unroll
-                for (int a = 0; a < 3; a++) {
-                    sc_range(w3[a], gp.R, lo, hi);
-                    int l0 = lo <= o3[a] ? 0 : (lo - o3[a]) >> 2;
-                    int l1 = hi < o3[a] ? -1 : min(3, (hi - o3[a]) >> 2);
-                    if (l0 > 3 || l1 < l0) empty = true;
-                    rng[2 * a] = l0;
-                    rng[2 * a + 1] = l1;
+    const float Tf = __uint_as_float(gp.tbits);
+
+    if (ncand <= (unsigned)gp.dense_min) {
+        // ------------------------------------------------------ scatter form
+        for (int v = threadIdx.x; v < 4096; v += blockDim.x) tile[v] = gp.tbits;
+        __syncthreads();
+        const float fvx = (float)vx, fvy = (float)vy;
+        const int nb = ncb;
+        while (true) {
+            int e = 0;
+            if (lane == 0) e = atomicAdd(&cursor, 1);
+            e = __shfl_sync(0xFFFFFFFFu, e, 0);
+            if (e >= nb) break;
+            const uint32_t beg = cb_beg[e], cnt = cb_cnt[e];
+            // home subcell relative to the brick's first subcell
+            const int home = cb_home[e];
+            const int dhx = ((home >> 10) & 31) - 16, dhy = ((home >> 5) & 31) - 16, dhz = (home & 31) - 16;
+            for (uint32_t base = 0; base < cnt; base += 32) {
+                const int nv = (int)min(32u, cnt - base);
+                float4 q = make_float4(0, 0, 0, 0);
+                int box = 1 << 12;
+                if (lane < nv) {
+                    q = pts[beg + base + lane];
+                    const int pk = __float_as_int(q.w);
+                    int l0x = max(0, dhx + nib(pk, 0)), l1x = min(3, dhx + nib(pk, 1));
+                    int l0y = max(0, dhy + nib(pk, 2)), l1y = min(3, dhy + nib(pk, 3));
+                    int l0z = max(0, dhz + nib(pk, 4)), l1z = min(3, dhz + nib(pk, 5));
+                    if (l0x <= l1x && l0y <= l1y && l0z <= l1z)
+                        box = l0x | (l1x << 2) | (l0y << 4) | (l1y << 6) | (l0z << 8) | (l1z << 10);
                 }
-                box = empty ? (1 << 12)
-                            : (rng[0] | (rng[1] << 2) | (rng[2] << 4) | (rng[3] << 6) | (rng[4] << 8) | (rng[5] << 10));
-            } else {
-                box = 1 << 12;
-            }
-            unsigned live = __ballot_sync(0xFFFFFFFFu, (box & (1 << 12)) == 0);
-            while (live) {
-                const int j = __ffs(live) - 1;
-                live &= live - 1;
-                const float px = __shfl_sync(0xFFFFFFFFu, q.x, j);
-                const float py = __shfl_sync(0xFFFFFFFFu, q.y, j);
-                const float pz = __shfl_sync(0xFFFFFFFFu, q.z, j);
-                const int bxv = __shfl_sync(0xFFFFFFFFu, box, j);
-                const int lx0 = bxv & 3, lx1 = (bxv >> 2) & 3, ly0 = (bxv >> 4) & 3, ly1 = (bxv >> 6) & 3;
-                const int lz0 = (bxv >> 8) & 3, lz1 = (bxv >> 10) & 3;
-                for (int lz = lz0; lz <= lz1; lz++) {
-                    const float z0 = (float)(oz + 4 * lz + vz), z1 = (float)(oz + 4 * lz + vz + 2);
-                    const float dz0 = fsub(pz, z0), dz1 = fsub(pz, z1);
-                    for (int ly = ly0; ly <= ly1; ly++) {
-                        const float dy = fsub(py, (float)(oy + 4 * ly) + fvy);
-                        for (int lx = lx0; lx <= lx1; lx++) {
-                            const float dx = fsub(px, (float)(ox + 4 * lx) + fvx);
-                            const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                            const float d0 = __fmaf_rn(dz0, dz0, dxy);
-                            const float d1 = __fmaf_rn(dz1, dz1, dxy);
-                            const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
-                            const uint32_t b0 = __float_as_uint(d0), b1 = __float_as_uint(d1);
-                            if (b0 < gp.tbits) atomicMin(&tile[v0], b0);
-                            if (b1 < gp.tbits) atomicMin(&tile[v0 + 512], b1);
+                unsigned live = __ballot_sync(0xFFFFFFFFu, (box & (1 << 12)) == 0);
+                while (live) {
+                    const int j = __ffs(live) - 1;
+                    live &= live - 1;
+                    const float px = __shfl_sync(0xFFFFFFFFu, q.x, j);
+                    const float py = __shfl_sync(0xFFFFFFFFu, q.y, j);
+                    const float pz = __shfl_sync(0xFFFFFFFFu, q.z, j);
+                    const int bxv = __shfl_sync(0xFFFFFFFFu, box, j);
+                    const int lx0 = bxv & 3, lx1 = (bxv >> 2) & 3, ly0 = (bxv >> 4) & 3, ly1 = (bxv >> 6) & 3;
+                    const int lz0 = (bxv >> 8) & 3, lz1 = (bxv >> 10) & 3;
+                    for (int lz = lz0; lz <= lz1; lz++) {
+                        const float z0 = (float)(oz + 4 * lz + vz), z1 = (float)(oz + 4 * lz + vz + 2);
+                        const float dz0 = fsub(pz, z0), dz1 = fsub(pz, z1);
+                        for (int ly = ly0; ly <= ly1; ly++) {
+                            const float dy = fsub(py, (float)(oy + 4 * ly) + fvy);
+                            for (int lx = lx0; lx <= lx1; lx++) {
+                                const float dx = fsub(px, (float)(ox + 4 * lx) + fvx);
+                                const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                                const float d0 = __fmaf_rn(dz0, dz0, dxy);
+                                const float d1 = __fmaf_rn(dz1, dz1, dxy);
+                                const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
+                                const uint32_t b0 = __float_as_uint(d0), b1 = __float_as_uint(d1);
+                                if (b0 < gp.tbits) atomicMin(&tile[v0], b0);
+                                if (b1 < gp.tbits) atomicMin(&tile[v0 + 512], b1);
+                            }
                         }
                     }
                 }
             }
+        }
+    } else {
+        // ------------------------------------------------------- gather form
+        const int nw = blockDim.x >> 5;
+        for (int sc = warp; sc < 64; sc += nw) {
+            const int lx = sc & 3, ly = (sc >> 2) & 3, lz = sc >> 4;
+            const int Sx = sx0 + lx, Sy = sy0 + ly, Sz = sz0 + lz;
+            const float fx = (float)(ox + 4 * lx + vx), fy = (float)(oy + 4 * ly + vy);
+            const float fz0 = (float)(oz + 4 * lz + vz), fz1 = fz0 + 2.0f;
+            const float blx = (float)(4 * Sx), bhx = blx + 3.0f;
+            const float bly = (float)(4 * Sy), bhy = bly + 3.0f;
+            const float blz = (float)(4 * Sz), bhz = blz + 3.0f;
+            float m0 = Tf, m1 = Tf;
+            float wmax = Tf;
+            for (int e = 0; e < noffs; e++) {
+                const int4 o = offs[e];
+                if ((float)o.w >= wmax) break;
+                const int hx = Sx + o.x, hy = Sy + o.y, hz = Sz + o.z;
+                if (hx < 0 || hy < 0 || hz < 0) continue;
+                const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
+                const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
+                if (r < 0) continue;
+                const unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
+                const uint32_t beg = __ldg(bin_off + bin), end = __ldg(bin_off + bin + 1);
+                for (uint32_t base = beg; base < end; base += 32) {
+                    const uint32_t j = base + lane;
+                    bool ok = false;
+                    float4 q = make_float4(0, 0, 0, 0);
+                    if (j < end) {
+                        q = pts[j];
+                        const int pk = __float_as_int(q.w);
+                        // membership of S: lo <= S - H <= hi on every axis
+                        ok = nib(pk, 0) <= -o.x && -o.x <= nib(pk, 1) && nib(pk, 2) <= -o.y && -o.y <= nib(pk, 3) &&
+                             nib(pk, 4) <= -o.z && -o.z <= nib(pk, 5);
+                        if (ok) {
+                            const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q.x), fsub(q.x, bhx)));
+                            const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q.y), fsub(q.y, bhy)));
+                            const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q.z), fsub(q.z, bhz)));
+                            const float lb = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
+                            ok = lb < wmax;
+                        }
+                    }
+                    unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
+                    while (live) {
+                        const int k = __ffs(live) - 1;
+                        live &= live - 1;
+                        const float px = __shfl_sync(0xFFFFFFFFu, q.x, k);
+                        const float py = __shfl_sync(0xFFFFFFFFu, q.y, k);
+                        const float pz = __shfl_sync(0xFFFFFFFFu, q.z, k);
+                        const float dx = fsub(px, fx), dy = fsub(py, fy);
+                        const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                        const float dz0 = fsub(pz, fz0), dz1 = fsub(pz, fz1);
+                        m0 = fminf(m0, __fmaf_rn(dz0, dz0, dxy));
+                        m1 = fminf(m1, __fmaf_rn(dz1, dz1, dxy));
+                    }
+                }
+                wmax = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(m0, m1))));
+            }
+            const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
+            tile[v0] = __float_as_uint(m0);
+            tile[v0 + 512] = __float_as_uint(m1);
         }
     }
     __syncthreads();
@@ -391,21 +492,24 @@ void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, cons
     if (p.n <= 0) return;
     k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, p, trans, R, scmap, bin_cnt, bin_of, rank_of, totals);
 }
-void launch_bin_scatter(PointSrc p, float3 trans, const int* bin_of, const uint32_t* rank_of, const uint32_t* bin_off,
-                        float4* sorted, cudaStream_t s) {
+void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
+                        const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, bin_of, rank_of, bin_off, sorted);
+    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, bin_of, rank_of, bin_off, sorted);
 }
 void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
-                   const uint32_t* bin_off, const float4* pts, const GatherParams& gp, void* interior, cudaStream_t s) {
+                   const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
+                   void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
     if (gp.dtype == 3)
-        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp, (float*)interior);
+        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs, noffs, gp,
+                                                                     (float*)interior);
     else if (gp.dtype == 100)
-        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp, (__half*)interior);
+        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs, noffs, gp,
+                                                                      (__half*)interior);
     else
-        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, gp,
-                                                                            (__nv_bfloat16*)interior);
+        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs,
+                                                                            noffs, gp, (__nv_bfloat16*)interior);
 }
 void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* cnt,
                        cudaStream_t s) {
