@@ -62,7 +62,7 @@ __global__ void k_fill_u32(uint32_t* p, long long n, uint32_t v) {
 // every apron voxel copies the matching interior voxel of its neighbour, or the
 // boundary value when no active brick contains that index-space position.
 template <typename T>
-__global__ void k_apron(TreeView t, const AtlasNode* __restrict__ amap, int ax, int ay, const T* __restrict__ interior,
+__global__ void k_apron(TreeView t, LeafGrid lg, const AtlasNode* __restrict__ amap, int ax, int ay, const T* __restrict__ interior,
                         T* __restrict__ apron, T boundval) {
     __shared__ int nslot[27];
     const int s = blockIdx.x;
@@ -72,7 +72,9 @@ __global__ void k_apron(TreeView t, const AtlasNode* __restrict__ amap, int ax, 
         int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
         int ns = -1;
         if (dx | dy | dz) {
-            long long nl = get_leaf_at_voxel(t, an.pos[0] + 16 * dx, an.pos[1] + 16 * dy, an.pos[2] + 16 * dz);
+            int px = an.pos[0] + 16 * dx, py = an.pos[1] + 16 * dy, pz = an.pos[2] + 16 * dz;
+            long long nl = lg.cells ? ((px < 0 || py < 0 || pz < 0) ? -1 : lookup_leaf(lg, t, px, py, pz))
+                                    : get_leaf_at_voxel(t, px, py, pz);
             if (nl >= 0) ns = slot_of_value(t.nodes[0][nl].value, ax, ay);
         }
         nslot[threadIdx.x] = ns;
@@ -220,18 +222,18 @@ void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s) {
     if (n <= 0) return;
     k_fill_u32<<<gs_blocks(n, 256), 256, 0, s>>>(p, n, v);
 }
-void launch_apron(const TreeView& t, const AtlasNode* amap, int used, int ax, int ay, int esize,
+void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, int used, int ax, int ay, int esize,
                   const void* interior, void* apron, uint32_t boundbits, cudaStream_t s) {
     if (used <= 0) return;
     if (esize == 4) {
         float b;
         memcpy(&b, &boundbits, 4);
-        k_apron<float><<<used, 256, 0, s>>>(t, amap, ax, ay, (const float*)interior, (float*)apron, b);
+        k_apron<float><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const float*)interior, (float*)apron, b);
     } else {
         uint16_t b16 = (uint16_t)boundbits;
         __half_raw hr;
         hr.x = b16;
-        k_apron<__half><<<used, 256, 0, s>>>(t, amap, ax, ay, (const __half*)interior, (__half*)apron, __half(hr));
+        k_apron<__half><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const __half*)interior, (__half*)apron, __half(hr));
     }
 }
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out, cudaStream_t s) {

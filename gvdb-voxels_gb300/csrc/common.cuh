@@ -157,6 +157,27 @@ __device__ inline long long get_leaf_at_voxel(const TreeView& t, int wx, int wy,
     return id;
 }
 
+// Dense lookup of the leaf reachable at a brick position: cells[(bx*dy + by)*dz + bz]
+// over the brick box [lo, lo+dim) = leaf index or -1.  Built by traversal, so it
+// answers exactly what get_pos_leaf answers (for trees whose top level is >= 1);
+// cells == nullptr means "not built": fall back to the traversal.
+struct LeafGrid {
+    const int* cells;
+    int lo[3];
+    int dim[3];
+    int lgrange0;
+};
+
+__device__ __forceinline__ long long lookup_leaf(const LeafGrid& g, const TreeView& t, int px, int py, int pz) {
+    if (g.cells) {
+        int bx = (px >> g.lgrange0) - g.lo[0], by = (py >> g.lgrange0) - g.lo[1], bz = (pz >> g.lgrange0) - g.lo[2];
+        if ((unsigned)bx >= (unsigned)g.dim[0] || (unsigned)by >= (unsigned)g.dim[1] || (unsigned)bz >= (unsigned)g.dim[2])
+            return -1;
+        return __ldg(g.cells + ((long long)bx * g.dim[1] + by) * g.dim[2] + bz);
+    }
+    return get_pos_leaf(t, px, py, pz);
+}
+
 // atlas slot from mValue (inverse of getAtlasPos, gvdb_allocator.cpp:705-715)
 __device__ __forceinline__ int slot_of_value(const int32_t* v, int ax, int ay) {
     if (v[0] < 0) return -1;

@@ -122,6 +122,11 @@ struct gbvdb_grid_s {
     DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted;
     DevBuf list_cnt, list_off, list_pts;
     DevBuf offs_buf;
+    // dense leaf lookup over the brick box of every leaf created since the last Clear
+    DevBuf lgrid;
+    LeafGrid lgv{nullptr, {0, 0, 0}, {0, 0, 0}, 4};
+    int lgdom_lo[3] = {0, 0, 0}, lgdom_hi[3] = {0, 0, 0};
+    bool lgdom_init = false;
     int noffs = 0;
     float offs_R = -1.f;
     uint32_t offs_T = 0;
@@ -212,6 +217,8 @@ struct gbvdb_grid_s {
 
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
+        lgdom_init = false;
+        lgv.cells = nullptr;
         atlas_last = 0;
         rebuild_topo = 1;
         sc_valid = false;
@@ -331,6 +338,14 @@ struct gbvdb_grid_s {
         memcpy(&errflag, pinned + 4 * (depth + 1), 4);
         if (errflag) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
         long long added = 0;
+        if (at[1] > at[0]) {  // leaves of this pass lie in the level-0 key domain
+            for (int a = 0; a < 3; a++) {
+                int lo = kd.d[0].lo[a], hi = kd.d[0].lo[a] + kd.d[0].dim[a] - 1;
+                lgdom_lo[a] = lgdom_init ? std::min(lgdom_lo[a], lo) : lo;
+                lgdom_hi[a] = lgdom_init ? std::max(lgdom_hi[a], hi) : hi;
+            }
+            lgdom_init = true;
+        }
         for (int l = 0; l < depth; l++) {
             long long cnt = (long long)at[l + 1] - (long long)at[l];
             if (cnt <= 0) continue;
@@ -350,6 +365,26 @@ struct gbvdb_grid_s {
             added += cnt;
         }
         return added;
+    }
+
+    // rebuild the dense leaf lookup after a topology change (exact: built by traversal)
+    void build_leaf_grid() {
+        lgv.cells = nullptr;
+        if (!lgdom_init || ncnt[0] == 0 || top_lev() == 0) return;
+        long long cells = 1;
+        int dim[3];
+        for (int a = 0; a < 3; a++) {
+            dim[a] = lgdom_hi[a] - lgdom_lo[a] + 1;
+            cells *= dim[a];
+        }
+        if (cells > (1ll << 28)) return;  // too sparse for a dense table: kernels traverse the tree
+        grow(lgrid, (size_t)cells * 4);
+        check(cudaMemsetAsync(lgrid.p, 0xFF, (size_t)cells * 4, stream), "leaf grid clear");
+        launch_build_leaf_grid(view(), ncnt[0], ptr<int>(lgrid), lgdom_lo, dim, lgrange[0], stream);
+        check_launch("leaf grid");
+        lgv.cells = ptr<int>(lgrid);
+        for (int a = 0; a < 3; a++) { lgv.lo[a] = lgdom_lo[a]; lgv.dim[a] = dim[a]; }
+        lgv.lgrange0 = lgrange[0];
     }
 
     void link_all(int depth) {
@@ -402,6 +437,7 @@ struct gbvdb_grid_s {
         allocate_from_bitmap(D, kd, bits);
         mark();
         link_all(D);
+        build_leaf_grid();
         mark();
         // pass 2 (ActivateExtraBricksGPU, VG.cpp:931-1016), only if radius >= 1 (VG.cpp:1207)
         if (radius >= 1) {
@@ -409,12 +445,14 @@ struct gbvdb_grid_s {
             t = view();
             int rlo[3], rhi[3];
             for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
-            launch_keys_box(t, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), nullptr, ptr<int>(misc) + 8,
-                            stream);
+            launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), nullptr,
+                            ptr<int>(misc) + 8, stream);
             check_launch("keys_extra");
-            allocate_from_bitmap(D, kd, bits);
-            mark();
-            link_all(D);
+            if (allocate_from_bitmap(D, kd, bits) > 0) {
+                mark();
+                link_all(D);
+                build_leaf_grid();
+            }
             mark();
         }
     }
@@ -436,7 +474,7 @@ struct gbvdb_grid_s {
         TreeView t = view();
         int rlo[3], rhi[3];
         for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
-        launch_keys_box(t, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), ptr<int>(markers),
+        launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), ptr<int>(markers),
                         ptr<int>(misc) + 8, stream);
         check_launch("keys_incr");
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
@@ -462,6 +500,7 @@ struct gbvdb_grid_s {
             launch_delink_upper(t, lev, ncnt[lev], stream);
             check_launch("delink_upper");
         }
+        build_leaf_grid();
         // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148)
         check(cudaMemsetAsync(ptr<char>(misc) + 64, 0, 8, stream), "count clear");
         launch_count_flags(ptr<Node>(nodes[0]), ncnt[0], reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 64),
@@ -598,7 +637,7 @@ struct gbvdb_grid_s {
         unsigned long long* totals = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 128);
         check(cudaMemsetAsync(totals, 0, 16, stream), "totals clear");
         TreeView t = view();
-        launch_bin_count(t, p, trans, R, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
+        launch_bin_count(t, lgv, p, trans, R, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
                          ptr<uint32_t>(rank_of), totals, stream);
         check_launch("bin_count");
         grow(scan_tmp, scan_tmp_bytes(nbins));
@@ -640,11 +679,11 @@ struct gbvdb_grid_s {
         grow(list_pts, (size_t)std::max(sc_len, 1ll) * 12);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
         TreeView t = view();
-        launch_list_count(t, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt), stream);
+        launch_list_count(t, lgv, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt), stream);
         grow(scan_tmp, scan_tmp_bytes(nsub));
         scan_exclusive_u32(ptr<uint32_t>(list_cnt), ptr<uint32_t>(list_off), nsub, scan_tmp.p, stream);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
-        launch_list_fill(t, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
+        launch_list_fill(t, lgv, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
                          ptr<uint32_t>(list_cnt), ptr<float>(list_pts), stream);
         check_launch("lists");
         lists_valid = true;
@@ -739,7 +778,7 @@ struct gbvdb_grid_s {
         } else {
             gp.dense_min = 2048;
             build_offsets(gp.lo_off, gp.hi_off, T, sc_R);
-            launch_gather(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
+            launch_gather(t, lgv, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
                           ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, interior, stream);
         }
         check_launch("gather");
@@ -758,7 +797,7 @@ struct gbvdb_grid_s {
         else if (ch[chan].dtype == GBVDB_T_HALF) bb = f2h_bits(boundval);
         else bb = f2bf_bits(boundval);
         TreeView t = view();
-        launch_apron(t, ptr<AtlasNode>(amap), atlas_last, ax, ay, ch[chan].esize, ch[chan].interior.p,
+        launch_apron(t, lgv, ptr<AtlasNode>(amap), atlas_last, ax, ay, ch[chan].esize, ch[chan].interior.p,
                      ch[chan].apron_buf.p, bb, stream);
         check_launch("apron");
         mark();
@@ -812,7 +851,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot};
     for (DevBuf* b : bufs) g->release(*b);

@@ -36,9 +36,11 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tm
 void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s);
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
                        uint32_t* bitmap, int* err, cudaStream_t s);
-void launch_keys_box(const TreeView& t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
-                     int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
+void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
+                     int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
                      int* err, cudaStream_t s);
+void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
+                            int lgrange0, cudaStream_t s);
 void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s);
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
@@ -58,7 +60,7 @@ void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag,
 void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
                          cudaStream_t s);
 void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s);
-void launch_apron(const TreeView& t, const AtlasNode* amap, int used, int ax, int ay, int esize,
+void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, int used, int ax, int ay, int esize,
                   const void* interior, void* apron, uint32_t boundbits, cudaStream_t s);
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out,
                           cudaStream_t s);
@@ -73,7 +75,7 @@ cudaError_t checksum_noalloc(const AtlasNode* amap, int used, int dtype, const v
 
 // ---- points.cu
 void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s);
-void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                       uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals,
                       cudaStream_t s);
 void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
@@ -91,13 +93,13 @@ struct GatherParams {
     int dense_min;     // bricks with more candidate points use the gather form
 };
 // offs: candidate home-bin offsets {dx, dy, dz, lb2} (H - S, subcell units), ascending lb2
-void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
+void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    void* interior, cudaStream_t s);
 // materialized subcell lists (export and the fallback gather)
-void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                        uint32_t* cnt, cudaStream_t s);
-void launch_list_fill(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                       const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s);
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s);

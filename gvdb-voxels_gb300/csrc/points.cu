@@ -50,15 +50,15 @@ __global__ void k_linked_list(const Node* leaves, long long n, const uint32_t* s
     if (leaves[i].parent != kUndef64) linked[scmap[i]] = (int)i;
 }
 
-__device__ __forceinline__ long long linked_leaf(const TreeView& t, int x, int y, int z) {
-    long long l = get_pos_leaf(t, x, y, z);
+__device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeView& t, int x, int y, int z) {
+    long long l = lookup_leaf(lg, t, x, y, z);
     if (l < 0 || t.nodes[0][l].parent == kUndef64) return -1;
     return l;
 }
 
 // Home-subcell counting pass + total subcell-list length (the reference's
 // pSCPntsLength) + orphans (valid points whose home leaf is not linked).
-__global__ void k_bin_count(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* __restrict__ scmap,
+__global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* __restrict__ scmap,
                            uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
     unsigned long long members = 0, orphans = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
@@ -67,7 +67,7 @@ __global__ void k_bin_count(TreeView t, PointSrc p, float3 trans, float R, const
         int h[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) h[a] = ((int)w[a]) & ~(kSc - 1);
-        long long leaf = linked_leaf(t, h[0], h[1], h[2]);
+        long long leaf = linked_leaf(lg, t, h[0], h[1], h[2]);
         if (leaf < 0) {
             bin_of[i] = -2;
             orphans++;
@@ -94,7 +94,7 @@ __global__ void k_bin_count(TreeView t, PointSrc p, float3 trans, float R, const
                 int y0 = max(lo[1], by << 4), y1 = min(hi[1], (by << 4) + 12);
                 for (int bz = lo[2] >> 4; bz <= hi[2] >> 4; bz++) {
                     int z0 = max(lo[2], bz << 4), z1 = min(hi[2], (bz << 4) + 12);
-                    if (linked_leaf(t, bx << 4, by << 4, bz << 4) < 0) continue;
+                    if (linked_leaf(lg, t, bx << 4, by << 4, bz << 4) < 0) continue;
                     members += (unsigned long long)(((x1 - x0) >> 2) + 1) * (((y1 - y0) >> 2) + 1) * (((z1 - z0) >> 2) + 1);
                 }
             }
@@ -217,7 +217,7 @@ constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 11 -> 
 //
 // One coalesced write of the brick from the tile at the end.
 template <typename T>
-__global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int* __restrict__ linked,
+__global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
                                                            const uint32_t* __restrict__ scmap,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int
         } else {
             int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
             if (px >= 0 && py >= 0 && pz >= 0) {
-                long long l = linked_leaf(t, px, py, pz);
+                long long l = linked_leaf(lg, t, px, py, pz);
                 if (l >= 0) r = (int)scmap[l];
             }
         }
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, const int
 // ---- materialized subcell lists (reference-shaped; export + fallback) ----
 
 template <bool kFill>
-__device__ void list_points(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+__device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
                             uint32_t* cnt, const uint32_t* off, float* out3) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float w[3];
@@ -425,7 +425,7 @@ __device__ void list_points(const TreeView& t, PointSrc p, float3 trans, float R
             for (int sy = lo[1]; sy <= hi[1]; sy += kSc)
                 for (int sz = lo[2]; sz <= hi[2]; sz += kSc) {
                     if (sx < 0 || sy < 0 || sz < 0) continue;
-                    long long leaf = linked_leaf(t, sx, sy, sz);
+                    long long leaf = linked_leaf(lg, t, sx, sy, sz);
                     if (leaf < 0) continue;
                     const Node& nd = t.nodes[0][leaf];
                     int loc = (((sz - nd.pos[2]) >> 2) << 4) | (((sy - nd.pos[1]) >> 2) << 2) | ((sx - nd.pos[0]) >> 2);
@@ -440,12 +440,13 @@ __device__ void list_points(const TreeView& t, PointSrc p, float3 trans, float R
                 }
     }
 }
-__global__ void k_list_count(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* cnt) {
-    list_points<false>(t, p, trans, R, scmap, cnt, nullptr, nullptr);
+__global__ void k_list_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                             uint32_t* cnt) {
+    list_points<false>(t, lg, p, trans, R, scmap, cnt, nullptr, nullptr);
 }
-__global__ void k_list_fill(TreeView t, PointSrc p, float3 trans, float R, const uint32_t* scmap, const uint32_t* off,
-                            uint32_t* cursor, float* out3) {
-    list_points<true>(t, p, trans, R, scmap, cursor, off, out3);
+__global__ void k_list_fill(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                            const uint32_t* off, uint32_t* cursor, float* out3) {
+    list_points<true>(t, lg, p, trans, R, scmap, cursor, off, out3);
 }
 
 // reference-shaped gather over materialized lists: one block per linked leaf,
@@ -487,39 +488,40 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
     if (n <= 0) return;
     k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
 }
-void launch_bin_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* bin_cnt,
-                      int* bin_of, uint32_t* rank_of, unsigned long long* totals, cudaStream_t s) {
+void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R,
+                      const uint32_t* scmap, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
+                      unsigned long long* totals, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, p, trans, R, scmap, bin_cnt, bin_of, rank_of, totals);
+    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, scmap, bin_cnt, bin_of, rank_of, totals);
 }
 void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
     if (p.n <= 0) return;
     k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, bin_of, rank_of, bin_off, sorted);
 }
-void launch_gather(const TreeView& t, const int* linked, long long nbricks, const uint32_t* scmap,
+void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
     if (gp.dtype == 3)
-        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs, noffs, gp,
+        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs, noffs, gp,
                                                                      (float*)interior);
     else if (gp.dtype == 100)
-        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs, noffs, gp,
+        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs, noffs, gp,
                                                                       (__half*)interior);
     else
-        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, linked, scmap, bin_off, pts, offs,
+        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs,
                                                                             noffs, gp, (__nv_bfloat16*)interior);
 }
-void launch_list_count(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, uint32_t* cnt,
-                       cudaStream_t s) {
+void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R,
+                       const uint32_t* scmap, uint32_t* cnt, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, p, trans, R, scmap, cnt);
+    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, scmap, cnt);
 }
-void launch_list_fill(const TreeView& t, PointSrc p, float3 trans, float R, const uint32_t* scmap, const uint32_t* off,
-                      uint32_t* cursor, float* out3, cudaStream_t s) {
+void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+                      const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, p, trans, R, scmap, off, cursor, out3);
+    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, scmap, off, cursor, out3);
 }
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s) {

@@ -91,7 +91,7 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
 // gvdbCalcExtraBrickId (hi_mul = 2, PT.cuh:467-512) and gvdbCalcIncreExtraBrickId
 // (hi_mul = 1, PT.cuh:420-465): every node position in the point's box that is not
 // reachable from the root becomes a key; reachable leaves are marked (incremental).
-__global__ void k_keys_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
+__global__ void k_keys_box(TreeView t, LeafGrid lg, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
                            int3 rlo, int3 rhi, KeyDomains dom, uint32_t* bm, int* markers, int* err) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float x, y, z;
@@ -119,13 +119,14 @@ __global__ void k_keys_box(TreeView t, PointSrc p, float3 orig, float radius, in
                     for (int nz = lo[2]; nz <= hi[2]; nz += rr) {
                         // guard: positions outside the root (the reference aliases them)
                         if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
-                        long long pid = get_pos_parent(t, nx, ny, nz, lev);
+                        // getPosParent(pos, 0) is the leaf reachable at pos: the dense grid answers it
+                        long long pid = (lev == 0) ? lookup_leaf(lg, t, nx, ny, nz) : get_pos_parent(t, nx, ny, nz, lev);
                         if (pid < 0) {
                             long long b = key_bit(dom.d[lev], nx >> t.lgrange[lev], ny >> t.lgrange[lev], nz >> t.lgrange[lev]);
                             if (b < 0) { atomicOr(err, 1); continue; }
                             set_bit(bm, b);
                         } else if (lev == 0 && markers) {
-                            markers[pid] = 1;
+                            if (__ldcg(markers + pid) == 0) markers[pid] = 1;
                         }
                     }
         }
@@ -211,6 +212,18 @@ __global__ void k_link_write(TreeView t, int lev, long long count, const int* ta
     long long slot = slot_of[i];
     if (slot < 0 || tag[slot] != (int)i) return;
     t.clist[lev + 1][slot] = ((unsigned long long)i << 16) | ((unsigned long long)lev << 8);
+}
+
+// one thread per leaf: the leaf reachable at its own position is entered in the grid
+__global__ void k_build_leaf_grid(TreeView t, long long n, int* cells, int3 lo, int3 dim, int lgrange0) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Node* nd = t.nodes[0] + i;
+    long long r = get_pos_leaf(t, nd->pos[0], nd->pos[1], nd->pos[2]);
+    if (r != i) return;
+    int bx = (nd->pos[0] >> lgrange0) - lo.x, by = (nd->pos[1] >> lgrange0) - lo.y, bz = (nd->pos[2] >> lgrange0) - lo.z;
+    if ((unsigned)bx >= (unsigned)dim.x || (unsigned)by >= (unsigned)dim.y || (unsigned)bz >= (unsigned)dim.z) return;
+    cells[((long long)bx * dim.y + by) * dim.z + bz] = (int)i;
 }
 
 __global__ void k_init_markers(const Node* leaves, long long n, int* markers, int accum) {
@@ -302,13 +315,19 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
                        uint32_t* bitmap, int* err, cudaStream_t s) {
     k_keys_pass1<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, depth, dom, t, bitmap, err);
 }
-void launch_keys_box(const TreeView& t, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
-                     int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
+void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
+                     int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
                      int* err, cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
-    k_keys_box<<<grid_stride_blocks(p.n, 128), 128, 0, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
+    k_keys_box<<<grid_stride_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
                                                              bitmap, markers, err);
+}
+void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
+                            int lgrange0, cudaStream_t s) {
+    if (n <= 0) return;
+    k_build_leaf_grid<<<blocks_for(n, 256), 256, 0, s>>>(t, n, cells, make_int3(lo[0], lo[1], lo[2]),
+                                                         make_int3(dim[0], dim[1], dim[2]), lgrange0);
 }
 void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s) {
     if (nwords <= 0) return;
