@@ -171,6 +171,45 @@ def cpu_baseline(pos, vel, steps=2):
                       "OpenMP %d threads" % (steps + 1, pts0.shape[0], cores)}
 
 
+def ref_cuda_inputs_safe(frames):
+    """The reference's kernels index child lists and subcell counters without
+    bounds checks; they stay in bounds when every coordinate is either < 0
+    (dropped) or > 0 and every box position lies inside the 1024^3 root."""
+    for p in frames:
+        if np.any(p == 0.0) or np.any(p >= 1024 - 4 * R_TOPO - 8):
+            return False
+    return True
+
+
+def bench_ref_cuda(frames_host, steps=3):
+    """The reference's own CUDA kernels (PTX built from its cuda_gvdb_module.cu) under a
+    restatement of its host code (oracle/ref_harness.cu), same frames and calls."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_harness
+
+    if not ref_cuda_inputs_safe(frames_host):
+        return {"unavailable": "inputs would make the reference kernels index outside their buffers"}
+    g = ref_harness.RefGrid(LOG2DIMS)
+    times = []
+    for k in range(steps + 2):
+        pts = frames_host[k % len(frames_host)]
+        g.set_points(pts)
+        g.sync()
+        t0 = time.perf_counter()
+        g.rebuild_topology(R_TOPO)
+        g.update_atlas()
+        g.insert_points_subcell(R_INSERT)
+        g.gather_levelset(RHO)
+        g.update_apron(BOUND)
+        g.sync()
+        if k >= 2:  # frames 0-1 are the two full rebuilds
+            times.append(time.perf_counter() - t0)
+    ms = 1000.0 * float(np.median(times))
+    return {"value": N_FLUID / (ms / 1000.0), "unit": "points/s", "ms_per_frame": ms, "frames": len(times),
+            "what": "reference kernels (PTX of cuda_gvdb_module.cu, --use_fast_math) + host orchestration restated "
+                    "from VolumeGVDB; incremental frames; host wall clock incl. its D2H/H2D pool copies"}
+
+
 def bench_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -358,9 +397,14 @@ def bench_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, vel)
+    if rank == 0 and world == 1 and args.ref_cuda:
+        grid.close()
+        del frames
+        torch.cuda.empty_cache()
+        fh = [(pos + 0.5 * (f + 1) * vel).astype(np.float32) for f in range(5)]
+        line["reference_cuda"] = bench_ref_cuda(fh)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    grid.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
@@ -373,6 +417,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-cuda", action="store_true", help="also time the reference's own CUDA kernels")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

@@ -58,12 +58,14 @@ __global__ void k_fill_u32(uint32_t* p, long long n, uint32_t v) {
 }
 
 // One block per assigned slot.  The 26 neighbour slots are looked up once per
-// brick (one tree traversal each, the reference does one per apron voxel); then
-// every apron voxel copies the matching interior voxel of its neighbour, or the
-// boundary value when no active brick contains that index-space position.
+// brick (the reference traverses the tree once per apron voxel); then the apron
+// record is filled by copies grouped by neighbour: the four y/z faces are rows
+// of the neighbour's boundary planes (16-byte vector loads and stores), the two
+// x faces are strided columns, edges and corners single lines and voxels.  A
+// missing neighbour gives the boundary value.
 template <typename T>
-__global__ void k_apron(TreeView t, LeafGrid lg, const AtlasNode* __restrict__ amap, int ax, int ay, const T* __restrict__ interior,
-                        T* __restrict__ apron, T boundval) {
+__global__ void __launch_bounds__(256) k_apron(TreeView t, LeafGrid lg, const AtlasNode* __restrict__ amap, int ax, int ay,
+                                               const T* __restrict__ interior, T* __restrict__ apron, T boundval) {
     __shared__ int nslot[27];
     const int s = blockIdx.x;
     const AtlasNode an = amap[s];
@@ -81,19 +83,61 @@ __global__ void k_apron(TreeView t, LeafGrid lg, const AtlasNode* __restrict__ a
     }
     __syncthreads();
     T* out = apron + (size_t)s * kApronStride;
-    for (int k = threadIdx.x; k < kApronVox; k += blockDim.x) {
-        int x, y, z;
-        apron_coord(k, x, y, z);
-        int dx = x == 0 ? -1 : (x == 17 ? 1 : 0);
-        int dy = y == 0 ? -1 : (y == 17 ? 1 : 0);
-        int dz = z == 0 ? -1 : (z == 17 ? 1 : 0);
-        int ns = nslot[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
-        T v = boundval;
-        if (ns >= 0) {
-            int lx = (x - 1) & 15, ly = (y - 1) & 15, lz = (z - 1) & 15;
-            v = interior[(size_t)ns * 4096 + (lz << 8) + (ly << 4) + lx];
+    constexpr int V = 16 / sizeof(T);  // elements per 16-byte vector
+    // y and z faces: 4 faces x 256 elements as 16-byte vectors
+    for (int k = threadIdx.x; k < 4 * 256 / V; k += blockDim.x) {
+        const int f = 2 + k / (256 / V);            // 2..5
+        const int e0 = (k % (256 / V)) * V;        // first element within the face
+        const int row = e0 >> 4, col = e0 & 15;    // face [row][col]
+        int dir, src;
+        if (f < 4) {  // y faces: neighbour plane y = 15 (f=2) or 0 (f=3); face [z][x]
+            dir = f == 2 ? (1 * 9 + 0 * 3 + 1) : (1 * 9 + 2 * 3 + 1);
+            src = (row << 8) + ((f == 2 ? 15 : 0) << 4) + col;
+        } else {      // z faces: neighbour plane z = 15 (f=4) or 0 (f=5); face [y][x]
+            dir = f == 4 ? (0 * 9 + 1 * 3 + 1) : (2 * 9 + 1 * 3 + 1);
+            src = ((f == 4 ? 15 : 0) << 8) + (row << 4) + col;
         }
-        out[k] = v;
+        const int ns = nslot[dir];
+        uint4 v;
+        if (ns >= 0) {
+            v = *reinterpret_cast<const uint4*>(interior + (size_t)ns * 4096 + src);
+        } else {
+            T b[V];
+#pragma unroll
+            for (int q = 0; q < V; q++) b[q] = boundval;
+            v = *reinterpret_cast<const uint4*>(b);
+        }
+        *reinterpret_cast<uint4*>(out + f * 256 + e0) = v;
+    }
+    // x faces: columns x = 15 (f=0) and x = 0 (f=1) of the x neighbours; face [z][y]
+    for (int k = threadIdx.x; k < 512; k += blockDim.x) {
+        const int f = k >> 8, e = k & 255, z = e >> 4, y = e & 15;
+        const int ns = nslot[1 * 9 + 1 * 3 + (f == 0 ? 0 : 2)];
+        out[f * 256 + e] = ns >= 0 ? interior[(size_t)ns * 4096 + (z << 8) + (y << 4) + (f == 0 ? 15 : 0)] : boundval;
+    }
+    // edges (12 x 16) and corners (8)
+    for (int k = threadIdx.x; k < 200; k += blockDim.x) {
+        int lx, ly, lz, dir;
+        if (k < 192) {
+            const int e = k >> 4, i = k & 15;
+            const int a = e >> 2, h0 = e & 1, h1 = (e >> 1) & 1;
+            if (a == 0) {         // along x: (y, z) = (h0, h1)
+                lx = i; ly = h0 ? 0 : 15; lz = h1 ? 0 : 15;
+                dir = (h1 ? 2 : 0) * 9 + (h0 ? 2 : 0) * 3 + 1;
+            } else if (a == 1) {  // along y: (x, z) = (h0, h1)
+                ly = i; lx = h0 ? 0 : 15; lz = h1 ? 0 : 15;
+                dir = (h1 ? 2 : 0) * 9 + 1 * 3 + (h0 ? 2 : 0);
+            } else {              // along z: (x, y) = (h0, h1)
+                lz = i; lx = h0 ? 0 : 15; ly = h1 ? 0 : 15;
+                dir = 1 * 9 + (h1 ? 2 : 0) * 3 + (h0 ? 2 : 0);
+            }
+        } else {
+            const int c = k - 192, hx = c & 1, hy = (c >> 1) & 1, hz = c >> 2;
+            lx = hx ? 0 : 15; ly = hy ? 0 : 15; lz = hz ? 0 : 15;
+            dir = (hz ? 2 : 0) * 9 + (hy ? 2 : 0) * 3 + (hx ? 2 : 0);
+        }
+        const int ns = nslot[dir];
+        out[1536 + k] = ns >= 0 ? interior[(size_t)ns * 4096 + (lz << 8) + (ly << 4) + lx] : boundval;
     }
 }
 

@@ -220,23 +220,29 @@ __device__ __forceinline__ void load_pos(const char* base, long long i, int stri
     z = __ldg(q + 2);
 }
 
-// padded-brick coordinate (x,y,z in [0,18)) on the apron shell -> apron record index
+// Apron record layout (1,736 voxels per slot, grouped by the neighbour they copy):
+//   faces  [f*256, +256)  f = 0:-x 1:+x 2:-y 3:+y 4:-z 5:+z; a face holds the 16x16
+//          voxels that match one interior plane of the face neighbour, in that
+//          plane's own order (x faces [z][y], y faces [z][x], z faces [y][x]);
+//   edges  [1536 + e*16, +16) e = 0..3 along x (y,z in {0,17}), 4..7 along y
+//          (x,z), 8..11 along z (x,y); bit order (high coordinate == 17);
+//   corners [1728 + c) c = (z==17)*4 + (y==17)*2 + (x==17).
+// padded-brick coordinate (x,y,z in [0,18)) on the apron shell -> record index
 __host__ __device__ inline int apron_index(int x, int y, int z) {
-    if (z == 0) return y * 18 + x;
-    if (z == 17) return 324 + y * 18 + x;
-    if (y == 0) return 648 + (z - 1) * 18 + x;
-    if (y == 17) return 936 + (z - 1) * 18 + x;
-    if (x == 0) return 1224 + (z - 1) * 16 + (y - 1);
-    return 1480 + (z - 1) * 16 + (y - 1);  // x == 17
-}
-// inverse of apron_index
-__host__ __device__ inline void apron_coord(int i, int& x, int& y, int& z) {
-    if (i < 324) { z = 0; y = i / 18; x = i % 18; return; }
-    if (i < 648) { i -= 324; z = 17; y = i / 18; x = i % 18; return; }
-    if (i < 936) { i -= 648; y = 0; z = 1 + i / 18; x = i % 18; return; }
-    if (i < 1224) { i -= 936; y = 17; z = 1 + i / 18; x = i % 18; return; }
-    if (i < 1480) { i -= 1224; x = 0; z = 1 + i / 16; y = 1 + i % 16; return; }
-    i -= 1480; x = 17; z = 1 + i / 16; y = 1 + i % 16;
+    const bool bx = x == 0 || x == 17, by = y == 0 || y == 17, bz = z == 0 || z == 17;
+    const int hx = x == 17, hy = y == 17, hz = z == 17;
+    const int nb = (int)bx + (int)by + (int)bz;
+    if (nb == 1) {
+        if (bx) return (0 + hx) * 256 + (z - 1) * 16 + (y - 1);
+        if (by) return (2 + hy) * 256 + (z - 1) * 16 + (x - 1);
+        return (4 + hz) * 256 + (y - 1) * 16 + (x - 1);
+    }
+    if (nb == 2) {
+        if (!bx) return 1536 + (hz * 2 + hy) * 16 + (x - 1);
+        if (!by) return 1536 + (4 + hz * 2 + hx) * 16 + (y - 1);
+        return 1536 + (8 + hy * 2 + hx) * 16 + (z - 1);
+    }
+    return 1728 + hz * 4 + hy * 2 + hx;
 }
 
 }  // namespace gbvdb

@@ -132,8 +132,11 @@ struct gbvdb_grid_s {
     uint32_t offs_T = 0;
 
     // scratch
-    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     unsigned char* pinned = nullptr;
+
+    // tuning
+    int dense_min = 2048;
 
     // profiling
     bool profile = false;
@@ -401,6 +404,8 @@ struct gbvdb_grid_s {
     void clear_bitmap(long long total_bits) {
         grow(bitmap, (size_t)(total_bits / 8) + 64);
         check(cudaMemsetAsync(bitmap.p, 0, (size_t)(total_bits / 8), stream), "bitmap clear");
+        grow(touched, (size_t)(total_bits / 8) + 64);
+        check(cudaMemsetAsync(touched.p, 0, (size_t)(total_bits / 8), stream), "touched clear");
         grow(misc, 256);
         check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
     }
@@ -445,8 +450,8 @@ struct gbvdb_grid_s {
             t = view();
             int rlo[3], rhi[3];
             for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
-            launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), nullptr,
-                            ptr<int>(misc) + 8, stream);
+            launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
+                            nullptr, ptr<int>(misc) + 8, stream);
             check_launch("keys_extra");
             if (allocate_from_bitmap(D, kd, bits) > 0) {
                 mark();
@@ -474,8 +479,8 @@ struct gbvdb_grid_s {
         TreeView t = view();
         int rlo[3], rhi[3];
         for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
-        launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(bitmap), ptr<int>(markers),
-                        ptr<int>(misc) + 8, stream);
+        launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
+                        ptr<int>(markers), ptr<int>(misc) + 8, stream);
         check_launch("keys_incr");
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
         long long nwords = bits / 32;
@@ -776,7 +781,7 @@ struct gbvdb_grid_s {
             launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
                                 interior, stream);
         } else {
-            gp.dense_min = 2048;
+            gp.dense_min = dense_min;
             build_offsets(gp.lo_off, gp.hi_off, T, sc_R);
             launch_gather(t, lgv, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
                           ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, interior, stream);
@@ -851,7 +856,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot};
     for (DevBuf* b : bufs) g->release(*b);
@@ -1207,6 +1212,17 @@ gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, voi
     if (interior) *interior = g->ch[chan].interior.p;
     if (apron) *apron = g->ch[chan].apron_buf.p;
     return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
+    GBVDB_GUARD(g)
+    if (param == GBVDB_TUNE_DENSE_MIN) {
+        if (value < 0 || value > (1ll << 31)) return GBVDB_INVALID_ARG;
+        g->dense_min = (int)value;
+        return GBVDB_OK;
+    }
+    return GBVDB_INVALID_ARG;
     GBVDB_END(g)
 }
 

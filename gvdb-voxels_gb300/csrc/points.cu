@@ -50,8 +50,13 @@ __global__ void k_linked_list(const Node* leaves, long long n, const uint32_t* s
     if (leaves[i].parent != kUndef64) linked[scmap[i]] = (int)i;
 }
 
+// the linked leaf at an index-space position.  A leaf is reachable from the root
+// only through a child-list entry, which the link pass writes after setting the
+// leaf's mParent, and delinking clears both; so every reachable leaf is linked and
+// the dense grid (built by traversal) answers directly.
 __device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeView& t, int x, int y, int z) {
-    long long l = lookup_leaf(lg, t, x, y, z);
+    if (lg.cells) return lookup_leaf(lg, t, x, y, z);
+    long long l = get_pos_leaf(t, x, y, z);
     if (l < 0 || t.nodes[0][l].parent == kUndef64) return -1;
     return l;
 }

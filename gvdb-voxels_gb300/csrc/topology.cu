@@ -13,6 +13,8 @@
 // i = ((x-lo)*ny + (y-lo))*nz + (z-lo), so ascending bit order equals the
 // reference's ascending u64 key order {lev, x, y, z} and a popcount prefix sum
 // gives each unique key its pool slot directly.
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace gbvdb {
@@ -89,10 +91,24 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
 }
 
 // gvdbCalcExtraBrickId (hi_mul = 2, PT.cuh:467-512) and gvdbCalcIncreExtraBrickId
-// (hi_mul = 1, PT.cuh:420-465): every node position in the point's box that is not
-// reachable from the root becomes a key; reachable leaves are marked (incremental).
-__global__ void k_keys_box(TreeView t, LeafGrid lg, PointSrc p, float3 orig, float radius, int hi_mul, int depth,
-                           int3 rlo, int3 rhi, KeyDomains dom, uint32_t* bm, int* markers, int* err) {
+// (hi_mul = 1, PT.cuh:420-465) in two steps.  The reference tests every node
+// position of every point's box against the tree.  Here (1) each point sets the
+// bits of the node positions its box covers in a per-level "touched" bitmap, and
+// (2) each touched position is resolved once: not reachable from the root -> a
+// key; a reachable leaf -> its marker.  Same sets, far fewer tree lookups.
+// Bits go to a per-block copy of the bitmap in shared memory when the whole
+// bitmap fits (kTouchSmemWords), then one atomicOr per non-zero word: a dense
+// region maps its many points onto a few words, which would otherwise be one hot
+// L2 line.  Larger (sparser) bitmaps are set in global memory directly.
+constexpr int kTouchSmemWords = 8192;
+__global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth, int3 rlo,
+                            int3 rhi, KeyDomains dom, uint32_t* touched, long long nwords, int* err) {
+    extern __shared__ uint32_t sbm[];
+    const bool use_smem = nwords <= kTouchSmemWords;
+    if (use_smem) {
+        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
+        __syncthreads();
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float x, y, z;
         load_pos(p.base, i, p.stride, p.off, x, y, z);
@@ -107,7 +123,8 @@ __global__ void k_keys_box(TreeView t, LeafGrid lg, PointSrc p, float3 orig, flo
             bmax[a] = (int)fadd(fi, hr);
         }
         for (int lev = 0; lev < depth; lev++) {
-            int rr = 1 << t.lgrange[lev];
+            int lg = t.lgrange[lev];
+            int rr = 1 << lg;
             int lo[3], hi[3];
 #pragma unroll
             for (int a = 0; a < 3; a++) {
@@ -119,18 +136,50 @@ __global__ void k_keys_box(TreeView t, LeafGrid lg, PointSrc p, float3 orig, flo
                     for (int nz = lo[2]; nz <= hi[2]; nz += rr) {
                         // guard: positions outside the root (the reference aliases them)
                         if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
-                        // getPosParent(pos, 0) is the leaf reachable at pos: the dense grid answers it
-                        long long pid = (lev == 0) ? lookup_leaf(lg, t, nx, ny, nz) : get_pos_parent(t, nx, ny, nz, lev);
-                        if (pid < 0) {
-                            long long b = key_bit(dom.d[lev], nx >> t.lgrange[lev], ny >> t.lgrange[lev], nz >> t.lgrange[lev]);
-                            if (b < 0) { atomicOr(err, 1); continue; }
-                            set_bit(bm, b);
-                        } else if (lev == 0 && markers) {
-                            if (__ldcg(markers + pid) == 0) markers[pid] = 1;
+                        long long b = key_bit(dom.d[lev], nx >> lg, ny >> lg, nz >> lg);
+                        if (b < 0) { atomicOr(err, 1); continue; }
+                        if (use_smem) {
+                            uint32_t bit = 1u << (b & 31);
+                            if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
+                        } else {
+                            set_bit(touched, b);
                         }
                     }
         }
     }
+    if (use_smem) {
+        __syncthreads();
+        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) {
+            uint32_t v = sbm[k];
+            if (v && (__ldcg(touched + k) & v) != v) atomicOr(touched + k, v);
+        }
+    }
+}
+
+// one thread per touched-bitmap word of level `lev`: getPosParent(pos, lev) for
+// every touched position; missing -> key bit, reachable leaf -> marker
+__global__ void k_resolve_touched(TreeView t, LeafGrid lg, int lev, KeyDomain d, const uint32_t* __restrict__ touched,
+                                  uint32_t* keys, int* markers) {
+    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long w0 = d.bitbase >> 5, nw = (d.nbits + 31) >> 5;
+    if (w >= nw) return;
+    uint32_t bits = touched[w0 + w];
+    uint32_t miss = 0;
+    const int lgr = t.lgrange[lev];
+    while (bits) {
+        int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        long long li = w * 32 + b;
+        int rz = (int)(li % d.dim[2]);
+        long long q = li / d.dim[2];
+        int ry = (int)(q % d.dim[1]);
+        int rx = (int)(q / d.dim[1]);
+        int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
+        long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
+        if (pid < 0) miss |= 1u << b;
+        else if (lev == 0 && markers) markers[pid] = 1;
+    }
+    if (miss) keys[w0 + w] = miss;  // each word has one owner thread
 }
 
 __global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32_t* __restrict__ cnt) {
@@ -316,12 +365,20 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
     k_keys_pass1<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, depth, dom, t, bitmap, err);
 }
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
-                     int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* bitmap, int* markers,
-                     int* err, cudaStream_t s) {
+                     int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
+                     uint32_t* bitmap, int* markers, int* err, cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
-    k_keys_box<<<grid_stride_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
-                                                             bitmap, markers, err);
+    long long nwords = 0;
+    for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
+    size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
+    // fewer, fuller blocks when each one flushes a shared bitmap
+    unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
+    k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
+    for (int lev = 0; lev < depth; lev++) {
+        long long nw = (dom.d[lev].nbits + 31) >> 5;
+        k_resolve_touched<<<blocks_for(nw, 128), 128, 0, s>>>(t, lg, lev, dom.d[lev], touched, bitmap, markers);
+    }
 }
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s) {

@@ -36,8 +36,9 @@ EXPORTS = [
     "gbvdb_get_node_counts", "gbvdb_get_point_bounds", "gbvdb_export_nodes", "gbvdb_export_childlist",
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
-    "gbvdb_get_stats", "gbvdb_checksum_noalloc",
+    "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning",
 ]
+TUNE_DENSE_MIN = 1
 
 
 class GbvdbError(RuntimeError):
@@ -96,6 +97,7 @@ def load(path=LIB_PATH):
     L.gbvdb_get_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
     L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
+    L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     _lib = L
     return L
 
@@ -285,6 +287,9 @@ class Grid:
         out = ctypes.c_double()
         self._check(self.L.gbvdb_checksum(self._h, chan, ctypes.byref(out)), "checksum")
         return out.value
+
+    def set_tuning(self, param, value):
+        self._check(self.L.gbvdb_set_tuning(self._h, int(param), int(value)), "set_tuning")
 
     def set_profile(self, on=True):
         self._check(self.L.gbvdb_set_profile(self._h, int(on)), "set_profile")

@@ -154,6 +154,10 @@ GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
 GBVDB_API gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out);
 /* device pointers of the atlas storage (interior bricks, apron records) for consumers */
 GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron);
+/* tuning parameters (no counterpart in the reference) */
+#define GBVDB_TUNE_DENSE_MIN 1   /* candidate points per brick above which gathers use the warp-per-subcell
+                                    form instead of the scatter form (default 2048) */
+GBVDB_API gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value);
 /* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
 GBVDB_API gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable);
 GBVDB_API gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap);

@@ -114,7 +114,8 @@ struct Harness {
     std::vector<int32_t> amap_cpu;
     // aux
     CUdeviceptr keys = 0, sorted = 0, marker = 0, presum = 0, cnt = 0, levcnt = 0, uniq = 0, range_res = 0;
-    size_t keys_cap = 0;
+    CUdeviceptr node_mk = 0;  // AUX_NODE_MARKER (separate from the unique pass's AUX_MARKER)
+    size_t keys_bytes = 0;
     CUdeviceptr sc_flag = 0, sc_map = 0, sc_cnt = 0, sc_off = 0, sc_pnts = 0, sc_pos = 0, sc_nid = 0;
     int sc_num = 0;
     int sc_len = 0;
@@ -366,14 +367,14 @@ struct Harness {
         }
     }
 
-    void keys_cap(size_t need) { realloc_dev(keys, keys_cap, need * 8); }
+    void keys_reserve(size_t need) { realloc_dev(keys, keys_bytes, need * 8); }
 
     void activate_bricks(float3 orig, int D, const int root[3]) {  // VG.cpp:1229-1413
         std::vector<int> rr(D);
         for (int l = 0; l < D; l++) rr[l] = range(l);
         aux(range_res, (size_t)D * 4);
         ck(cuMemcpyHtoD(range_res, rr.data(), (size_t)D * 4), "range_res");
-        keys_cap((size_t)npts * D);
+        keys_reserve((size_t)npts * D);
         int off = 0, stride = 12;
         void* a[8] = {&npts, &D, &range_res, &pts, &off, &stride, &orig, &keys};
         launch("gvdbCalcBrickId", npts / 512 + 1, 1, 1, 512, 1, 1, a);
@@ -401,10 +402,10 @@ struct Harness {
         std::vector<uint16_t> uni;
         if (incr) {
             if (nleaf == 0) return 0;
-            aux(marker, (size_t)nleaf * 4);
+            aux(node_mk, (size_t)nleaf * 4);
             std::vector<int> mk(nleaf, 0);
             if (accum) for (int i = 0; i < nleaf; i++) mk[i] = node(0, i)->flags;
-            ck(cuMemcpyHtoD(marker, mk.data(), (size_t)nleaf * 4), "markers");
+            ck(cuMemcpyHtoD(node_mk, mk.data(), (size_t)nleaf * 4), "markers");
         }
         // worst case keys per point: every node position of the box at every level
         size_t per = 0;
@@ -412,13 +413,13 @@ struct Harness {
             size_t w = (size_t)std::floor((incr ? 2.0 : 3.0) * radius + 2) / (size_t)range(l) + 2;
             per += w * w * w;
         }
-        keys_cap((size_t)npts * per + 64);
+        keys_reserve((size_t)npts * per + 64);
         CUdeviceptr excnt;
         ck(cuMemAlloc(&excnt, 64), "excnt");
         ck(cuMemsetD8(excnt, 0, 64), "excnt");
         prepare(true);
         int off = 0, stride = 12;
-        CUdeviceptr mk_dev = marker;
+        CUdeviceptr mk_dev = node_mk;
         if (incr) {
             void* a[12] = {&cuinfo, &radius, &npts, &D, &range_res, &pts, &off, &stride, &orig, &keys, &excnt, &mk_dev};
             launch("gvdbCalcIncreExtraBrickId", npts / 512 + 1, 1, 1, 512, 1, 1, a);
@@ -433,7 +434,7 @@ struct Harness {
         sort_unique(ex, D, uni, lc);
         if (incr) {
             std::vector<int> mk(nleaf);
-            ck(cuMemcpyDtoH(mk.data(), marker, (size_t)nleaf * 4), "markers");
+            ck(cuMemcpyDtoH(mk.data(), node_mk, (size_t)nleaf * 4), "markers");
             for (int i = 0; i < nleaf; i++) node(0, i)->flags = (uint8_t)mk[i];
         }
         alloc_nodes(uni, lc, D);
