@@ -317,9 +317,9 @@ struct gbvdb_grid_s {
         return kd;
     }
 
-    // dedup keys of one pass (bitmap already filled) and append the new nodes to the pools
-    // in ascending key order; returns the number of new nodes
-    long long allocate_from_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
+    // per-level unique-key counts of one pass (bitmap already filled): prefix of the
+    // popcounts at each level's first word, and the total; one readback
+    std::vector<uint32_t> count_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
         long long nwords = total_bits / 32;
         grow(pcnt, (size_t)(nwords + 1) * 4);
         grow(pscan, (size_t)(nwords + 1) * 4);
@@ -328,7 +328,6 @@ struct gbvdb_grid_s {
         check_launch("popc");
         scan_exclusive_u32(ptr<uint32_t>(pcnt), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
         check_launch("scan");
-        // per-level totals: prefix at each level's first word, and the grand total
         std::vector<uint32_t> at(depth + 1);
         for (int l = 0; l <= depth; l++) {
             long long w = l < depth ? kd.d[l].bitbase / 32 : nwords;
@@ -336,10 +335,18 @@ struct gbvdb_grid_s {
         }
         int errflag = 0;
         check(cudaMemcpyAsync(pinned + 4 * (depth + 1), ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        n_readback++;
         sync();
         memcpy(at.data(), pinned, 4 * (depth + 1));
         memcpy(&errflag, pinned + 4 * (depth + 1), 4);
+        if (errflag & 2)
+            throw StatusError{GBVDB_INVALID_ARG, "a point's activation box spans more than 2^26 nodes of one level"};
         if (errflag) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
+        return at;
+    }
+
+    // append the nodes of the counted pass to the pools in ascending key order
+    long long allocate_counted(int depth, const KeyDomains& kd, const std::vector<uint32_t>& at) {
         long long added = 0;
         if (at[1] > at[0]) {  // leaves of this pass lie in the level-0 key domain
             for (int a = 0; a < 3; a++) {
@@ -368,6 +375,10 @@ struct gbvdb_grid_s {
             added += cnt;
         }
         return added;
+    }
+
+    long long allocate_from_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
+        return allocate_counted(depth, kd, count_bitmap(depth, kd, total_bits));
     }
 
     // rebuild the dense leaf lookup after a topology change (exact: built by traversal)
@@ -483,20 +494,12 @@ struct gbvdb_grid_s {
                         ptr<int>(markers), ptr<int>(misc) + 8, stream);
         check_launch("keys_incr");
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
-        long long nwords = bits / 32;
-        grow(pcnt, (size_t)(nwords + 1) * 4);
-        grow(pscan, (size_t)(nwords + 1) * 4);
-        grow(scan_tmp, scan_tmp_bytes(nwords));
-        launch_popc(ptr<uint32_t>(bitmap), nwords, ptr<uint32_t>(pcnt), stream);
-        scan_exclusive_u32(ptr<uint32_t>(pcnt), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
-        check_launch("incr scan");
-        uint32_t total = 0;
-        readback(&total, ptr<uint32_t>(pscan) + nwords, 4);
+        std::vector<uint32_t> at = count_bitmap(D, kd, bits);
         mark();
-        if (total == 0) return;
+        if (at[(size_t)D] == 0) return;
         launch_apply_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), stream);
         check_launch("apply_markers");
-        allocate_from_bitmap(D, kd, bits);
+        allocate_counted(D, kd, at);
         link_all(D);
         t = view();
         launch_delink_leaf(t, ncnt[0], stream);
@@ -612,10 +615,8 @@ struct gbvdb_grid_s {
         launch_node_flags(ptr<Node>(nodes[0]), nleaf, 1, ptr<uint32_t>(flags), stream);
         scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(scmap), nleaf, scan_tmp.p, stream);
         check_launch("scmap");
-        uint32_t nb = 0;
-        readback(&nb, ptr<uint32_t>(scmap) + nleaf, 4);
-        sc_nbricks = nb;
-        grow(linked, (size_t)(nb + 1) * 4);
+        // the linked count scmap[nleaf] is read back with the binning totals
+        grow(linked, (size_t)(nleaf + 1) * 4);
         launch_linked_list(ptr<Node>(nodes[0]), nleaf, ptr<uint32_t>(scmap), ptr<int>(linked), stream);
         check_launch("linked");
     }
@@ -630,7 +631,7 @@ struct gbvdb_grid_s {
         stage_begin();
         build_linked();
         mark();
-        long long nbins = sc_nbricks * 64;
+        long long nbins = ncnt[0] * 64;  // upper bound: bins of unlinked leaves stay empty
         grow(bin_cnt, (size_t)(nbins + 1) * 4);
         grow(bin_off, (size_t)(nbins + 1) * 4);
         check(cudaMemsetAsync(bin_cnt.p, 0, (size_t)(nbins + 1) * 4, stream), "bin clear");
@@ -649,12 +650,16 @@ struct gbvdb_grid_s {
         scan_exclusive_u32(ptr<uint32_t>(bin_cnt), ptr<uint32_t>(bin_off), nbins, scan_tmp.p, stream);
         check_launch("bin scan");
         unsigned long long tot[2];
-        uint32_t binned = 0;
+        uint32_t binned = 0, nb = 0;
         check(cudaMemcpyAsync(pinned, totals, 16, cudaMemcpyDeviceToHost, stream), "rb");
         check(cudaMemcpyAsync(pinned + 16, ptr<uint32_t>(bin_off) + nbins, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        check(cudaMemcpyAsync(pinned + 20, ptr<uint32_t>(scmap) + ncnt[0], 4, cudaMemcpyDeviceToHost, stream), "rb");
+        n_readback++;
         sync();
         memcpy(tot, pinned, 16);
         memcpy(&binned, pinned + 16, 4);
+        memcpy(&nb, pinned + 20, 4);
+        sc_nbricks = nb;
         mark();
         grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
         launch_bin_scatter(p, trans, R, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),

@@ -74,8 +74,16 @@ __device__ __forceinline__ long long key_bit(const KeyDomain& d, int x, int y, i
 }
 
 // gvdbCalcBrickId (PT.cuh:352-382): key of every level below the root for every
-// point whose coordinates are all >= 0
-__global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom, TreeView tv, uint32_t* bm, int* err) {
+// point whose coordinates are all >= 0 (bits collected per block in shared memory
+// when the bitmap fits, as for the box keys below)
+__global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom, TreeView tv, uint32_t* bm,
+                             long long nwords, int* err) {
+    extern __shared__ uint32_t sbm[];
+    const bool use_smem = nwords <= 8192;
+    if (use_smem) {
+        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
+        __syncthreads();
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float x, y, z;
         load_pos(p.base, i, p.stride, p.off, x, y, z);
@@ -85,7 +93,19 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
             int lg = tv.lgrange[lev];
             long long b = key_bit(dom.d[lev], cover_coord(w0, lg), cover_coord(w1, lg), cover_coord(w2, lg));
             if (b < 0) { atomicOr(err, 1); continue; }
-            set_bit(bm, b);
+            if (use_smem) {
+                uint32_t bit = 1u << (b & 31);
+                if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
+            } else {
+                set_bit(bm, b);
+            }
+        }
+    }
+    if (use_smem) {
+        __syncthreads();
+        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) {
+            uint32_t v = sbm[k];
+            if (v && (__ldcg(bm + k) & v) != v) atomicOr(bm + k, v);
         }
     }
 }
@@ -101,6 +121,20 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
 // region maps its many points onto a few words, which would otherwise be one hot
 // L2 line.  Larger (sparser) bitmaps are set in global memory directly.
 constexpr int kTouchSmemWords = 8192;
+
+__device__ __forceinline__ void touch_bit(uint32_t* sbm, bool use_smem, uint32_t* touched, long long b) {
+    if (use_smem) {
+        uint32_t bit = 1u << (b & 31);
+        if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
+    } else {
+        set_bit(touched, b);
+    }
+}
+
+// Work is flattened across the warp: each lane computes its point's per-axis
+// ranges of node positions at a level, a warp prefix sum over the lanes' counts
+// lays all (point, position) items out in one list, and the lanes then take
+// consecutive items, so that boxes of 1 to 8 positions do not leave lanes idle.
 __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth, int3 rlo,
                             int3 rhi, KeyDomains dom, uint32_t* touched, long long nwords, int* err) {
     extern __shared__ uint32_t sbm[];
@@ -109,42 +143,79 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
         for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
         __syncthreads();
     }
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
-        float x, y, z;
-        load_pos(p.base, i, p.stride, p.off, x, y, z);
-        float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
-        if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
-        int bmin[3], bmax[3];
-        float hr = hi_mul == 2 ? __fmul_rn(2.0f, radius) : radius;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            float fi = (float)(int)w[a];
-            bmin[a] = (int)fsub(fi, radius);
-            bmax[a] = (int)fadd(fi, hr);
-        }
-        for (int lev = 0; lev < depth; lev++) {
-            int lg = t.lgrange[lev];
-            int rr = 1 << lg;
-            int lo[3], hi[3];
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long gwarp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const float hr = hi_mul == 2 ? __fmul_rn(2.0f, radius) : radius;
+    for (long long base = gwarp * 32; base < p.n; base += nwarps * 32) {
+        const long long i = base + lane;
+        bool valid = i < p.n;
+        int bmin[3] = {0, 0, 0}, bmax[3] = {-1, -1, -1};
+        if (valid) {
+            float x, y, z;
+            load_pos(p.base, i, p.stride, p.off, x, y, z);
+            float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
+            valid = !(w[0] < 0 || w[1] < 0 || w[2] < 0);
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                lo[a] = bmin[a] / rr * rr;
-                hi[a] = bmax[a] / rr * rr;
+                float fi = (float)(int)w[a];
+                bmin[a] = (int)fsub(fi, radius);
+                bmax[a] = (int)fadd(fi, hr);
             }
-            for (int nx = lo[0]; nx <= hi[0]; nx += rr)
-                for (int ny = lo[1]; ny <= hi[1]; ny += rr)
-                    for (int nz = lo[2]; nz <= hi[2]; nz += rr) {
-                        // guard: positions outside the root (the reference aliases them)
-                        if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
-                        long long b = key_bit(dom.d[lev], nx >> lg, ny >> lg, nz >> lg);
-                        if (b < 0) { atomicOr(err, 1); continue; }
-                        if (use_smem) {
-                            uint32_t bit = 1u << (b & 31);
-                            if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
-                        } else {
-                            set_bit(touched, b);
-                        }
-                    }
+        }
+        for (int lev = 0; lev < depth; lev++) {
+            const int lg = t.lgrange[lev];
+            const int rr = 1 << lg;
+            int lo[3], cnt[3];
+            const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                lo[a] = bmin[a] / rr * rr;  // C truncation, as the reference
+                int hi = bmax[a] / rr * rr;
+                // positions outside the root are skipped: clip the range to it
+                if (lo[a] < rl[a]) lo[a] += (rl[a] - lo[a] + rr - 1) / rr * rr;
+                if (hi > rh[a]) hi -= (hi - rh[a] + rr - 1) / rr * rr;
+                cnt[a] = valid && hi >= lo[a] ? (hi - lo[a]) / rr + 1 : 0;
+            }
+            long long mine64 = (long long)cnt[0] * cnt[1] * cnt[2];
+            if (mine64 > (1ll << 26)) {  // keeps the warp's item count within int
+                atomicOr(err, 2);
+                mine64 = 0;
+            }
+            const int mine = (int)mine64;
+            int incl = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            for (int k0 = 0; k0 < total; k0 += 32) {
+                const int k = k0 + lane;
+                // owner lane: the first lane whose inclusive prefix exceeds k
+                int owner = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    int cand = owner + step - 1;
+                    int pv = __shfl_sync(0xFFFFFFFFu, incl, cand);
+                    if (pv <= k) owner += step;
+                }
+                const int excl = __shfl_sync(0xFFFFFFFFu, incl - mine, owner);
+                const int ocx = __shfl_sync(0xFFFFFFFFu, cnt[0], owner);
+                const int ocy = __shfl_sync(0xFFFFFFFFu, cnt[1], owner);
+                const int olx = __shfl_sync(0xFFFFFFFFu, lo[0], owner);
+                const int oly = __shfl_sync(0xFFFFFFFFu, lo[1], owner);
+                const int olz = __shfl_sync(0xFFFFFFFFu, lo[2], owner);
+                if (k >= total) continue;
+                const int li = k - excl;
+                const int ix = li % ocx, iy = (li / ocx) % ocy, iz = li / (ocx * ocy);
+                const int nx = olx + ix * rr, ny = oly + iy * rr, nz = olz + iz * rr;
+                // guard: positions outside the root (the reference aliases them)
+                if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
+                long long b = key_bit(dom.d[lev], nx >> lg, ny >> lg, nz >> lg);
+                if (b < 0) { atomicOr(err, 1); continue; }
+                touch_bit(sbm, use_smem, touched, b);
+            }
         }
     }
     if (use_smem) {
@@ -362,7 +433,11 @@ void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s) {
 }
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
                        uint32_t* bitmap, int* err, cudaStream_t s) {
-    k_keys_pass1<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, depth, dom, t, bitmap, err);
+    long long nwords = 0;
+    for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
+    size_t smem = nwords <= 8192 ? (size_t)nwords * 4 : 0;
+    unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
+    k_keys_pass1<<<blocks, 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, err);
 }
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
