@@ -116,9 +116,11 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
 }
 
 // Binned record of one point: position (after +trans) and, in .w, its subcell
-// membership range relative to its home subcell H = floor(w/4): six signed
-// nibbles lo_x, hi_x, lo_y, hi_y, lo_z, hi_z with lo = int(w-R)/4 - H and
-// hi = int(w+1+R)/4 - H (fits for R <= 11, the range the brick-tiled gather serves).
+// membership relative to its home subcell H = floor(w/4) as three 9-bit masks
+// (axis a at bit 9a): bit d+4 is set iff subcell H+d is a member on that axis,
+// i.e. lo <= d <= hi with lo = int(w-R)/4 - H and hi = int(w+1+R)/4 - H.  For
+// R <= 11 (the range the brick-tiled gather serves) lo >= -4 and hi <= 3, so the
+// masks are exact; outside that range they are clipped and not used.
 __device__ __forceinline__ int pack_ranges(const float* w, float R) {
     int packed = 0;
 #pragma unroll
@@ -126,13 +128,21 @@ __device__ __forceinline__ int pack_ranges(const float* w, float R) {
         int lo, hi;
         sc_range(w[a], R, lo, hi);
         int h = ((int)w[a]) >> 2;
-        int l = (lo >> 2) - h, u = (hi >> 2) - h;  // lo, hi are multiples of 4 (lo may be negative)
-        packed |= ((l & 15) << (8 * a)) | ((u & 15) << (8 * a + 4));
+        int l = max((lo >> 2) - h, -4), u = min((hi >> 2) - h, 4);  // lo, hi are multiples of 4
+        if (l <= u) packed |= (int)((((1u << (u - l + 1)) - 1u) << (l + 4)) << (9 * a));
     }
     return packed;
 }
-__device__ __forceinline__ int nib(int packed, int k) {  // signed nibble k (0..5 in lo_x,hi_x,lo_y,...)
-    return (packed << (28 - 4 * k)) >> 28;
+// member range [l, u] on axis a (relative to the home subcell); false when empty
+__device__ __forceinline__ bool mask_range(int packed, int a, int& l, int& u) {
+    const unsigned f = ((unsigned)packed >> (9 * a)) & 0x1FFu;
+    l = __ffs(f) - 5;
+    u = 27 - __clz(f);
+    return f != 0;
+}
+// bits an offset o = H - S must find set for S to be a member (d = S - H = -o)
+__device__ __forceinline__ int member_bits(int ox, int oy, int oz) {
+    return (1 << (4 - ox)) | (1 << (13 - oy)) | (1 << (22 - oz));
 }
 
 __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, const int* __restrict__ bin_of,
@@ -203,6 +213,36 @@ __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out)
 
 constexpr int kGatherThreads = 256;
 constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 11 -> offsets within +-1 brick)
+constexpr int kQueue = 64;      // per-warp point queue of the gather form (SoA x, y, z)
+static_assert((kGatherThreads / 32) * 3 * kQueue * 4 <= kMaxBins * 12, "queues fit in the bin scratch");
+
+// packed FP32 pairs (f32x2 arithmetic, round-to-nearest, no contraction)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2pack(float lo, float hi) {
+    return (f32x2)__float_as_uint(lo) | ((f32x2)__float_as_uint(hi) << 32);
+}
+__device__ __forceinline__ float f2lo(f32x2 v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2hi(f32x2 v) { return __uint_as_float((unsigned)(v >> 32)); }
+__device__ __forceinline__ f32x2 f2sub(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
 
 // One block per linked leaf.  Setup: the 3x3x3 neighbour ranks and the
 // non-empty home bins that can hold members of this brick's subcells.  Then
@@ -222,7 +262,7 @@ constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 11 -> 
 //
 // One coalesced write of the brick from the tile at the end.
 template <typename T>
-__global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
+__global__ void __launch_bounds__(kGatherThreads, 5) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
                                                            const uint32_t* __restrict__ scmap,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
@@ -230,9 +270,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid 
                                                            GatherParams gp, T* __restrict__ interior) {
     __shared__ uint32_t tile[4096];
     __shared__ int nrank[27];
-    __shared__ uint32_t cb_beg[kMaxBins];
-    __shared__ uint32_t cb_cnt[kMaxBins];
-    __shared__ int cb_home[kMaxBins];
+    // candidate bins (both forms count them; the scatter form walks them), reused
+    // by the gather form as per-warp point queues once the form is chosen
+    __shared__ __align__(16) unsigned char scratch[kMaxBins * 12];
+    uint32_t* cb_beg = reinterpret_cast<uint32_t*>(scratch);
+    uint32_t* cb_cnt = cb_beg + kMaxBins;
+    int* cb_home = reinterpret_cast<int*>(cb_cnt + kMaxBins);
     __shared__ int ncb;
     __shared__ int cursor;
     __shared__ unsigned int ncand;
@@ -313,10 +356,12 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid 
                 if (lane < nv) {
                     q = pts[beg + base + lane];
                     const int pk = __float_as_int(q.w);
-                    int l0x = max(0, dhx + nib(pk, 0)), l1x = min(3, dhx + nib(pk, 1));
-                    int l0y = max(0, dhy + nib(pk, 2)), l1y = min(3, dhy + nib(pk, 3));
-                    int l0z = max(0, dhz + nib(pk, 4)), l1z = min(3, dhz + nib(pk, 5));
-                    if (l0x <= l1x && l0y <= l1y && l0z <= l1z)
+                    int rx0, rx1, ry0, ry1, rz0, rz1;
+                    const bool ne = mask_range(pk, 0, rx0, rx1) & mask_range(pk, 1, ry0, ry1) & mask_range(pk, 2, rz0, rz1);
+                    int l0x = max(0, dhx + rx0), l1x = min(3, dhx + rx1);
+                    int l0y = max(0, dhy + ry0), l1y = min(3, dhy + ry1);
+                    int l0z = max(0, dhz + rz0), l1z = min(3, dhz + rz1);
+                    if (ne && l0x <= l1x && l0y <= l1y && l0z <= l1z)
                         box = l0x | (l1x << 2) | (l0y << 4) | (l1y << 6) | (l0z << 8) | (l1z << 10);
                 }
                 unsigned live = __ballot_sync(0xFFFFFFFFu, (box & (1 << 12)) == 0);
@@ -351,17 +396,57 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid 
         }
     } else {
         // ------------------------------------------------------- gather form
+        // Lane layout: half hf = lane >> 4 takes every other pair of queued points,
+        // column (cx, cy) = lane & 15 holds the 4 voxels z = 0..3 of that column, so
+        // one pass over the queue evaluates 4 points per warp step.  The two halves
+        // keep partial minima of the same voxels and merge them after every bin.
+        float* qx = reinterpret_cast<float*>(scratch) + warp * (3 * kQueue);
+        float* qy = qx + kQueue;
+        float* qz = qy + kQueue;
         const int nw = blockDim.x >> 5;
+        const int hf = lane >> 4, cx = lane & 3, cy = (lane >> 2) & 3;
+        const unsigned lt = (1u << lane) - 1u;
         for (int sc = warp; sc < 64; sc += nw) {
             const int lx = sc & 3, ly = (sc >> 2) & 3, lz = sc >> 4;
             const int Sx = sx0 + lx, Sy = sy0 + ly, Sz = sz0 + lz;
-            const float fx = (float)(ox + 4 * lx + vx), fy = (float)(oy + 4 * ly + vy);
-            const float fz0 = (float)(oz + 4 * lz + vz), fz1 = fz0 + 2.0f;
+            const float fx = (float)(ox + 4 * lx + cx), fy = (float)(oy + 4 * ly + cy);
+            const float fz = (float)(oz + 4 * lz);
+            const f32x2 fxx = f2pack(fx, fx), fyy = f2pack(fy, fy);
+            const f32x2 z0 = f2pack(fz, fz), z1 = f2pack(fz + 1.0f, fz + 1.0f);
+            const f32x2 z2 = f2pack(fz + 2.0f, fz + 2.0f), z3 = f2pack(fz + 3.0f, fz + 3.0f);
             const float blx = (float)(4 * Sx), bhx = blx + 3.0f;
             const float bly = (float)(4 * Sy), bhy = bly + 3.0f;
             const float blz = (float)(4 * Sz), bhz = blz + 3.0f;
-            float m0 = Tf, m1 = Tf;
+            float m0 = Tf, m1 = Tf, m2 = Tf, m3 = Tf;
             float wmax = Tf;
+            int nq = 0;
+            // evaluate the queued points [0, nq) against the column's 4 voxels
+            auto drain = [&]() {
+                const int n4 = (nq + 3) & ~3;
+                if (lane < n4 - nq) {  // pad with points at infinity (d^2 = inf)
+                    qx[nq + lane] = __int_as_float(0x7F800000);
+                    qy[nq + lane] = __int_as_float(0x7F800000);
+                    qz[nq + lane] = __int_as_float(0x7F800000);
+                }
+                __syncwarp();
+                for (int i = 2 * hf; i < n4; i += 4) {
+                    const f32x2 px = *reinterpret_cast<const f32x2*>(qx + i);
+                    const f32x2 py = *reinterpret_cast<const f32x2*>(qy + i);
+                    const f32x2 pz = *reinterpret_cast<const f32x2*>(qz + i);
+                    const f32x2 dx = f2sub(px, fxx), dy = f2sub(py, fyy);
+                    const f32x2 dxy = f2fma(dy, dy, f2mul(dx, dx));
+                    f32x2 dz = f2sub(pz, z0), r = f2fma(dz, dz, dxy);
+                    m0 = fmin3(m0, f2lo(r), f2hi(r));
+                    dz = f2sub(pz, z1); r = f2fma(dz, dz, dxy);
+                    m1 = fmin3(m1, f2lo(r), f2hi(r));
+                    dz = f2sub(pz, z2); r = f2fma(dz, dz, dxy);
+                    m2 = fmin3(m2, f2lo(r), f2hi(r));
+                    dz = f2sub(pz, z3); r = f2fma(dz, dz, dxy);
+                    m3 = fmin3(m3, f2lo(r), f2hi(r));
+                }
+                __syncwarp();
+                nq = 0;
+            };
             for (int e = 0; e < noffs; e++) {
                 const int4 o = offs[e];
                 if ((float)o.w >= wmax) break;
@@ -372,17 +457,15 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid 
                 if (r < 0) continue;
                 const unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
                 const uint32_t beg = __ldg(bin_off + bin), end = __ldg(bin_off + bin + 1);
+                if (beg == end) continue;
+                const int need = member_bits(o.x, o.y, o.z);
                 for (uint32_t base = beg; base < end; base += 32) {
                     const uint32_t j = base + lane;
                     bool ok = false;
                     float4 q = make_float4(0, 0, 0, 0);
                     if (j < end) {
                         q = pts[j];
-                        const int pk = __float_as_int(q.w);
-                        // membership of S: lo <= S - H <= hi on every axis
-                        ok = nib(pk, 0) <= -o.x && -o.x <= nib(pk, 1) && nib(pk, 2) <= -o.y && -o.y <= nib(pk, 3) &&
-                             nib(pk, 4) <= -o.z && -o.z <= nib(pk, 5);
-                        if (ok) {
+                        if ((__float_as_int(q.w) & need) == need) {
                             const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q.x), fsub(q.x, bhx)));
                             const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q.y), fsub(q.y, bhy)));
                             const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q.z), fsub(q.z, bhz)));
@@ -390,25 +473,31 @@ __global__ void __launch_bounds__(kGatherThreads) k_gather(TreeView t, LeafGrid 
                             ok = lb < wmax;
                         }
                     }
-                    unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
-                    while (live) {
-                        const int k = __ffs(live) - 1;
-                        live &= live - 1;
-                        const float px = __shfl_sync(0xFFFFFFFFu, q.x, k);
-                        const float py = __shfl_sync(0xFFFFFFFFu, q.y, k);
-                        const float pz = __shfl_sync(0xFFFFFFFFu, q.z, k);
-                        const float dx = fsub(px, fx), dy = fsub(py, fy);
-                        const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                        const float dz0 = fsub(pz, fz0), dz1 = fsub(pz, fz1);
-                        m0 = fminf(m0, __fmaf_rn(dz0, dz0, dxy));
-                        m1 = fminf(m1, __fmaf_rn(dz1, dz1, dxy));
+                    const unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
+                    if (ok) {
+                        const int k = nq + __popc(live & lt);
+                        qx[k] = q.x;
+                        qy[k] = q.y;
+                        qz[k] = q.z;
                     }
+                    nq += __popc(live);
+                    if (nq >= 32) drain();
                 }
-                wmax = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(m0, m1))));
+                if (nq) drain();
+                // merge the halves' minima; wmax = the largest voxel minimum
+                m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
+                m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
+                m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
+                m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
+                wmax = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3)))));
             }
-            const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
-            tile[v0] = __float_as_uint(m0);
-            tile[v0 + 512] = __float_as_uint(m1);
+            if (hf == 0) {
+                const int v = ((4 * lz) << 8) | ((4 * ly + cy) << 4) | (4 * lx + cx);
+                tile[v] = __float_as_uint(m0);
+                tile[v + 256] = __float_as_uint(m1);
+                tile[v + 512] = __float_as_uint(m2);
+                tile[v + 768] = __float_as_uint(m3);
+            }
         }
     }
     __syncthreads();
