@@ -776,6 +776,7 @@ struct gbvdb_grid_s {
             }
         }
         gp.tbits = bits_of(T);
+        gp.rcut = std::isfinite(T) ? (float)(std::sqrt((double)T) + 0.01) : INFINITY;
         gp.lo_off = (int)std::floor((-1.0 - sc_R) / 4.0) - 1;
         gp.hi_off = (int)std::ceil((4.0 + sc_R) / 4.0);
         int span = 4 + gp.hi_off - gp.lo_off;

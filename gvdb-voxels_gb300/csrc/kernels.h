@@ -92,6 +92,7 @@ struct GatherParams {
     int ax, ay;        // atlas axis counts
     int lo_off, hi_off;  // home-bin offset range H - S (subcell units)
     int dense_min;     // bricks with more candidate points use the gather form
+    float rcut;        // per-axis distance at or beyond which d^2 >= cutoff (conservative)
 };
 // offs: candidate home-bin offsets {dx, dy, dz, lb2} (H - S, subcell units), ascending lb2
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,

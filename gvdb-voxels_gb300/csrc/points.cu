@@ -175,27 +175,32 @@ __device__ __forceinline__ __half cvt_out<__half>(float v) { return __float2half
 template <>
 __device__ __forceinline__ __nv_bfloat16 cvt_out<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
-// final voxel value from min squared distance m
-__device__ __forceinline__ float finish(const GatherParams& gp, float m, float old) {
-    float c = __fsqrt_rn(m);
-    if (gp.mode == 0) {
-        float base = gp.accum ? old : 0.0f;
-        return fmaxf(base, fsub(gp.rho, c));
-    }
-    float base = gp.accum ? old : 3.0f;
-    return fminf(base, fsub(c, gp.rho));
+// final voxel value from min squared distance m, with c = sqrt(m) given
+__device__ __forceinline__ float finish_c(const GatherParams& gp, float c, float old) {
+    if (gp.mode == 0) return fmaxf(gp.accum ? old : 0.0f, fsub(gp.rho, c));
+    return fminf(gp.accum ? old : 3.0f, fsub(c, gp.rho));
 }
 
-// write the brick's 4096 voxel values from the min-d^2 tile (coalesced, 4 voxels per access)
 template <typename T>
 __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out) {
+    // voxels no point reached hold the cutoff: their sqrt is one per thread
+    const float sqrtT = __fsqrt_rn(__uint_as_float(gp.tbits));
     for (int v4 = threadIdx.x; v4 < 1024; v4 += blockDim.x) {
         float r[4];
+        const uint4 m4 = reinterpret_cast<const uint4*>(tile)[v4];
+        const uint32_t mv[4] = {m4.x, m4.y, m4.z, m4.w};
+        const bool any = (m4.x != gp.tbits) | (m4.y != gp.tbits) | (m4.z != gp.tbits) | (m4.w != gp.tbits);
+        float c[4] = {sqrtT, sqrtT, sqrtT, sqrtT};
+        if (__any_sync(__activemask(), any)) {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (mv[k] != gp.tbits) c[k] = __fsqrt_rn(__uint_as_float(mv[k]));
+        }
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             int v = v4 * 4 + k;
             float old = gp.accum ? ld_f32<T>(out + v) : 0.f;
-            r[k] = finish(gp, __uint_as_float(tile[v]), old);
+            r[k] = finish_c(gp, c[k], old);
         }
         if constexpr (sizeof(T) == 4) {
             reinterpret_cast<float4*>(out)[v4] = make_float4(r[0], r[1], r[2], r[3]);
@@ -211,10 +216,12 @@ __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out)
     }
 }
 
-constexpr int kGatherThreads = 256;
-constexpr int kMaxBins = 1728;  // 12^3 candidate home bins at most (R <= 11 -> offsets within +-1 brick)
-constexpr int kQueue = 64;      // per-warp point queue of the gather form (SoA x, y, z)
-static_assert((kGatherThreads / 32) * 3 * kQueue * 4 <= kMaxBins * 12, "queues fit in the bin scratch");
+constexpr int kGatherThreads = 128;
+constexpr int kQueue = 64;  // per-warp point queue of the gather form (SoA x, y, z)
+constexpr int kLive = 256;  // live points per batch of the scatter form
+constexpr int kScratch = kLive * 16 > (kGatherThreads / 32) * 3 * kQueue * 4 ? kLive * 16
+                                                                              : (kGatherThreads / 32) * 3 * kQueue * 4;
+static_assert(kGatherThreads == 128, "the scatter form gives each of the 4 warps 4 tile rows");
 
 // packed FP32 pairs (f32x2 arithmetic, round-to-nearest, no contraction)
 typedef unsigned long long f32x2;
@@ -244,41 +251,38 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     return r;
 }
 
-// One block per linked leaf.  Setup: the 3x3x3 neighbour ranks and the
-// non-empty home bins that can hold members of this brick's subcells.  Then
-// one of two forms, chosen per brick by its candidate point count:
+// One block per linked leaf.  Setup: the ranks of the 3x3x3 neighbour bricks and
+// their point ranges in the home-binned array (a brick's 64 bins are contiguous).
+// Then one of two forms, chosen per brick by the number of points homed in the
+// neighbourhood (either form is exact; the choice only affects speed):
 //
-// scatter (sparse bricks): warps take bins, lanes take 32 points of a bin; for
-//   each point the warp visits the point's member subcells of this brick, 2
-//   voxels per lane per subcell, and reduces min d^2 into the shared tile with
-//   shared atomics (skipped when d^2 >= the static cutoff T).
-// gather (dense bricks): each warp owns whole subcells in turn (2 voxels per
-//   lane, min d^2 in registers).  It visits candidate home bins in ascending
-//   order of their lower-bound distance lb^2 to the subcell (host table) and
-//   stops at the first bin with lb^2 >= wmax, the largest current minimum of
-//   its 64 voxels; a point is evaluated only if it is a member and its own
-//   lower bound to the subcell's voxel box is below wmax.  Skipped points
-//   cannot lower any voxel's minimum, so the result is exact.
+// scatter (sparse bricks): every thread loads one neighbourhood point at a time
+//   (all loads in flight together) and derives its member subcells in this
+//   brick; each warp then walks its live points: for each member subcell, 2
+//   voxels per lane, min d^2 reduced into the shared tile with shared atomics
+//   (skipped when d^2 >= the static cutoff T).
+// gather (dense bricks): each warp owns whole subcells in turn.  It visits
+//   candidate home bins in ascending order of their lower-bound distance lb^2 to
+//   the subcell (host table) and stops at the first bin with lb^2 >= wmax, the
+//   largest current minimum of its 64 voxels; a point is queued only if it is a
+//   member and its own lower bound to the subcell's voxel box is below wmax.
+//   Skipped points cannot lower any voxel's minimum, so the result is exact.
 //
 // One coalesced write of the brick from the tile at the end.
 template <typename T>
-__global__ void __launch_bounds__(kGatherThreads, 5) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
+__global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
                                                            const uint32_t* __restrict__ scmap,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
                                                            const int4* __restrict__ offs, int noffs,
                                                            GatherParams gp, T* __restrict__ interior) {
-    __shared__ uint32_t tile[4096];
+    __shared__ __align__(16) uint32_t tile[4096];
     __shared__ int nrank[27];
-    // candidate bins (both forms count them; the scatter form walks them), reused
-    // by the gather form as per-warp point queues once the form is chosen
-    __shared__ __align__(16) unsigned char scratch[kMaxBins * 12];
-    uint32_t* cb_beg = reinterpret_cast<uint32_t*>(scratch);
-    uint32_t* cb_cnt = cb_beg + kMaxBins;
-    int* cb_home = reinterpret_cast<int*>(cb_cnt + kMaxBins);
-    __shared__ int ncb;
-    __shared__ int cursor;
-    __shared__ unsigned int ncand;
+    __shared__ uint32_t nb_beg[27];
+    __shared__ uint32_t nb_pre[28];  // exclusive prefix of the neighbours' point counts
+    // scatter form: the live-point list; gather form: per-warp point queues
+    __shared__ __align__(16) unsigned char scratch[kScratch];
+    __shared__ int nlive;
 
     const int leaf = linked[blockIdx.x];
     const Node nd = t.nodes[0][leaf];
@@ -286,113 +290,113 @@ __global__ void __launch_bounds__(kGatherThreads, 5) k_gather(TreeView t, LeafGr
     if (slot < 0) return;
     const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
     const int sx0 = ox >> 2, sy0 = oy >> 2, sz0 = oz >> 2;
-
-    if (threadIdx.x < 27) {
-        int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
-        int r = -1;
-        if ((dx | dy | dz) == 0) {
-            r = (int)scmap[leaf];
-        } else {
-            int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
-            if (px >= 0 && py >= 0 && pz >= 0) {
-                long long l = linked_leaf(lg, t, px, py, pz);
-                if (l >= 0) r = (int)scmap[l];
-            }
-        }
-        nrank[threadIdx.x] = r;
-    }
-    if (threadIdx.x == 0) { ncb = 0; cursor = 0; ncand = 0; }
-    __syncthreads();
-
-    // candidate home bins: H (in subcells) within [S + lo_off, S + hi_off] of some S of this brick
-    const int span = 4 + gp.hi_off - gp.lo_off;
-    const int nc = span * span * span;
-    unsigned local_pts = 0;
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-        int cx = c % span, cy = (c / span) % span, cz = c / (span * span);
-        int hx = sx0 + gp.lo_off + cx, hy = sy0 + gp.lo_off + cy, hz = sz0 + gp.lo_off + cz;
-        if (hx < 0 || hy < 0 || hz < 0) continue;
-        int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
-        if (bx < -1 || bx > 1 || by < -1 || by > 1 || bz < -1 || bz > 1) continue;
-        int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
-        if (r < 0) continue;
-        unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
-        uint32_t b = bin_off[bin], e = bin_off[bin + 1];
-        if (e > b) {
-            int k = atomicAdd(&ncb, 1);
-            cb_beg[k] = b;
-            cb_cnt[k] = e - b;
-            cb_home[k] = ((hx - sx0 + 16) << 10) | ((hy - sy0 + 16) << 5) | (hz - sz0 + 16);  // relative, biased
-            local_pts += e - b;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) local_pts += __shfl_down_sync(0xFFFFFFFFu, local_pts, o);
-    if ((threadIdx.x & 31) == 0 && local_pts) atomicAdd(&ncand, local_pts);
-    __syncthreads();
-
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int vx = lane & 3, vy = (lane >> 2) & 3, vz = lane >> 4;
+
+    for (int v = threadIdx.x; v < 1024; v += blockDim.x)
+        reinterpret_cast<uint4*>(tile)[v] = make_uint4(gp.tbits, gp.tbits, gp.tbits, gp.tbits);
+    if (warp == 0) {
+        int r = -1;
+        uint32_t beg = 0, cnt = 0;
+        if (lane < 27) {
+            int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+            if ((dx | dy | dz) == 0) {
+                r = (int)scmap[leaf];
+            } else {
+                int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
+                if (px >= 0 && py >= 0 && pz >= 0) {
+                    long long l = linked_leaf(lg, t, px, py, pz);
+                    if (l >= 0) r = (int)scmap[l];
+                }
+            }
+            if (r >= 0) {
+                beg = __ldg(bin_off + (size_t)r * 64);
+                cnt = __ldg(bin_off + (size_t)r * 64 + 64) - beg;
+            }
+            nrank[lane] = r;
+            nb_beg[lane] = beg;
+        }
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane < 28) nb_pre[lane] = incl - cnt;
+    }
+    __syncthreads();
+    const uint32_t ncand = nb_pre[27];
     const float Tf = __uint_as_float(gp.tbits);
 
     if (ncand <= (unsigned)gp.dense_min) {
         // ------------------------------------------------------ scatter form
-        for (int v = threadIdx.x; v < 4096; v += blockDim.x) tile[v] = gp.tbits;
-        __syncthreads();
-        const float fvx = (float)vx, fvy = (float)vy;
-        const int nb = ncb;
-        while (true) {
-            int e = 0;
-            if (lane == 0) e = atomicAdd(&cursor, 1);
-            e = __shfl_sync(0xFFFFFFFFu, e, 0);
-            if (e >= nb) break;
-            const uint32_t beg = cb_beg[e], cnt = cb_cnt[e];
-            // home subcell relative to the brick's first subcell
-            const int home = cb_home[e];
-            const int dhx = ((home >> 10) & 31) - 16, dhy = ((home >> 5) & 31) - 16, dhz = (home & 31) - 16;
-            for (uint32_t base = 0; base < cnt; base += 32) {
-                const int nv = (int)min(32u, cnt - base);
-                float4 q = make_float4(0, 0, 0, 0);
-                int box = 1 << 12;
-                if (lane < nv) {
-                    q = pts[beg + base + lane];
-                    const int pk = __float_as_int(q.w);
-                    int rx0, rx1, ry0, ry1, rz0, rz1;
-                    const bool ne = mask_range(pk, 0, rx0, rx1) & mask_range(pk, 1, ry0, ry1) & mask_range(pk, 2, rz0, rz1);
-                    int l0x = max(0, dhx + rx0), l1x = min(3, dhx + rx1);
-                    int l0y = max(0, dhy + ry0), l1y = min(3, dhy + ry1);
-                    int l0z = max(0, dhz + rz0), l1z = min(3, dhz + rz1);
-                    if (ne && l0x <= l1x && l0y <= l1y && l0z <= l1z)
-                        box = l0x | (l1x << 2) | (l0y << 4) | (l1y << 6) | (l0z << 8) | (l1z << 10);
+        // A point's reach inside this brick: its member subcells, cut to the
+        // voxels within rcut of it on every axis (brick-local voxel box).  The
+        // live points of a batch of candidates go to a shared list; then every
+        // warp walks the whole list but updates only the 4 tile rows y it owns
+        // (lanes: x = lane & 15, one of 2 rows; z walked in a loop), so no two
+        // threads ever update the same voxel at once and no atomics are needed.
+        float4* live_pts = reinterpret_cast<float4*>(scratch);
+        for (uint32_t cbase = 0; cbase < ncand; cbase += kLive) {
+            if (threadIdx.x == 0) nlive = 0;
+            __syncthreads();
+            const uint32_t cend = min(ncand, cbase + (uint32_t)kLive);
+            for (uint32_t idx = cbase + threadIdx.x; idx < cend; idx += blockDim.x) {
+                int nb = 0;  // neighbour holding point idx: last nb with nb_pre[nb] <= idx
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (nb + step < 27 && nb_pre[nb + step] <= idx) nb += step;
+                const float4 q = pts[nb_beg[nb] + (idx - nb_pre[nb])];
+                const int pk = __float_as_int(q.w);
+                const float pw[3] = {q.x, q.y, q.z};
+                const int org[3] = {ox, oy, oz};
+                int packed = 0;
+                bool ok = true;
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    int rl, ru;
+                    ok &= mask_range(pk, a, rl, ru);
+                    const int dh = (((int)pw[a]) >> 2) - (org[a] >> 2);  // home subcell, brick-relative
+                    const float lp = fsub(pw[a], (float)org[a]);
+                    int v0 = max(4 * (dh + rl), (int)ceilf(fsub(lp, gp.rcut)));
+                    int v1 = min(4 * (dh + ru) + 3, (int)floorf(fadd(lp, gp.rcut)));
+                    v0 = max(v0, 0);
+                    v1 = min(v1, 15);
+                    ok &= v0 <= v1;
+                    packed |= (v0 | (v1 << 4)) << (8 * a);
                 }
-                unsigned live = __ballot_sync(0xFFFFFFFFu, (box & (1 << 12)) == 0);
-                while (live) {
-                    const int j = __ffs(live) - 1;
-                    live &= live - 1;
-                    const float px = __shfl_sync(0xFFFFFFFFu, q.x, j);
-                    const float py = __shfl_sync(0xFFFFFFFFu, q.y, j);
-                    const float pz = __shfl_sync(0xFFFFFFFFu, q.z, j);
-                    const int bxv = __shfl_sync(0xFFFFFFFFu, box, j);
-                    const int lx0 = bxv & 3, lx1 = (bxv >> 2) & 3, ly0 = (bxv >> 4) & 3, ly1 = (bxv >> 6) & 3;
-                    const int lz0 = (bxv >> 8) & 3, lz1 = (bxv >> 10) & 3;
-                    for (int lz = lz0; lz <= lz1; lz++) {
-                        const float z0 = (float)(oz + 4 * lz + vz), z1 = (float)(oz + 4 * lz + vz + 2);
-                        const float dz0 = fsub(pz, z0), dz1 = fsub(pz, z1);
-                        for (int ly = ly0; ly <= ly1; ly++) {
-                            const float dy = fsub(py, (float)(oy + 4 * ly) + fvy);
-                            for (int lx = lx0; lx <= lx1; lx++) {
-                                const float dx = fsub(px, (float)(ox + 4 * lx) + fvx);
-                                const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                                const float d0 = __fmaf_rn(dz0, dz0, dxy);
-                                const float d1 = __fmaf_rn(dz1, dz1, dxy);
-                                const int v0 = ((4 * lz + vz) << 8) | ((4 * ly + vy) << 4) | (4 * lx + vx);
-                                const uint32_t b0 = __float_as_uint(d0), b1 = __float_as_uint(d1);
-                                if (b0 < gp.tbits) atomicMin(&tile[v0], b0);
-                                if (b1 < gp.tbits) atomicMin(&tile[v0 + 512], b1);
+                if (ok) live_pts[atomicAdd(&nlive, 1)] = make_float4(q.x, q.y, q.z, __int_as_float(packed));
+            }
+            __syncthreads();
+            const int nl = nlive;
+            const int xl = lane & 15, yl = lane >> 4;
+            for (int e = 0; e < nl; e++) {
+                const float4 L = live_pts[e];
+                const int bx = __float_as_int(L.w);
+                const int x0 = bx & 15, x1 = (bx >> 4) & 15;
+                const int y0 = max((bx >> 8) & 15, 4 * warp), y1 = min((bx >> 12) & 15, 4 * warp + 3);
+                const int z0 = (bx >> 16) & 15, z1 = (bx >> 20) & 15;
+                if (y0 > y1) continue;
+                const int x = x0 + xl;
+                const float dx = fsub(L.x, (float)(ox + x));
+                for (int ys = y0; ys <= y1; ys += 2) {
+                    const int y = ys + yl;
+                    if (x <= x1 && y <= y1) {
+                        const float dy = fsub(L.y, (float)(oy + y));
+                        const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                        if (__float_as_uint(dxy) < gp.tbits) {
+                            uint32_t* col = tile + (z0 << 8) + (y << 4) + x;
+                            float fz = (float)(oz + z0);  // integer-valued: += 1 is exact
+                            for (int z = z0; z <= z1; z++, col += 256, fz += 1.0f) {
+                                const float dz = fsub(L.z, fz);
+                                const uint32_t d = __float_as_uint(__fmaf_rn(dz, dz, dxy));
+                                if (d < *col) *col = d;
                             }
                         }
                     }
                 }
+                __syncwarp();  // this entry's updates are visible to every lane before the next
             }
+            __syncthreads();  // the list is refilled by the next batch
         }
     } else {
         // ------------------------------------------------------- gather form
@@ -447,49 +451,74 @@ __global__ void __launch_bounds__(kGatherThreads, 5) k_gather(TreeView t, LeafGr
                 __syncwarp();
                 nq = 0;
             };
-            for (int e = 0; e < noffs; e++) {
-                const int4 o = offs[e];
-                if ((float)o.w >= wmax) break;
-                const int hx = Sx + o.x, hy = Sy + o.y, hz = Sz + o.z;
-                if (hx < 0 || hy < 0 || hz < 0) continue;
-                const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
-                const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
-                if (r < 0) continue;
-                const unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
-                const uint32_t beg = __ldg(bin_off + bin), end = __ldg(bin_off + bin + 1);
-                if (beg == end) continue;
-                const int need = member_bits(o.x, o.y, o.z);
-                for (uint32_t base = beg; base < end; base += 32) {
-                    const uint32_t j = base + lane;
-                    bool ok = false;
-                    float4 q = make_float4(0, 0, 0, 0);
-                    if (j < end) {
-                        q = pts[j];
-                        if ((__float_as_int(q.w) & need) == need) {
-                            const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q.x), fsub(q.x, bhx)));
-                            const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q.y), fsub(q.y, bhy)));
-                            const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q.z), fsub(q.z, bhz)));
-                            const float lb = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
-                            ok = lb < wmax;
+            // offsets in groups of 32: each lane resolves one offset's bin range up
+            // front (one memory round trip per group instead of one per bin)
+            bool done = false;
+            for (int g0 = 0; g0 < noffs && !done; g0 += 32) {
+                const int e = g0 + lane;
+                uint32_t gbeg = 0, gcnt = 0;
+                int gneed = 0;
+                float glb = INFINITY;
+                if (e < noffs) {
+                    const int4 o = offs[e];
+                    glb = (float)o.w;
+                    gneed = member_bits(o.x, o.y, o.z);
+                    const int hx = Sx + o.x, hy = Sy + o.y, hz = Sz + o.z;
+                    if (hx >= 0 && hy >= 0 && hz >= 0) {
+                        const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
+                        const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
+                        if (r >= 0) {
+                            const unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
+                            gbeg = __ldg(bin_off + bin);
+                            gcnt = __ldg(bin_off + bin + 1) - gbeg;
                         }
                     }
-                    const unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
-                    if (ok) {
-                        const int k = nq + __popc(live & lt);
-                        qx[k] = q.x;
-                        qy[k] = q.y;
-                        qz[k] = q.z;
-                    }
-                    nq += __popc(live);
-                    if (nq >= 32) drain();
                 }
-                if (nq) drain();
-                // merge the halves' minima; wmax = the largest voxel minimum
-                m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
-                m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
-                m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
-                m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
-                wmax = __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3)))));
+                unsigned nonempty = __ballot_sync(0xFFFFFFFFu, gcnt > 0);
+                while (nonempty) {
+                    const int l = __ffs(nonempty) - 1;
+                    nonempty &= nonempty - 1;
+                    // sorted by lb^2: the first bin at or beyond wmax ends the subcell
+                    if (__shfl_sync(0xFFFFFFFFu, glb, l) >= wmax) {
+                        done = true;
+                        break;
+                    }
+                    const uint32_t beg = __shfl_sync(0xFFFFFFFFu, gbeg, l);
+                    const uint32_t end = beg + __shfl_sync(0xFFFFFFFFu, gcnt, l);
+                    const int need = __shfl_sync(0xFFFFFFFFu, gneed, l);
+                    for (uint32_t base = beg; base < end; base += 32) {
+                        const uint32_t j = base + lane;
+                        bool ok = false;
+                        float4 q = make_float4(0, 0, 0, 0);
+                        if (j < end) {
+                            q = pts[j];
+                            if ((__float_as_int(q.w) & need) == need) {
+                                const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q.x), fsub(q.x, bhx)));
+                                const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q.y), fsub(q.y, bhy)));
+                                const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q.z), fsub(q.z, bhz)));
+                                const float lb = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
+                                ok = lb < wmax;
+                            }
+                        }
+                        const unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
+                        if (ok) {
+                            const int k = nq + __popc(live & lt);
+                            qx[k] = q.x;
+                            qy[k] = q.y;
+                            qz[k] = q.z;
+                        }
+                        nq += __popc(live);
+                        if (nq >= 32) drain();
+                    }
+                    if (nq) drain();
+                    // merge the halves' minima; wmax = the largest voxel minimum
+                    m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
+                    m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
+                    m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
+                    m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
+                    wmax = __uint_as_float(
+                        __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3)))));
+                }
             }
             if (hf == 0) {
                 const int v = ((4 * lz) << 8) | ((4 * ly + cy) << 4) | (4 * lx + cx);
