@@ -251,6 +251,118 @@ def bench_reference(args):
     return 0
 
 
+# ---------------------------------------------------------------- served form
+SERVE_KINDS = (  # generator, grid (top -> leaf), mode, r = R, rho, boundval
+    ("shell", (3, 3, 3, 4), 0, 1.0, 1.0, 0.0),
+    ("fluid", (3, 3, 3, 4), 1, 4.0, 2.0, 3.0),
+    ("surface", (4, 4, 3, 4), 0, 1.5, 1.5, 0.0),
+)
+
+
+def serve_pools(nmax, seed):
+    """One pinned host pool of nmax points per generator (random order, so that the
+    first n points are a uniform subset)."""
+    import datasets
+    import torch
+
+    rng = np.random.default_rng(seed)
+    pools = []
+    for kind, *_ in SERVE_KINDS:
+        if kind == "shell":
+            p = datasets.shell(nmax, seed=int(rng.integers(1 << 30)))
+        elif kind == "fluid":
+            p, _ = datasets.fluid(nmax, seed=int(rng.integers(1 << 30)))
+        else:
+            p = datasets.surface(nmax, seed=int(rng.integers(1 << 30)))
+        p = p[rng.permutation(p.shape[0])]
+        t = torch.from_numpy(np.ascontiguousarray(p, dtype=np.float32)).pin_memory()
+        pools.append(t)
+    return pools
+
+
+def serve_requests(count, seed, pools, lo=1e4, hi=4e6, upd_frac=0.3, nres=8):
+    """The request stream: size log-uniform in [lo, hi], generator uniform, 30% incremental
+    updates (5% of a resident grid's points moved by N(0, 2)), FP32 / FP16 storage
+    alternating.  Payloads are prepared up front in pinned host memory."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    reqs, resident = [], {}
+    for i in range(count):
+        if resident and rng.random() < upd_frac:
+            rid = int(rng.choice(sorted(resident)))
+            k, prev = resident[rid]
+            q = prev.numpy().copy()
+            idx = rng.choice(q.shape[0], max(1, q.shape[0] // 20), replace=False)
+            q[idx] += rng.normal(0.0, 2.0, size=(idx.size, 3)).astype(np.float32)
+            pts = torch.from_numpy(q).pin_memory()
+            resident[rid] = (k, pts)
+        else:
+            k = int(rng.integers(len(SERVE_KINDS)))
+            n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+            pts = pools[k][:n]
+            rid = -1
+            if len(resident) < nres and rng.random() < 0.25:
+                rid = len(resident)
+                resident[rid] = (k, pts)
+        reqs.append({"kind": k, "points": pts, "resident_id": rid, "dtype": 3 if i % 2 == 0 else 100})
+    return reqs
+
+
+def serve_run(reqs, rate, workers, seed, cap):
+    """Submit the stream with Poisson arrivals at `rate` req/s (rate None: all at once) to
+    a server with `workers` workers; returns latency percentiles and throughput."""
+    import gbvdb
+
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(reqs)) if rate else np.zeros(len(reqs))
+    arrive = np.cumsum(gaps)
+    srv = gbvdb.Server(0, workers=workers, mem_cap_bytes=cap)
+    tickets = []
+    t0 = time.perf_counter()
+    for r, ta in zip(reqs, arrive):
+        d = ta - (time.perf_counter() - t0)
+        if d > 0:
+            time.sleep(d)
+        _, dims, mode, rad, rho, bv = SERVE_KINDS[r["kind"]]
+        tickets.append(srv.submit(r["points"].numpy(), log2dims=dims, radius=rad, gather_radius=rho, mode=mode,
+                                  dtype=r["dtype"], boundval=bv, resident_id=r["resident_id"]))
+    res = [srv.wait(t) for t in tickets]
+    srv.close()
+    bad = [x["status"] for x in res if x["status"] not in (gbvdb.OK, gbvdb.NOOP, gbvdb.DEPTH_UNSUPPORTED)]
+    lat = np.array([x["t_end_ms"] - x["t_submit_ms"] for x in res])
+    span_s = (max(x["t_end_ms"] for x in res) - min(x["t_submit_ms"] for x in res)) / 1000.0
+    pts = float(sum(int(r["points"].shape[0]) for r in reqs))
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "points_per_s": pts / span_s, "requests_per_s": len(reqs) / span_s, "errors": len(bad),
+            "checksums": [x["checksum"] for x in res]}
+
+
+def bench_served(args):
+    """Served form vs the plain per-call loop (the same calls back to back on one
+    worker) on the mixed-size stream, per arrival rate and at saturation."""
+    pools = serve_pools(int(args.serve_max_points), seed=4)
+    reqs = serve_requests(args.serve_requests, seed=4, pools=pools, hi=args.serve_max_points)
+    cap = 120 << 30
+    out = {"requests": len(reqs), "workers": args.serve_workers, "cap_bytes": cap,
+           "stream": "log-uniform [1e4, %.0e] points; shell / fluid / surface generators; 30%% incremental "
+                     "updates of resident grids (5%% of points moved by N(0,2)); FP32 / FP16 alternating; "
+                     "Poisson arrivals; host (pinned) points, H2D inside each job" % args.serve_max_points,
+           "plain": "one worker: the per-frame calls of each request back to back on one stream",
+           "points_total": float(sum(int(r["points"].shape[0]) for r in reqs)), "rates": []}
+    # warm-up (library, allocator pools)
+    serve_run(reqs[: min(20, len(reqs))], None, args.serve_workers, 0, cap)
+    for rate in [None] + list(args.serve_rates):
+        srv = serve_run(reqs, rate, args.serve_workers, 5, cap)
+        pln = serve_run(reqs, rate, 1, 5, cap)
+        same = srv.pop("checksums") == pln.pop("checksums")
+        out["rates"].append({"rate_req_s": rate if rate else "saturation", "served": srv, "plain": pln,
+                             "same_results": same})
+    sat = out["rates"][0]
+    out["speedup_points_per_s_at_saturation"] = sat["served"]["points_per_s"] / sat["plain"]["points_per_s"]
+    return out
+
+
 def bench_ours(args):
     import torch
 
@@ -397,9 +509,14 @@ def bench_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, vel)
+    if rank == 0 and world == 1 and not args.no_served:
+        grid.close()
+        frames.clear()
+        torch.cuda.empty_cache()
+        line["served"] = bench_served(args)
     if rank == 0 and world == 1 and args.ref_cuda:
         grid.close()
-        del frames
+        frames.clear()
         torch.cuda.empty_cache()
         fh = [(pos + 0.5 * (f + 1) * vel).astype(np.float32) for f in range(5)]
         line["reference_cuda"] = bench_ref_cuda(fh)
@@ -418,6 +535,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-cuda", action="store_true", help="also time the reference's own CUDA kernels")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-form stream")
+    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-workers", type=int, default=8)
+    ap.add_argument("--serve-max-points", type=float, default=4e6)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 500.0, 2000.0])
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

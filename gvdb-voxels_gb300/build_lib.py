@@ -16,7 +16,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbvdb.so")
 
-SOURCES = ["scan.cu", "topology.cu", "atlas.cu", "points.cu", "grid.cu"]
+SOURCES = ["scan.cu", "topology.cu", "atlas.cu", "points.cu", "grid.cu", "server.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]

@@ -209,22 +209,57 @@ __global__ void k_fill_interior(const AtlasNode* __restrict__ amap, int used, T*
 constexpr int kNoAllocMaxSlots = 65536;
 static __device__ __align__(256) double g_slot_partials[kNoAllocMaxSlots];
 
-// one block per slot (grid-stride over slots): fixed-order FP64 sum of the 4096 interior voxels
+// Compensated FP32 accumulation (Knuth's TwoSum: s + e == a + b exactly in
+// round-to-nearest): a running pair (hi, lo) whose value hi + lo carries about
+// 48 significant bits, so a brick's 4096 values are summed to near-FP64 accuracy
+// with FP32 arithmetic (GB300's FP64 rate is a small fraction of its FP32 rate).
+// Non-finite sums keep hi (inf / nan) and drop the error term.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    if (isfinite(s)) lo = __fadd_rn(lo, e);
+}
+__device__ __forceinline__ void df_merge(float& hi, float& lo, float h2, float l2) {
+    df_add(hi, lo, h2);
+    lo = __fadd_rn(lo, l2);
+}
+
+// one block per slot (grid-stride over slots): fixed-order sum of the 4096 interior
+// voxels (compensated FP32 per thread and across the warp, FP64 across the warps),
+// so the result is deterministic.  Launched with 256 threads per block.
 template <typename T>
 __global__ void k_slot_sums(const AtlasNode* __restrict__ amap, int used, const T* __restrict__ interior,
                             double* __restrict__ partials) {
     __shared__ double red[32];
+    constexpr int V = 16 / sizeof(T);  // elements per 16-byte load
     for (int s = blockIdx.x; s < used; s += gridDim.x) {
-        double acc = 0.0;
-        if (amap[s].leaf >= 0)
-            for (int v = threadIdx.x; v < 4096; v += blockDim.x) acc += (double)to_f32(interior[(size_t)s * 4096 + v]);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        float hi = 0.0f, lo = 0.0f;
+        if (amap[s].leaf >= 0) {
+            // all of this thread's 16-byte loads of the brick in flight together
+            const uint4* src = reinterpret_cast<const uint4*>(interior + (size_t)s * 4096);
+            constexpr int kLoads = 4096 / V / 256;
+            uint4 w[kLoads];
+#pragma unroll
+            for (int k = 0; k < kLoads; k++) w[k] = __ldcs(src + threadIdx.x + 256 * k);
+#pragma unroll
+            for (int k = 0; k < kLoads; k++) {
+                const T* e = reinterpret_cast<const T*>(&w[k]);
+#pragma unroll
+                for (int q = 0; q < V; q++) df_add(hi, lo, to_f32(e[q]));
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xFFFFFFFFu, hi, o), l2 = __shfl_down_sync(0xFFFFFFFFu, lo, o);
+            df_merge(hi, lo, h2, l2);
+        }
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)hi + (double)lo;
         __syncthreads();
-        if (threadIdx.x < 32) {
-            double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xFFFFFFFFu, t, o);
-            if (threadIdx.x == 0) partials[s] = t;
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w8 = 0; w8 < (int)(blockDim.x >> 5); w8++) t += red[w8];
+            partials[s] = t;
         }
         __syncthreads();
     }
@@ -299,6 +334,19 @@ void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* int
         k_checksum<__half><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __half*)interior, out);
     else
         k_checksum<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, out);
+}
+void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
+                           double* out, cudaStream_t s) {
+    if (used > 0) {
+        unsigned blocks = (unsigned)std::min(used, 152 * 8);
+        if (dtype == 3)
+            k_slot_sums<float><<<blocks, 256, 0, s>>>(amap, used, (const float*)interior, partials);
+        else if (dtype == 100)
+            k_slot_sums<__half><<<blocks, 256, 0, s>>>(amap, used, (const __half*)interior, partials);
+        else
+            k_slot_sums<__nv_bfloat16><<<blocks, 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
+    }
+    k_sum_partials<<<1, 1024, 0, s>>>(partials, used, out);
 }
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value, cudaStream_t s) {
     if (used <= 0) return;

@@ -835,6 +835,24 @@ struct gbvdb_grid_s {
         return GBVDB_OUT_OF_MEMORY;                       \
     }
 
+// Grids allocate with cudaMallocAsync from the device's default memory pool.  By
+// default that pool returns freed memory to the driver at every synchronisation,
+// so a grid that is rebuilt or replaced pays for fresh driver allocations; keep
+// the freed memory in the pool instead (a setting of this process's pool only).
+static void keep_pool_memory(int device) {
+    static std::mutex mu;
+    static bool done[128] = {false};
+    std::lock_guard<std::mutex> lk(mu);
+    if (device < 0 || device >= 128 || done[device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+    done[device] = true;
+}
+
 extern "C" {
 
 gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
@@ -846,6 +864,7 @@ gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
         return GBVDB_CUDA_ERROR;
     }
     if (cudaSetDevice(device) != cudaSuccess) return GBVDB_CUDA_ERROR;
+    keep_pool_memory(device);
     gbvdb_grid g = new (std::nothrow) gbvdb_grid_s();
     if (!g) return GBVDB_OUT_OF_MEMORY;
     g->device = device;
@@ -947,9 +966,7 @@ gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron, int
     C.apron = apron;
     C.esize = es;
     long long slots = (long long)g->ax * g->ay * g->az;
-    C.cap_slots = 0;
-    g->release(C.interior);
-    g->release(C.apron_buf);
+    // a channel added again keeps its storage when it is large enough
     g->grow(C.interior, (size_t)slots * 4096 * es);
     g->grow(C.apron_buf, (size_t)slots * kApronStride * es);
     g->check(cudaMemsetAsync(C.interior.p, 0, (size_t)slots * 4096 * es, g->stream), "channel clear");
@@ -1181,10 +1198,10 @@ gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
     GBVDB_GUARD(g)
     if (chan < 0 || chan >= 8 || !g->ch[chan].used || !out) return GBVDB_INVALID_ARG;
     g->grow(g->misc, 256);
+    g->grow(g->xfer, (size_t)std::max(g->atlas_last, 1) * 8);
     double* d = reinterpret_cast<double*>(g->ptr<char>(g->misc) + 192);
-    g->check(cudaMemsetAsync(d, 0, 8, g->stream), "checksum clear");
-    launch_checksum(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p, d,
-                    g->stream);
+    launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
+                          g->ptr<double>(g->xfer), d, g->stream);
     g->check_launch("checksum");
     g->readback(out, d, 8);
     return GBVDB_OK;
@@ -1248,6 +1265,21 @@ gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4) {
     out4[3] = g->sc_nbricks;
     return GBVDB_OK;
     GBVDB_END(g)
+}
+
+// device bytes held by the grid's buffers (pools, atlas, scratch): the server's memory accounting
+size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
+    if (!g) return 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    size_t b = 0;
+    const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
+                            &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
+                            &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
+                            &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot};
+    for (const DevBuf* d : bufs) b += d->cap;
+    for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
+    for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;
+    return b;
 }
 
 gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap) {

@@ -65,6 +65,9 @@ void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, 
                   const void* interior, void* apron, uint32_t boundbits, cudaStream_t s);
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out,
                           cudaStream_t s);
+// deterministic FP64 channel sum: per-slot partials, then one fixed-order block
+void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
+                           double* out, cudaStream_t s);
 void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* interior, double* out,
                      cudaStream_t s);
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value,

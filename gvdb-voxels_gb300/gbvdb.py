@@ -37,7 +37,25 @@ EXPORTS = [
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning",
+    "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
+    "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
+
+
+class Job(ctypes.Structure):
+    """gbvdb_job (include/gbvdb.h)."""
+    _fields_ = [("points", ctypes.c_void_p), ("n", ctypes.c_int64), ("points_on_device", ctypes.c_int32),
+                ("stride", ctypes.c_int32), ("levs", ctypes.c_int32), ("log2dim_leaf_first", ctypes.c_int32 * 8),
+                ("resident_id", ctypes.c_int32), ("mode", ctypes.c_int32), ("dtype", ctypes.c_int32),
+                ("radius", ctypes.c_float), ("insert_radius", ctypes.c_float), ("gather_radius", ctypes.c_float),
+                ("boundval", ctypes.c_float), ("orig", ctypes.c_float * 3)]
+
+
+class JobResult(ctypes.Structure):
+    """gbvdb_job_result (include/gbvdb.h)."""
+    _fields_ = [("status", ctypes.c_int32), ("bricks", ctypes.c_int64), ("sc_len", ctypes.c_int64),
+                ("checksum", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
+                ("t_end_ms", ctypes.c_double)]
 TUNE_DENSE_MIN = 1
 
 
@@ -98,6 +116,14 @@ def load(path=LIB_PATH):
     L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
+    L.gbvdb_server_create.argtypes = [i32, i32, i64, ctypes.POINTER(vp)]
+    L.gbvdb_server_submit.argtypes = [vp, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_server_wait.argtypes = [vp, i64, ctypes.POINTER(JobResult)]
+    L.gbvdb_server_poll.argtypes = [vp, i64, ctypes.POINTER(ctypes.c_int)]
+    L.gbvdb_server_resident.argtypes = [vp, i32, ctypes.POINTER(vp)]
+    L.gbvdb_server_release.argtypes = [vp, i32]
+    L.gbvdb_server_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_server_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -140,7 +166,20 @@ class Grid:
             msg = (self.L.gbvdb_last_error(self._h) or b"").decode()
         raise GbvdbError(st, "%s failed: %s" % (what, msg))
 
+    @classmethod
+    def _borrow(cls, handle):
+        """A view of a grid owned elsewhere (a server's resident grid): never destroyed here."""
+        g = cls.__new__(cls)
+        g.L = load()
+        g._h = handle
+        g._borrowed = True
+        g._points = None
+        return g
+
     def close(self):
+        if getattr(self, "_borrowed", False):
+            self._h = None
+            return
         if getattr(self, "_h", None) is not None and self._h.value:
             self.L.gbvdb_destroy(self._h)
             self._h = None
@@ -308,3 +347,101 @@ class Grid:
 def bf16_to_f32(u16):
     """Raw bfloat16 bits (uint16) -> float32."""
     return (u16.astype(np.uint32) << 16).view(np.float32)
+
+
+class Server:
+    """The served form (include/gbvdb.h, no counterpart in the reference): a request
+    loop whose worker threads run voxelize-and-gather jobs concurrently on one GPU.
+
+    submit() takes host points (a C-contiguous float32 (N, 3) numpy array, kept
+    alive until the job ends) or a CUDA tensor; wait() returns a dict with the
+    job's status, bricks, subcell-list length, FP64 checksum and server-clock
+    times (ms)."""
+
+    def __init__(self, device=0, workers=8, mem_cap_bytes=120 << 30):
+        self.L = load()
+        self.s = ctypes.c_void_p()
+        st = self.L.gbvdb_server_create(int(device), int(workers), int(mem_cap_bytes), ctypes.byref(self.s))
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_create")
+        self._keep = {}
+
+    def submit(self, points, log2dims=(3, 3, 3, 4), radius=1.0, insert_radius=None, gather_radius=1.0, mode=0,
+               dtype=T_FLOAT, boundval=0.0, orig=(0, 0, 0), resident_id=-1):
+        j = Job()
+        if hasattr(points, "data_ptr"):
+            ptr, n, stride = _dev_ptr(points)
+            j.points_on_device = 1
+        else:
+            arr = np.ascontiguousarray(points, dtype=np.float32)
+            if arr.ndim != 2 or arr.shape[1] != 3:
+                raise ValueError("host points must be (N, 3) float32")
+            ptr, n, stride = arr.ctypes.data, arr.shape[0], 12
+            j.points_on_device = 0
+            points = arr
+        j.points, j.n, j.stride = ptr, n, stride
+        dims = list(log2dims)[::-1]  # top -> leaf given; leaf first here
+        j.levs = len(dims)
+        for i, d in enumerate(dims):
+            j.log2dim_leaf_first[i] = int(d)
+        j.resident_id = int(resident_id)
+        j.mode = int(mode)
+        j.dtype = int(dtype)
+        j.radius = float(radius)
+        j.insert_radius = float(radius if insert_radius is None else insert_radius)
+        j.gather_radius = float(gather_radius)
+        j.boundval = float(boundval)
+        for a in range(3):
+            j.orig[a] = float(orig[a])
+        t = ctypes.c_int64()
+        st = self.L.gbvdb_server_submit(self.s, ctypes.byref(j), ctypes.byref(t))
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_submit")
+        self._keep[t.value] = points
+        return t.value
+
+    def wait(self, ticket):
+        r = JobResult()
+        st = self.L.gbvdb_server_wait(self.s, int(ticket), ctypes.byref(r))
+        self._keep.pop(ticket, None)
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_wait")
+        return {"status": r.status, "bricks": r.bricks, "sc_len": r.sc_len, "checksum": r.checksum,
+                "t_submit_ms": r.t_submit_ms, "t_start_ms": r.t_start_ms, "t_end_ms": r.t_end_ms}
+
+    def poll(self, ticket):
+        d = ctypes.c_int()
+        st = self.L.gbvdb_server_poll(self.s, int(ticket), ctypes.byref(d))
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_poll")
+        return bool(d.value)
+
+    def resident(self, resident_id):
+        """A Grid view of an idle resident grid (not owned: do not destroy)."""
+        g = ctypes.c_void_p()
+        st = self.L.gbvdb_server_resident(self.s, int(resident_id), ctypes.byref(g))
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_resident")
+        return Grid._borrow(g)
+
+    def release(self, resident_id):
+        st = self.L.gbvdb_server_release(self.s, int(resident_id))
+        if st != OK:
+            raise GbvdbError(st, "gbvdb_server_release")
+
+    def stats(self):
+        a = (ctypes.c_int64 * 6)()
+        self.L.gbvdb_server_stats(self.s, a)
+        return dict(zip(["queued", "running", "completed", "held_bytes", "cap_bytes", "resident"], list(a)))
+
+    def close(self):
+        if self.s:
+            self.L.gbvdb_server_destroy(self.s)
+            self.s = ctypes.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

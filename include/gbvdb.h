@@ -165,6 +165,54 @@ GBVDB_API gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap);
  * linked leaves of the last insert} */
 GBVDB_API gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4);
 
+/* --- served form (no counterpart in the reference) -------------------------
+ * A request loop over voxelize-and-gather jobs: worker threads, each with its
+ * own stream and reusable grid, run queued jobs concurrently on the device.  A
+ * job is the per-frame sequence SetPoints, RebuildTopology, UpdateAtlas,
+ * InsertPointsSubcell(4), GatherDensity / GatherLevelSet into channel 0,
+ * UpdateApron(0, boundval), then the FP64 checksum of channel 0.  With
+ * resident_id >= 0 the job runs on a grid kept on the device under that id
+ * (created on first use; later jobs on it take the incremental rebuild path);
+ * jobs of one resident grid run in submission order.  Jobs are admitted while
+ * the device bytes held by all grids plus the job's estimate stay within
+ * mem_cap_bytes (one job always runs). */
+typedef struct gbvdb_server_s* gbvdb_server;
+typedef struct {
+    const void* points;          /* float3 positions, element i at points + i*stride */
+    int64_t n;                   /* number of points */
+    int32_t points_on_device;    /* 1: device pointer (borrowed until the job ends); 0: host memory */
+    int32_t stride;              /* bytes between points (0 = 12) */
+    int32_t levs;                /* Configure(levs, log2dim): log2 dims, leaf first */
+    int32_t log2dim_leaf_first[8];
+    int32_t resident_id;         /* -1: fresh grid; >= 0: resident grid id */
+    int32_t mode;                /* 0 GatherDensity, 1 GatherLevelSet */
+    int32_t dtype;               /* GBVDB_T_FLOAT, GBVDB_T_HALF or GBVDB_T_BFLOAT16 */
+    float radius;                /* RebuildTopology radius */
+    float insert_radius;         /* InsertPointsSubcell radius */
+    float gather_radius;         /* gather radius rho */
+    float boundval;              /* UpdateApron boundary value */
+    float orig[3];               /* RebuildTopology orig / insert and gather trans */
+} gbvdb_job;
+typedef struct {
+    int32_t status;              /* gbvdb_status of the job */
+    int64_t bricks;              /* linked leaves of the insert */
+    int64_t sc_len;              /* subcell list length (pSCPntsLength) */
+    double checksum;             /* FP64 sum of channel 0 */
+    double t_submit_ms, t_start_ms, t_end_ms;  /* server clock */
+} gbvdb_job_result;
+GBVDB_API gbvdb_status gbvdb_server_create(int device, int workers, int64_t mem_cap_bytes, gbvdb_server* out);
+GBVDB_API gbvdb_status gbvdb_server_submit(gbvdb_server s, const gbvdb_job* job, int64_t* ticket);
+/* blocks until the job ends; the ticket is released */
+GBVDB_API gbvdb_status gbvdb_server_wait(gbvdb_server s, int64_t ticket, gbvdb_job_result* out);
+GBVDB_API gbvdb_status gbvdb_server_poll(gbvdb_server s, int64_t ticket, int* done);
+/* the grid of an idle resident id (exports, checksums); valid until released */
+GBVDB_API gbvdb_status gbvdb_server_resident(gbvdb_server s, int32_t resident_id, gbvdb_grid* out);
+GBVDB_API gbvdb_status gbvdb_server_release(gbvdb_server s, int32_t resident_id);
+/* out6 = {queued, running, completed, device bytes held, memory cap, resident grids} */
+GBVDB_API gbvdb_status gbvdb_server_stats(gbvdb_server s, int64_t* out6);
+/* finishes the queued jobs, then frees every grid */
+GBVDB_API gbvdb_status gbvdb_server_destroy(gbvdb_server s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,134 @@
+"""The served form (gbvdb_server_*): jobs run concurrently by worker threads give
+the same results as the same jobs run alone through the plain per-call API,
+resident grids follow the plain path's full / incremental rebuild sequence, and
+memory admission serialises jobs when the cap leaves room for one."""
+import numpy as np
+import pytest
+
+import datasets
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs():
+    rng = np.random.default_rng(40)
+    out = []
+    for k in range(14):
+        n = int(np.exp(rng.uniform(np.log(1e4), np.log(3e5))))
+        if k % 2 == 0:
+            pts = datasets.shell(n, seed=400 + k, center=(512.0, 512.0, 512.0))
+        else:
+            pts = datasets.sphere_surface(n, seed=400 + k)
+        mode = 1 if k % 5 == 4 else 0
+        dtype = [3, 100, 101][k % 3]
+        out.append(dict(points=pts, mode=mode, dtype=dtype, radius=1.0, gather_radius=1.0 if mode == 0 else 1.5,
+                        boundval=0.0 if mode == 0 else 3.0))
+    return out
+
+
+def _plain(gbvdb, j, grid=None):
+    import torch
+
+    g = grid or gbvdb.Grid(0, (3, 3, 3, 4))
+    if grid is None:
+        g.add_channel(0, j["dtype"])
+    p = torch.from_numpy(j["points"]).cuda()
+    n = g.set_points(p)
+    g.rebuild_topology(n, j["radius"])
+    g.update_atlas()
+    _, ln = g.insert_points_subcell(4, n, j["radius"])
+    if j["mode"] == 0:
+        g.gather_density(4, n, j["gather_radius"], (0, 0, 0), ln)
+    else:
+        g.gather_levelset(4, n, j["gather_radius"], (0, 0, 0), ln)
+    g.update_apron(0, j["boundval"])
+    torch.cuda.synchronize()
+    return g, {"checksum": g.checksum(0), "sc_len": int(ln), "bricks": g.stats()["bricks"]}
+
+
+def _submit(srv, j, resident_id=-1):
+    return srv.submit(j["points"], radius=j["radius"], gather_radius=j["gather_radius"], mode=j["mode"],
+                      dtype=j["dtype"], boundval=j["boundval"], resident_id=resident_id)
+
+
+def test_served_results_match_alone(gpu_lib):
+    import gbvdb
+
+    jobs = _jobs()
+    alone = []
+    for j in jobs:
+        g, r = _plain(gbvdb, j)
+        g.close()
+        alone.append(r)
+    srv = gbvdb.Server(0, workers=6, mem_cap_bytes=64 << 30)
+    try:
+        tickets = [_submit(srv, j) for j in jobs]
+        mixed = [srv.wait(t) for t in tickets]
+    finally:
+        srv.close()
+    for a, m in zip(alone, mixed):
+        assert m["status"] == gbvdb.OK
+        assert m["sc_len"] == a["sc_len"]
+        assert m["bricks"] == a["bricks"]
+        assert m["checksum"] == a["checksum"]  # bit-exact: deterministic FP64 sum of identical atlases
+    # the jobs overlapped: some job started before an earlier one ended
+    starts = sorted((m["t_start_ms"], m["t_end_ms"]) for m in mixed)
+    assert any(starts[i + 1][0] < starts[i][1] for i in range(len(starts) - 1))
+
+
+def test_served_resident_grid_updates(gpu_lib):
+    import gbvdb
+
+    base = datasets.shell(120000, seed=77, center=(512.0, 512.0, 512.0))
+    rng = np.random.default_rng(78)
+    frames = [base]
+    for _ in range(3):  # 5% of the points moved by N(0, 2)
+        p = frames[-1].copy()
+        idx = rng.choice(p.shape[0], p.shape[0] // 20, replace=False)
+        p[idx] += rng.normal(0.0, 2.0, size=(idx.size, 3)).astype(np.float32)
+        frames.append(p)
+    spec = dict(mode=1, dtype=3, radius=2.0, gather_radius=1.0, boundval=3.0)
+    # plain: one grid through the four frames (full, full, incremental, incremental)
+    g = None
+    plain = []
+    for f in frames:
+        g, r = _plain(gbvdb, dict(spec, points=f), grid=g) if g else _plain(gbvdb, dict(spec, points=f))
+        plain.append(r)
+    nodes_plain = [g.nodes(l) for l in range(4)]
+    srv = gbvdb.Server(0, workers=4)
+    try:
+        # interleave fresh jobs so that the resident jobs meet other work
+        t = []
+        for k, f in enumerate(frames):
+            t.append(_submit(srv, dict(spec, points=f), resident_id=3))
+            t.append(_submit(srv, dict(spec, points=datasets.shell(30000, seed=90 + k, center=(512.0, 512.0, 512.0)))))
+        res = [srv.wait(x) for x in t]
+        served = res[0::2]
+        rg = srv.resident(3)
+        nodes_served = [rg.nodes(l) for l in range(4)]
+        assert srv.stats()["resident"] == 1
+        srv.release(3)
+        assert srv.stats()["resident"] == 0
+    finally:
+        srv.close()
+    for p, s in zip(plain, served):
+        assert s["status"] == gbvdb.OK
+        assert (s["sc_len"], s["bricks"], s["checksum"]) == (p["sc_len"], p["bricks"], p["checksum"])
+    # resident jobs ran in submission order
+    assert all(served[i]["t_start_ms"] >= served[i - 1]["t_end_ms"] for i in range(1, len(served)))
+    for a, b in zip(nodes_plain, nodes_served):
+        assert a.shape == b.shape and a.tobytes() == b.tobytes()
+
+
+def test_served_memory_admission(gpu_lib):
+    import gbvdb
+
+    jobs = _jobs()[:6]
+    srv = gbvdb.Server(0, workers=4, mem_cap_bytes=1)  # room for one job at a time
+    try:
+        res = [srv.wait(t) for t in [_submit(srv, j) for j in jobs]]
+    finally:
+        srv.close()
+    assert all(r["status"] == gbvdb.OK for r in res)
+    spans = sorted((r["t_start_ms"], r["t_end_ms"]) for r in res)
+    assert all(spans[i + 1][0] >= spans[i][1] for i in range(len(spans) - 1))
