@@ -363,6 +363,75 @@ def bench_served(args):
     return out
 
 
+def bench_surface(args, steps=5):
+    """Surface-fusion workload (16,777,216 points, seed 2, grid (4,4,3,4), density rho = r = R
+    = 1.5): full-rebuild frames per storage type (FP32 accumulation in all three)."""
+    import datasets
+    import torch
+
+    import gbvdb
+
+    pts = datasets.surface(16_777_216, seed=2)
+    d = torch.from_numpy(pts).cuda()
+    stream = torch.cuda.current_stream()
+    out = {"points": int(pts.shape[0]), "valid_points": int(np.all(pts >= 0, axis=1).sum()),
+           "frame": "RequestFullRebuild + RebuildTopology(r=1.5) + UpdateAtlas + InsertPointsSubcell(4, R=1.5) + "
+                    "GatherDensity(rho=1.5) + UpdateApron(0, 0.0)", "dtypes": {}}
+    for name, dt in (("f32", gbvdb.T_FLOAT), ("f16", gbvdb.T_HALF), ("bf16", gbvdb.T_BFLOAT16)):
+        g = gbvdb.Grid(0, (4, 4, 3, 4), stream=stream)
+        g.set_channel_default(64, 64, 1)
+        g.add_channel(0, dt)
+        n = g.set_points(d)
+
+        def frame():
+            g.request_full_rebuild(True)
+            g.rebuild_topology(n, 1.5)
+            g.update_atlas()
+            _, ln = g.insert_points_subcell(4, n, 1.5)
+            g.gather_density(4, n, 1.5, (0, 0, 0), ln)
+            g.update_apron(0, 0.0)
+
+        for _ in range(3):
+            frame()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            frame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        st = g.stats()
+        info = g.atlas_info(0)
+        out["dtypes"][name] = {"ms_per_frame": ms, "points_per_s": pts.shape[0] / (ms / 1000.0),
+                               "linked_bricks": st["bricks"], "subcell_list_len": st["sc_len"],
+                               "atlas_slots": info["used"] if isinstance(info, dict) else None}
+        g.close()
+    del d
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_batched(args):
+    """Batched uneven grids: `count` clouds (seed 3, sizes log-uniform in [1e4, 2e6], shell or
+    sphere-surface generator, grid (3,3,3,4), density rho = r = R = 1, FP32) submitted at once
+    to the server vs one by one on one worker."""
+    import datasets
+    import torch
+
+    clouds = datasets.batched(count=args.batch_grids, seed=3)
+    host = [torch.from_numpy(c).pin_memory() for c in clouds]
+    reqs = [{"kind": 0, "points": h, "resident_id": -1, "dtype": 3} for h in host]
+    cap = 120 << 30
+    serve_run(reqs[: min(8, len(reqs))], None, args.serve_workers, 0, cap)  # warm-up
+    srv = serve_run(reqs, None, args.serve_workers, 0, cap)
+    pln = serve_run(reqs, None, 1, 0, cap)
+    same = srv.pop("checksums") == pln.pop("checksums")
+    return {"grids": len(reqs), "points_total": float(sum(int(h.shape[0]) for h in host)),
+            "served": srv, "plain": pln, "same_results": same,
+            "speedup_points_per_s": srv["points_per_s"] / pln["points_per_s"]}
+
+
 def bench_ours(args):
     import torch
 
@@ -509,11 +578,17 @@ def bench_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, vel)
+    if rank == 0 and world == 1 and not args.no_surface:
+        grid.close()
+        frames.clear()
+        torch.cuda.empty_cache()
+        line["surface"] = bench_surface(args)
     if rank == 0 and world == 1 and not args.no_served:
         grid.close()
         frames.clear()
         torch.cuda.empty_cache()
         line["served"] = bench_served(args)
+        line["batched"] = bench_batched(args)
     if rank == 0 and world == 1 and args.ref_cuda:
         grid.close()
         frames.clear()
@@ -536,7 +611,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-cuda", action="store_true", help="also time the reference's own CUDA kernels")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form stream")
+    ap.add_argument("--no-surface", action="store_true", help="skip the 16.8M-point surface workload")
     ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--batch-grids", type=int, default=64)
     ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-max-points", type=float, default=4e6)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 500.0, 2000.0])

@@ -195,3 +195,31 @@ def test_insert_before_topology_is_noop(gpu_lib):
     n = g.set_points(d)
     st, ln = g.insert_points_subcell(4, n, 1.0)
     assert st == gbvdb.NOOP and ln == -1
+
+
+def _surface_crop():
+    """The surface-fusion workload (16,777,216 points, seed 2, grid (4,4,3,4)) cropped to
+    x, y in [1792, 2304) and z < 600: part of the z = 0 plane patch and the spheres there,
+    across the x = y = 2048 level-2 node boundary (depth 3)."""
+    pts = datasets.surface(16_777_216, seed=2)
+    m = (pts[:, 0] >= 1792) & (pts[:, 0] < 2304) & (pts[:, 1] >= 1792) & (pts[:, 1] < 2304) & (pts[:, 2] < 600)
+    return np.ascontiguousarray(pts[m])
+
+
+@pytest.mark.parametrize("dtype,rtol,atol", [("f32", 1e-5, 1e-6), ("half", 1e-3, 1e-3), ("bf16", 8e-3, 8e-3)])
+def test_surface_config_storage_types(gpu_lib, dtype, rtol, atol):
+    """Density (rho = r = R = 1.5) of the surface workload stored as FP32, FP16 and BF16
+    (FP32 accumulation in all three) against the FP64 oracle: topology and subcells
+    exact, values within the storage type's tolerance (max errors printed)."""
+    import gbvdb
+
+    dt = {"f32": gbvdb.T_FLOAT, "half": gbvdb.T_HALF, "bf16": gbvdb.T_BFLOAT16}[dtype]
+    pts = _surface_crop()
+    assert pts.shape[0] > 100_000
+    _, o = H.run_oracle(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5)
+    _, g = H.run_gpu(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5, dtype=dt)
+    assert o[0]["depth"] == 3
+    H.compare_topology(o[0], g[0])
+    H.compare_subcells(o[0], g[0])
+    err = H.compare_values(o[0], g[0], rtol, atol, dtype=dt)
+    print("surface crop %s: %d points, max abs error vs FP64 %.3g" % (dtype, pts.shape[0], err))

@@ -132,3 +132,25 @@ def test_served_memory_admission(gpu_lib):
     assert all(r["status"] == gbvdb.OK for r in res)
     spans = sorted((r["t_start_ms"], r["t_end_ms"]) for r in res)
     assert all(spans[i + 1][0] >= spans[i][1] for i in range(len(spans) - 1))
+
+
+def test_batched_grids_config(gpu_lib):
+    """Batched uneven grids (the shell / sphere-surface generator mix, density rho = r = R
+    = 1, FP32): all grids submitted at once give the same results as one by one."""
+    import gbvdb
+
+    clouds = datasets.batched(count=24, seed=3, lo=1e4, hi=3e5)
+    jobs = [dict(points=c, mode=0, dtype=3, radius=1.0, gather_radius=1.0, boundval=0.0) for c in clouds]
+    alone = []
+    for j in jobs:
+        g, r = _plain(gbvdb, j)
+        g.close()
+        alone.append(r)
+    srv = gbvdb.Server(0, workers=16)
+    try:
+        res = [srv.wait(t) for t in [_submit(srv, j) for j in jobs]]
+    finally:
+        srv.close()
+    for a, m in zip(alone, res):
+        assert m["status"] == gbvdb.OK
+        assert (m["sc_len"], m["bricks"], m["checksum"]) == (a["sc_len"], a["bricks"], a["checksum"])
