@@ -280,6 +280,43 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int used, do
     }
 }
 
+// One brick layer of the atlas in the reference's atlas layout (a 3D volume of
+// ax*18 x ay*18 x az*18 voxels, x fastest, padded 18^3 bricks at getAtlasPos):
+// slab[zz][y][x] for zz in [0, 18), the layer of slots bz*ax*ay .. +ax*ay.  Slots
+// at or beyond `valid` are written as zero.
+template <typename T>
+__global__ void k_slab_pack(const T* __restrict__ interior, const T* __restrict__ apron, int ax, int ay, int bz,
+                            long long valid, T* __restrict__ slab) {
+    const long long W = (long long)ax * 18, H = (long long)ay * 18, n = W * H * 18;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)((i / W) % H), zz = (int)(i / (W * H));
+        const int bx = x / 18, by = y / 18, px = x - 18 * bx, py = y - 18 * by;
+        const long long slot = ((long long)bz * ay + by) * ax + bx;
+        T v = T(0.0f);
+        if (slot < valid) {
+            const bool in = px >= 1 && px <= 16 && py >= 1 && py <= 16 && zz >= 1 && zz <= 16;
+            v = in ? interior[slot * 4096 + ((zz - 1) << 8) + ((py - 1) << 4) + (px - 1)]
+                   : apron[slot * kApronStride + apron_index(px, py, zz)];
+        }
+        slab[i] = v;
+    }
+}
+template <typename T>
+__global__ void k_slab_unpack(const T* __restrict__ slab, int ax, int ay, int bz, T* __restrict__ interior,
+                              T* __restrict__ apron) {
+    const long long W = (long long)ax * 18, H = (long long)ay * 18, n = W * H * 18;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)((i / W) % H), zz = (int)(i / (W * H));
+        const int bx = x / 18, by = y / 18, px = x - 18 * bx, py = y - 18 * by;
+        const long long slot = ((long long)bz * ay + by) * ax + bx;
+        const bool in = px >= 1 && px <= 16 && py >= 1 && py <= 16 && zz >= 1 && zz <= 16;
+        if (in)
+            interior[slot * 4096 + ((zz - 1) << 8) + ((py - 1) << 4) + (px - 1)] = slab[i];
+        else
+            apron[slot * kApronStride + apron_index(px, py, zz)] = slab[i];
+    }
+}
+
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 inline unsigned gs_blocks(long long n, int t) {
     long long b = (n + t - 1) / t;
@@ -347,6 +384,26 @@ void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const voi
             k_slot_sums<__nv_bfloat16><<<blocks, 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
     }
     k_sum_partials<<<1, 1024, 0, s>>>(partials, used, out);
+}
+void launch_slab_pack(const void* interior, const void* apron, int esize, int ax, int ay, int bz, long long valid,
+                      void* slab, cudaStream_t s) {
+    long long n = (long long)ax * 18 * ay * 18 * 18;
+    if (esize == 4)
+        k_slab_pack<float><<<gs_blocks(n, 256), 256, 0, s>>>((const float*)interior, (const float*)apron, ax, ay, bz,
+                                                             valid, (float*)slab);
+    else
+        k_slab_pack<__half><<<gs_blocks(n, 256), 256, 0, s>>>((const __half*)interior, (const __half*)apron, ax, ay,
+                                                              bz, valid, (__half*)slab);
+}
+void launch_slab_unpack(const void* slab, int esize, int ax, int ay, int bz, void* interior, void* apron,
+                        cudaStream_t s) {
+    long long n = (long long)ax * 18 * ay * 18 * 18;
+    if (esize == 4)
+        k_slab_unpack<float><<<gs_blocks(n, 256), 256, 0, s>>>((const float*)slab, ax, ay, bz, (float*)interior,
+                                                               (float*)apron);
+    else
+        k_slab_unpack<__half><<<gs_blocks(n, 256), 256, 0, s>>>((const __half*)slab, ax, ay, bz, (__half*)interior,
+                                                                (__half*)apron);
 }
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value, cudaStream_t s) {
     if (used <= 0) return;

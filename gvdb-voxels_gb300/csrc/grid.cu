@@ -815,6 +815,306 @@ struct gbvdb_grid_s {
         stage_end();
         return GBVDB_OK;
     }
+
+    // ------------------------------------------------------- configuration
+    gbvdb_status configure(int nlev, const int* ld) {  // Configure (VG.cpp:2380-2434)
+        if (nlev < 2 || nlev > kMaxLev || !ld) return GBVDB_INVALID_ARG;
+        int d[kMaxLev];
+        long long rg = 1;
+        int lg = 0;
+        for (int l = 0; l < nlev; l++) {
+            d[l] = ld[l] == 0 ? 1 : ld[l];  // VG.cpp:2394
+            if (d[l] < 1 || d[l] > 6) return GBVDB_INVALID_ARG;
+            lg += d[l];
+            if (lg > 30) return GBVDB_NOT_SUPPORTED;
+        }
+        lg = 0;
+        for (int l = 0; l < nlev; l++) {
+            lg += d[l];
+            log2dim[l] = d[l];
+            res[l] = 1 << d[l];
+            rg <<= d[l];
+            range[l] = rg;
+            lgrange[l] = lg;
+        }
+        for (int l = nlev; l < kMaxLev; l++) { log2dim[l] = 0; res[l] = 1; range[l] = rg; lgrange[l] = lg; }
+        levs = nlev;
+        configured = true;
+        clear_topology();  // Configure ends with Clear (VG.cpp:2431)
+        return GBVDB_OK;
+    }
+
+    gbvdb_status add_channel(int chan, int dtype, int apron, int cax, int cay, int caz) {  // VG.cpp:2437-2453
+        if (!configured) return GBVDB_INVALID_ARG;
+        if (chan < 0 || chan >= 8) return GBVDB_INVALID_ARG;
+        if (apron != 1) return GBVDB_NOT_SUPPORTED;  // the reference's apron kernels assume 1 (VG.cpp:4448)
+        if (log2dim[0] != 4) return GBVDB_NOT_SUPPORTED;
+        int es;
+        if (dtype == GBVDB_T_FLOAT) es = 4;
+        else if (dtype == GBVDB_T_HALF || dtype == GBVDB_T_BFLOAT16) es = 2;
+        else return GBVDB_NOT_SUPPORTED;
+        if (cax == 0 && cay == 0 && caz == 0) {  // VG.cpp:2441-2444
+            if (chan == 0) { cax = def_ax; cay = def_ay; caz = def_az; }
+            else { cax = ax; cay = ay; caz = az; }
+        }
+        if (cax <= 0 || cay <= 0 || caz <= 0) return GBVDB_INVALID_ARG;
+        if (chan == 0) { ax = cax; ay = cay; az = caz; }
+        else if (cax != ax || cay != ay) return GBVDB_NOT_SUPPORTED;  // all channels share the slot layout
+        Channel& C = ch[chan];
+        C.used = true;
+        C.dtype = dtype;
+        C.apron = apron;
+        C.esize = es;
+        long long slots = (long long)ax * ay * az;
+        // a channel added again keeps its storage when it is large enough
+        grow(C.interior, (size_t)slots * 4096 * es);
+        grow(C.apron_buf, (size_t)slots * kApronStride * es);
+        check(cudaMemsetAsync(C.interior.p, 0, (size_t)slots * 4096 * es, stream), "channel clear");
+        check(cudaMemsetAsync(C.apron_buf.p, 0, (size_t)slots * kApronStride * es, stream), "channel clear");
+        C.cap_slots = slots;
+        return GBVDB_OK;
+    }
+
+    // ------------------------------------------------------------------ VBX
+    // SaveVBX / LoadVBX (VG.cpp:1626-1767, 507-683; format GVDB_FILESPEC.txt:12-122),
+    // version 1.11: header with the grid transform (identity: this path has none), one
+    // grid, topology pools (64-byte nodes, res^3 u64 child lists; level 0 has none),
+    // then each channel as the reference's atlas volume (ax*18 x ay*18 x az*18 voxels,
+    // x fastest) written one 18-slice brick layer at a time.
+    struct File {
+        FILE* f = nullptr;
+        ~File() {
+            if (f) fclose(f);
+        }
+    };
+    static void wr(FILE* f, const void* p, size_t n) {
+        if (n && fwrite(p, 1, n, f) != n) throw StatusError{GBVDB_INVALID_ARG, "VBX write failed"};
+    }
+    static void rd(FILE* f, void* p, size_t n) {
+        if (n && fread(p, 1, n, f) != n) throw StatusError{GBVDB_INVALID_ARG, "VBX file truncated"};
+    }
+    template <typename T>
+    static void wv(FILE* f, const T& v) { wr(f, &v, sizeof(T)); }
+    template <typename T>
+    static T rv(FILE* f) {
+        T v;
+        rd(f, &v, sizeof(T));
+        return v;
+    }
+
+    int num_channels() const {  // channels 0..k-1 must be in use (the reference's atlas list)
+        int k = 0;
+        while (k < 8 && ch[k].used) k++;
+        return k;
+    }
+
+    gbvdb_status save_vbx(const char* path) {
+        if (!configured || !path) return GBVDB_INVALID_ARG;
+        const int nch = num_channels();
+        if (nch == 0) throw StatusError{GBVDB_INVALID_ARG, "SaveVBX needs channel 0"};
+        for (int c = nch; c < 8; c++)
+            if (ch[c].used) throw StatusError{GBVDB_NOT_SUPPORTED, "SaveVBX needs channels 0..k-1 without gaps"};
+        sync();
+        File F;
+        F.f = fopen(path, "wb");
+        if (!F.f) throw StatusError{GBVDB_INVALID_ARG, std::string("cannot open ") + path};
+        FILE* f = F.f;
+        const uint8_t major = 1, minor = 11;
+        wv(f, major);
+        wv(f, minor);
+        const float pretrans[3] = {0, 0, 0}, angs[3] = {0, 0, 0}, scal[3] = {1, 1, 1}, trans[3] = {0, 0, 0};
+        wr(f, pretrans, 12);
+        wr(f, angs, 12);
+        wr(f, scal, 12);
+        wr(f, trans, 12);
+        const int num_grids = 1;
+        wv(f, num_grids);
+        const long table = ftell(f);
+        uint64_t goff = 0;
+        wv(f, goff);
+        goff = (uint64_t)ftell(f);
+        char name[256];
+        memset(name, 0, sizeof(name));
+        wr(f, name, 256);
+        wv(f, (uint8_t)'f');  // data type: float (FP16 / BF16 channels carry their own channel type below)
+        wv(f, (uint8_t)1);    // components
+        wv(f, (uint8_t)0);    // compression
+        const float vs[3] = {1, 1, 1};
+        wr(f, vs, 12);
+        wv(f, (int32_t)ncnt[0]);  // brick count = level-0 pool total
+        const int32_t leafdim[3] = {res[0], res[0], res[0]};
+        wr(f, leafdim, 12);
+        wv(f, (int32_t)1);  // apron
+        wv(f, (int32_t)nch);
+        const int32_t axisres[3] = {ax * 18, ay * 18, az * 18};
+        wv(f, (uint64_t)ch[0].esize * (uint64_t)axisres[0] * (uint64_t)axisres[1] * (uint64_t)axisres[2]);
+        wv(f, (uint8_t)2);  // topology: gvdb
+        wv(f, (int32_t)0);  // reuse
+        wv(f, (uint8_t)0);  // atlas layout
+        const int32_t axiscnt[3] = {ax, ay, az};
+        wr(f, axiscnt, 12);
+        wr(f, axisres, 12);
+        wv(f, (int32_t)levs);
+        wv(f, (uint64_t)(root_lev >= 0 ? elem(0, root_lev, 0) : kUndefL));
+        for (int l = 0; l < levs; l++) {
+            wv(f, (int32_t)log2dim[l]);
+            wv(f, (int32_t)res[l]);
+            const int32_t rg[3] = {(int32_t)range[l], (int32_t)range[l], (int32_t)range[l]};
+            wr(f, rg, 12);
+            wv(f, (int32_t)ncnt[l]);
+            wv(f, (int32_t)sizeof(Node));
+            wv(f, (int32_t)(l >= 1 ? ncnt[l] : 0));
+            wv(f, (int32_t)(l >= 1 ? cl_len(l) * 8 : 0));
+        }
+        std::vector<unsigned char> host;
+        for (int l = 0; l < levs; l++) {  // pool 0
+            size_t bytes = (size_t)ncnt[l] * sizeof(Node);
+            host.resize(bytes);
+            if (bytes) check(cudaMemcpy(host.data(), nodes[l].p, bytes, cudaMemcpyDeviceToHost), "VBX nodes");
+            wr(f, host.data(), bytes);
+        }
+        for (int l = 1; l < levs; l++) {  // pool 1
+            size_t bytes = (size_t)(ncnt[l] * cl_len(l)) * 8;
+            host.resize(bytes);
+            if (bytes) check(cudaMemcpy(host.data(), clist[l].p, bytes, cudaMemcpyDeviceToHost), "VBX child lists");
+            wr(f, host.data(), bytes);
+        }
+        const size_t slab_elems = (size_t)axisres[0] * axisres[1] * 18;
+        for (int c = 0; c < nch; c++) {
+            const Channel& C = ch[c];
+            wv(f, (int32_t)C.dtype);
+            wv(f, (int32_t)C.esize);
+            grow(xfer, slab_elems * C.esize);
+            host.resize(slab_elems * C.esize);
+            // slots past the assigned ones are written as zero (the reference writes whatever its
+            // atlas texture holds there)
+            const long long valid = std::min<long long>(std::min<long long>(C.cap_slots, atlas_last),
+                                                        (long long)ax * ay * az);
+            for (int bz = 0; bz < az; bz++) {
+                launch_slab_pack(C.interior.p, C.apron_buf.p, C.esize, ax, ay, bz, valid, xfer.p, stream);
+                check_launch("VBX slab");
+                check(cudaMemcpyAsync(host.data(), xfer.p, host.size(), cudaMemcpyDeviceToHost, stream), "VBX atlas");
+                sync();
+                wr(f, host.data(), host.size());
+            }
+        }
+        if (fseek(f, table, SEEK_SET) != 0) throw StatusError{GBVDB_INVALID_ARG, "VBX seek failed"};
+        wv(f, goff);
+        return GBVDB_OK;
+    }
+
+    gbvdb_status load_vbx(const char* path) {
+        if (!path) return GBVDB_INVALID_ARG;
+        File F;
+        F.f = fopen(path, "rb");
+        if (!F.f) throw StatusError{GBVDB_INVALID_ARG, std::string("cannot open ") + path};
+        FILE* f = F.f;
+        const uint8_t major = rv<uint8_t>(f), minor = rv<uint8_t>(f);
+        if ((major == 1 && minor >= 11) || major > 1) {
+            float tf[12];
+            rd(f, tf, sizeof(tf));  // grid transform: kept by the renderer, not by this path
+        }
+        const int32_t num_grids = rv<int32_t>(f);
+        uint8_t masks = (major == 1 && minor == 0) ? 1 : 0;
+        if (major >= 2) masks = rv<uint8_t>(f);
+        if (masks) throw StatusError{GBVDB_NOT_SUPPORTED, "VBX with node bitmasks"};
+        if (num_grids < 1) throw StatusError{GBVDB_INVALID_ARG, "VBX without grids"};
+        std::vector<uint64_t> offs((size_t)num_grids);
+        rd(f, offs.data(), offs.size() * 8);
+        if (fseek(f, (long)offs[0], SEEK_SET) != 0) throw StatusError{GBVDB_INVALID_ARG, "VBX seek failed"};
+        char name[256];
+        rd(f, name, 256);
+        const uint8_t dt = rv<uint8_t>(f), comps = rv<uint8_t>(f), comp = rv<uint8_t>(f);
+        float vs[3];
+        rd(f, vs, 12);
+        rv<int32_t>(f);  // brick count (= level-0 pool count, read again below)
+        int32_t leafdim[3];
+        rd(f, leafdim, 12);
+        const int32_t apron = rv<int32_t>(f), nch = rv<int32_t>(f);
+        rv<uint64_t>(f);  // atlas size
+        const uint8_t topo = rv<uint8_t>(f);
+        rv<int32_t>(f);  // topology reuse
+        const uint8_t layout = rv<uint8_t>(f);
+        int32_t axc[3], axr[3];
+        rd(f, axc, 12);
+        rd(f, axr, 12);
+        if (dt != 'f' || comps != 1 || comp != 0 || topo != 2 || layout != 0 || apron != 1 || leafdim[0] != 16 ||
+            nch < 1 || nch > 8)
+            throw StatusError{GBVDB_NOT_SUPPORTED, "VBX grid: float, 1 component, uncompressed, gvdb topology, atlas "
+                                                   "layout, 16^3 bricks with apron 1 only"};
+        const int32_t nlev = rv<int32_t>(f);
+        const uint64_t root = rv<uint64_t>(f);
+        if (nlev < 2 || nlev > kMaxLev) throw StatusError{GBVDB_NOT_SUPPORTED, "VBX level count"};
+        int32_t ld[kMaxLev], cnt0[kMaxLev], w0[kMaxLev], cnt1[kMaxLev], w1[kMaxLev];
+        for (int l = 0; l < nlev; l++) {
+            ld[l] = rv<int32_t>(f);
+            rv<int32_t>(f);  // res
+            int32_t rg[3];
+            rd(f, rg, 12);
+            cnt0[l] = rv<int32_t>(f);
+            w0[l] = rv<int32_t>(f);
+            cnt1[l] = rv<int32_t>(f);
+            w1[l] = rv<int32_t>(f);
+        }
+        gbvdb_status st = configure(nlev, ld);
+        if (st != GBVDB_OK) return st;
+        for (int l = 0; l < nlev; l++) {
+            if (w0[l] != (int)sizeof(Node) || cnt0[l] < 0)
+                throw StatusError{GBVDB_NOT_SUPPORTED, "VBX node records are not 64 bytes"};
+            if (l == 0 ? (long long)cnt1[0] * w1[0] != 0 : (cnt1[l] != cnt0[l] || w1[l] != cl_len(l) * 8))
+                throw StatusError{GBVDB_NOT_SUPPORTED, "VBX child lists do not match the configuration"};
+        }
+        std::vector<unsigned char> host;
+        root_lev = -1;
+        for (int l = 0; l < nlev; l++) {
+            ensure_pool(l, std::max(cnt0[l], 1));
+            size_t bytes = (size_t)cnt0[l] * sizeof(Node);
+            host.resize(bytes);
+            rd(f, host.data(), bytes);
+            long long flagged = 0;
+            for (int i = 0; i < cnt0[l]; i++) flagged += host[(size_t)i * sizeof(Node) + 1] != 0;
+            if (bytes) check(cudaMemcpy(nodes[l].p, host.data(), bytes, cudaMemcpyHostToDevice), "VBX nodes");
+            ncnt[l] = cnt0[l];
+            nused[l] = flagged;
+            if (root != kUndefL && (int)((root >> 8) & 0xFF) == l && cnt0[l] > 0) {
+                Node r;
+                memcpy(&r, host.data() + (size_t)(root >> 16) * sizeof(Node), sizeof(Node));
+                root_lev = l;
+                for (int a = 0; a < 3; a++) root_pos[a] = r.pos[a];
+            }
+        }
+        for (int l = 1; l < nlev; l++) {
+            size_t bytes = (size_t)cnt1[l] * (size_t)w1[l];
+            host.resize(bytes);
+            rd(f, host.data(), bytes);
+            if (bytes) check(cudaMemcpy(clist[l].p, host.data(), bytes, cudaMemcpyHostToDevice), "VBX child lists");
+        }
+        last_depth = root_lev >= 0 ? root_lev : 0;
+        def_ax = axc[0];
+        def_ay = axc[1];
+        def_az = axc[2];
+        for (int c = 0; c < 8; c++) ch[c].used = false;
+        const size_t slab_elems = (size_t)axr[0] * axr[1] * 18;
+        if (axr[0] != axc[0] * 18 || axr[1] != axc[1] * 18 || axr[2] != axc[2] * 18)
+            throw StatusError{GBVDB_NOT_SUPPORTED, "VBX atlas resolution is not axiscnt * 18"};
+        for (int c = 0; c < nch; c++) {
+            const int32_t ctype = rv<int32_t>(f), cstride = rv<int32_t>(f);
+            st = add_channel(c, ctype, 1, axc[0], axc[1], axc[2]);
+            if (st != GBVDB_OK) return st;
+            Channel& C = ch[c];
+            if (cstride != C.esize) throw StatusError{GBVDB_NOT_SUPPORTED, "VBX channel stride"};
+            grow(xfer, slab_elems * C.esize);
+            host.resize(slab_elems * C.esize);
+            for (int bz = 0; bz < axc[2]; bz++) {
+                rd(f, host.data(), host.size());
+                check(cudaMemcpyAsync(xfer.p, host.data(), host.size(), cudaMemcpyHostToDevice, stream), "VBX atlas");
+                launch_slab_unpack(xfer.p, C.esize, ax, ay, bz, C.interior.p, C.apron_buf.p, stream);
+                check_launch("VBX slab");
+                sync();
+            }
+        }
+        return update_atlas();  // LoadVBX ends with UpdateAtlas (VG.cpp:676)
+    }
 };
 
 // ------------------------------------------------------------------ C ABI
@@ -906,25 +1206,7 @@ const char* gbvdb_last_error(gbvdb_grid g) { return g ? g->err.c_str() : "null g
 
 gbvdb_status gbvdb_configure(gbvdb_grid g, int levs, const int* log2dim) {
     GBVDB_GUARD(g)
-    if (levs < 2 || levs > kMaxLev || !log2dim) return GBVDB_INVALID_ARG;
-    long long rg = 1;
-    int lg = 0;
-    for (int l = 0; l < levs; l++) {
-        int d = log2dim[l] == 0 ? 1 : log2dim[l];  // VG.cpp:2394
-        if (d < 1 || d > 6) return GBVDB_INVALID_ARG;
-        lg += d;
-        if (lg > 30) return GBVDB_NOT_SUPPORTED;
-        g->log2dim[l] = d;
-        g->res[l] = 1 << d;
-        rg <<= d;
-        g->range[l] = rg;
-        g->lgrange[l] = lg;
-    }
-    for (int l = levs; l < kMaxLev; l++) { g->log2dim[l] = 0; g->res[l] = 1; g->range[l] = rg; g->lgrange[l] = lg; }
-    g->levs = levs;
-    g->configured = true;
-    g->clear_topology();  // Configure ends with Clear (VG.cpp:2431)
-    return GBVDB_OK;
+    return g->configure(levs, log2dim);
     GBVDB_END(g)
 }
 
@@ -945,34 +1227,19 @@ gbvdb_status gbvdb_set_channel_default(gbvdb_grid g, int ax, int ay, int az) {
 
 gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron, int ax, int ay, int az) {
     GBVDB_GUARD(g)
-    if (!g->configured) return GBVDB_INVALID_ARG;
-    if (chan < 0 || chan >= 8) return GBVDB_INVALID_ARG;
-    if (apron != 1) return GBVDB_NOT_SUPPORTED;  // the reference's apron kernels assume 1 (VG.cpp:4448)
-    if (g->log2dim[0] != 4) return GBVDB_NOT_SUPPORTED;
-    int es;
-    if (dtype == GBVDB_T_FLOAT) es = 4;
-    else if (dtype == GBVDB_T_HALF || dtype == GBVDB_T_BFLOAT16) es = 2;
-    else return GBVDB_NOT_SUPPORTED;
-    if (ax == 0 && ay == 0 && az == 0) {  // VG.cpp:2441-2444
-        if (chan == 0) { ax = g->def_ax; ay = g->def_ay; az = g->def_az; }
-        else { ax = g->ax; ay = g->ay; az = g->az; }
-    }
-    if (ax <= 0 || ay <= 0 || az <= 0) return GBVDB_INVALID_ARG;
-    if (chan == 0) { g->ax = ax; g->ay = ay; g->az = az; }
-    else if (ax != g->ax || ay != g->ay) return GBVDB_NOT_SUPPORTED;  // all channels share the slot layout
-    Channel& C = g->ch[chan];
-    C.used = true;
-    C.dtype = dtype;
-    C.apron = apron;
-    C.esize = es;
-    long long slots = (long long)g->ax * g->ay * g->az;
-    // a channel added again keeps its storage when it is large enough
-    g->grow(C.interior, (size_t)slots * 4096 * es);
-    g->grow(C.apron_buf, (size_t)slots * kApronStride * es);
-    g->check(cudaMemsetAsync(C.interior.p, 0, (size_t)slots * 4096 * es, g->stream), "channel clear");
-    g->check(cudaMemsetAsync(C.apron_buf.p, 0, (size_t)slots * kApronStride * es, g->stream), "channel clear");
-    C.cap_slots = slots;
-    return GBVDB_OK;
+    return g->add_channel(chan, dtype, apron, ax, ay, az);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_save_vbx(gbvdb_grid g, const char* path) {
+    GBVDB_GUARD(g)
+    return g->save_vbx(path);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_load_vbx(gbvdb_grid g, const char* path) {
+    GBVDB_GUARD(g)
+    return g->load_vbx(path);
     GBVDB_END(g)
 }
 

@@ -65,6 +65,11 @@ void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, 
                   const void* interior, void* apron, uint32_t boundbits, cudaStream_t s);
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out,
                           cudaStream_t s);
+// one brick layer (18 voxel slices) of the reference's atlas layout <-> interior + apron records
+void launch_slab_pack(const void* interior, const void* apron, int esize, int ax, int ay, int bz, long long valid,
+                      void* slab, cudaStream_t s);
+void launch_slab_unpack(const void* slab, int esize, int ax, int ay, int bz, void* interior, void* apron,
+                        cudaStream_t s);
 // deterministic FP64 channel sum: per-slot partials, then one fixed-order block
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s);

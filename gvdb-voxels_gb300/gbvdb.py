@@ -36,7 +36,7 @@ EXPORTS = [
     "gbvdb_get_node_counts", "gbvdb_get_point_bounds", "gbvdb_export_nodes", "gbvdb_export_childlist",
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
-    "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning",
+    "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -116,6 +116,8 @@ def load(path=LIB_PATH):
     L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
+    L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
+    L.gbvdb_load_vbx.argtypes = [vp, ctypes.c_char_p]
     L.gbvdb_server_create.argtypes = [i32, i32, i64, ctypes.POINTER(vp)]
     L.gbvdb_server_submit.argtypes = [vp, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_server_wait.argtypes = [vp, i64, ctypes.POINTER(JobResult)]
@@ -321,6 +323,14 @@ class Grid:
             self._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nsub + 1,
             pts.ctypes.data if total_len > 0 else None, total_len), "export_subcells")
         return off, pts
+
+    def save_vbx(self, path):
+        """SaveVBX (gvdb_volume_gvdb.cpp:1626-1767)."""
+        self._check(self.L.gbvdb_save_vbx(self._h, os.fsencode(path)), "save_vbx")
+
+    def load_vbx(self, path):
+        """LoadVBX (gvdb_volume_gvdb.cpp:507-683): replaces configuration, pools and channels."""
+        self._check(self.L.gbvdb_load_vbx(self._h, os.fsencode(path)), "load_vbx")
 
     def checksum(self, chan=0):
         out = ctypes.c_double()

@@ -137,6 +137,13 @@ GBVDB_API gbvdb_status gbvdb_export_atlas_map(gbvdb_grid g, void* host_out, int6
  * is unspecified, as in the reference (PT.cuh:266 uses atomicAdd slots) */
 GBVDB_API gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int64_t cap_offsets,
                                              float* points, int64_t cap_points);
+/* SaveVBX / LoadVBX (gvdb_volume_gvdb.cpp:1626-1767, 507-683; GVDB_FILESPEC.txt): version
+ * 1.11, one grid, identity transform, GVDB topology pools and every channel 0..k-1 in the
+ * atlas layout (FP16 / BF16 channels carry their extension type codes 100 / 101).  Loading
+ * accepts 1.x / 2.x files without node bitmasks, float grids, uncompressed, atlas layout,
+ * 16^3 bricks with apron 1, and ends with UpdateAtlas as the reference does. */
+GBVDB_API gbvdb_status gbvdb_save_vbx(gbvdb_grid g, const char* path);
+GBVDB_API gbvdb_status gbvdb_load_vbx(gbvdb_grid g, const char* path);
 /* FP64 sum of the interior voxels of all assigned slots (total-mass check) */
 GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
 /* Allocation-free variant of gbvdb_checksum (no counterpart in the reference).

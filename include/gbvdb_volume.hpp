@@ -131,6 +131,10 @@ class VolumeGVDB {
     }
     void FillChannel(uchar chan, float value) { chk(gbvdb_fill_channel(g_, chan, value), "FillChannel"); }
 
+    // SaveVBX / LoadVBX (VG.cpp:1626-1767, 507-683)
+    void SaveVBX(const char* fname) { chk(gbvdb_save_vbx(g_, fname), "SaveVBX"); }
+    bool LoadVBX(const char* fname) { return chk(gbvdb_load_vbx(g_, fname), "LoadVBX") == GBVDB_OK; }
+
     // accessors (VG.h:563-564, 637-641)
     uint64 getNumTotalNodes(int lev) {
         int64_t tot[10], used[10];

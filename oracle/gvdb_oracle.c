@@ -894,3 +894,103 @@ double og_checksum(const OGrid* g, int chan) {
     }
     return s;
 }
+
+/* SaveVBX (VG.cpp:1626-1767; format GVDB_FILESPEC.txt:12-122), version 1.11, one grid:
+ * header (version, identity transform, grid count, grid offset table), grid header,
+ * topology (levels, root id, per-level log2 dim / res / range / pool counts and widths),
+ * pool 0 of every level, pool 1 of every level (level 0 has none), then each channel as
+ * the atlas volume (ax*18 x ay*18 x az*18 voxels, x fastest) in FP32.  Slots past the
+ * assigned ones are written as zero.  Returns 0 on success. */
+int og_save_vbx(const OGrid* g, const char* path) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return -1;
+    int nch = 0;
+    while (nch < OG_MAXCHAN && g->chan[nch].used) nch++;
+    const uint8_t major = 1, minor = 11;
+    fwrite(&major, 1, 1, f);
+    fwrite(&minor, 1, 1, f);
+    const float pretrans[3] = {0, 0, 0}, angs[3] = {0, 0, 0}, scal[3] = {1, 1, 1}, trans[3] = {0, 0, 0};
+    fwrite(pretrans, 4, 3, f);
+    fwrite(angs, 4, 3, f);
+    fwrite(scal, 4, 3, f);
+    fwrite(trans, 4, 3, f);
+    const int32_t num_grids = 1;
+    fwrite(&num_grids, 4, 1, f);
+    const long table = ftell(f);
+    uint64_t goff = 0;
+    fwrite(&goff, 8, 1, f);
+    goff = (uint64_t)ftell(f);
+    char name[256];
+    memset(name, 0, sizeof(name));
+    fwrite(name, 1, 256, f);
+    const uint8_t dt = 'f', comps = 1, comp = 0, topo = 2, layout = 0;
+    fwrite(&dt, 1, 1, f);
+    fwrite(&comps, 1, 1, f);
+    fwrite(&comp, 1, 1, f);
+    const float vs[3] = {1, 1, 1};
+    fwrite(vs, 4, 3, f);
+    const int32_t leafcnt = (int32_t)g->ncnt[0];
+    fwrite(&leafcnt, 4, 1, f);
+    const int32_t leafdim[3] = {g->res[0], g->res[0], g->res[0]};
+    fwrite(leafdim, 4, 3, f);
+    const int32_t apron = 1, nch32 = nch;
+    fwrite(&apron, 4, 1, f);
+    fwrite(&nch32, 4, 1, f);
+    const int32_t axisres[3] = {g->ax * 18, g->ay * 18, g->az * 18};
+    const uint64_t atlas_sz = 4ull * (uint64_t)axisres[0] * (uint64_t)axisres[1] * (uint64_t)axisres[2];
+    fwrite(&atlas_sz, 8, 1, f);
+    fwrite(&topo, 1, 1, f);
+    const int32_t reuse = 0;
+    fwrite(&reuse, 4, 1, f);
+    fwrite(&layout, 1, 1, f);
+    const int32_t axiscnt[3] = {g->ax, g->ay, g->az};
+    fwrite(axiscnt, 4, 3, f);
+    fwrite(axisres, 4, 3, f);
+    const int32_t levels = g->levs;
+    fwrite(&levels, 4, 1, f);
+    /* mRoot = PoolAlloc(0, D, ...) at a full rebuild (VG.cpp:1290): Elem(0, D, 0) */
+    const int D = g->last_depth;
+    const uint64_t root = (D >= 0 && D < g->levs && g->ncnt[D] > 0) ? ((uint64_t)D << 8) : 0xFFFFFFFFull;
+    fwrite(&root, 8, 1, f);
+    for (int l = 0; l < g->levs; l++) {
+        const int32_t ld = g->log2dim[l], res = g->res[l];
+        const int32_t rg[3] = {(int32_t)g->range[l], (int32_t)g->range[l], (int32_t)g->range[l]};
+        const int32_t cnt0 = (int32_t)g->ncnt[l], w0 = (int32_t)sizeof(ONode);
+        const int32_t cnt1 = l >= 1 ? (int32_t)g->ncnt[l] : 0, w1 = l >= 1 ? (int32_t)(og_cl_len(g, l) * 8) : 0;
+        fwrite(&ld, 4, 1, f);
+        fwrite(&res, 4, 1, f);
+        fwrite(rg, 4, 3, f);
+        fwrite(&cnt0, 4, 1, f);
+        fwrite(&w0, 4, 1, f);
+        fwrite(&cnt1, 4, 1, f);
+        fwrite(&w1, 4, 1, f);
+    }
+    for (int l = 0; l < g->levs; l++)
+        if (g->ncnt[l]) fwrite(g->nodes[l], sizeof(ONode), g->ncnt[l], f);
+    for (int l = 1; l < g->levs; l++)
+        if (g->ncnt[l]) fwrite(g->clist[l], 8, g->ncnt[l] * og_cl_len(g, l), f);
+    const size_t W = (size_t)axisres[0], H = (size_t)axisres[1];
+    float* slice = (float*)malloc(W * H * sizeof(float));
+    for (int c = 0; c < nch; c++) {
+        const int32_t ctype = 3, cstride = 4;
+        fwrite(&ctype, 4, 1, f);
+        fwrite(&cstride, 4, 1, f);
+        for (int z = 0; z < axisres[2]; z++) {
+            for (size_t y = 0; y < H; y++)
+                for (size_t x = 0; x < W; x++) {
+                    const int bx = (int)(x / 18), by = (int)(y / 18), bz = z / 18;
+                    const int64_t slot = ((int64_t)bz * g->ay + by) * g->ax + bx;
+                    float v = 0.0f;
+                    if (slot < g->atlas_last && g->chan[c].data)
+                        v = (float)g->chan[c].data[(size_t)slot * 5832 +
+                                                   (size_t)(((z % 18) * 18 + (int)(y % 18)) * 18 + (int)(x % 18))];
+                    slice[y * W + x] = v;
+                }
+            fwrite(slice, sizeof(float), W * H, f);
+        }
+    }
+    free(slice);
+    fseek(f, table, SEEK_SET);
+    fwrite(&goff, 8, 1, f);
+    return fclose(f) == 0 ? 0 : -1;
+}

@@ -96,6 +96,8 @@ def lib():
         L.og_subcell_map.argtypes = [vp]
         L.og_checksum.restype = ctypes.c_double
         L.og_checksum.argtypes = [vp, i32]
+        L.og_save_vbx.restype = i32
+        L.og_save_vbx.argtypes = [vp, ctypes.c_char_p]
         _lib = L
     return _lib
 
@@ -241,3 +243,7 @@ class OracleGrid:
 
     def checksum(self, chan=0):
         return float(lib().og_checksum(self._h, chan))
+
+    def save_vbx(self, path):
+        """SaveVBX restated (VG.cpp:1626-1767): FP32 atlas from the FP64 oracle values."""
+        assert lib().og_save_vbx(self._h, os.fsencode(path)) == 0
