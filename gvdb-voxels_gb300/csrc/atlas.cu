@@ -317,6 +317,97 @@ __global__ void k_slab_unpack(const T* __restrict__ slab, int ax, int ay, int bz
     }
 }
 
+// UpdateNeighbors (VG.cpp:2527-2556): per leaf, the leaf at its centre -/+ one brick
+// along x, y, z (order -x, -y, -z, +x, +y, +z), -1 where there is none
+__global__ void k_neighbors(TreeView t, LeafGrid lg, long long n, int d, int* __restrict__ table) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Node nd = t.nodes[0][i];
+    const int dir[6][3] = {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const int px = nd.pos[0] + d / 2 + dir[k][0] * d, py = nd.pos[1] + d / 2 + dir[k][1] * d,
+                  pz = nd.pos[2] + d / 2 + dir[k][2] * d;
+        long long nl = -1;
+        if (px >= 0 && py >= 0 && pz >= 0) nl = lg.cells ? lookup_leaf(lg, t, px, py, pz) : get_leaf_at_voxel(t, px, py, pz);
+        table[i * 6 + k] = (int)nl;
+    }
+}
+
+// UpdateApronFaces (VG.cpp:4461-4496, gvdbUpdateApronFacesF OP.cuh:27-61): one block
+// per assigned slot; for each of its -x, -y, -z neighbours that owns a slot, the
+// slot's first interior plane goes to the neighbour's far apron face and the
+// neighbour's last interior plane to the slot's near face.  Each face record has one
+// writer (the slot on its far side), so no two blocks write the same voxel.
+template <typename T>
+__global__ void k_apron_faces(const Node* __restrict__ leaves, const AtlasNode* __restrict__ amap, int used, int ax,
+                              int ay, const int* __restrict__ table, T* __restrict__ interior, T* __restrict__ apron) {
+    const int s = blockIdx.x;
+    const int L = amap[s].leaf;
+    if (L < 0) return;
+    for (int side = 0; side < 3; side++) {
+        const int nb = table[(size_t)L * 6 + side];
+        if (nb < 0) continue;
+        const int ns = slot_of_value(leaves[nb].value, ax, ay);
+        if (ns < 0 || ns >= used || amap[ns].leaf != nb) continue;
+        const T* si = interior + (size_t)s * 4096;
+        const T* ni = interior + (size_t)ns * 4096;
+        T* sa = apron + (size_t)s * kApronStride + (2 * side) * 256;       // near face of the slot
+        T* na = apron + (size_t)ns * kApronStride + (2 * side + 1) * 256;  // far face of the neighbour
+        for (int e = threadIdx.x; e < 256; e += blockDim.x) {
+            const int hi = e >> 4, lo = e & 15;  // face element order: x faces [z][y], y faces [z][x], z faces [y][x]
+            int first, last;
+            if (side == 0) { first = (hi << 8) + (lo << 4); last = first + 15; }
+            else if (side == 1) { first = (hi << 8) + lo; last = first + (15 << 4); }
+            else { first = (hi << 4) + lo; last = first + (15 << 8); }
+            sa[e] = ni[last];
+            na[e] = si[first];
+        }
+    }
+}
+
+// Compute(FUNC_SMOOTH) one pass (gvdbOpSmooth, OP.cuh:383-400), one block per assigned
+// slot: the padded brick (interior + the six apron faces: the stencil never reads
+// edges or corners) is staged in shared memory, so the slot's interior is rewritten
+// from the values before the pass.  v = p1*c + x-1 + x+1 + y-1 + y+1 + z-1 + z+1 in
+// FP32 (this order, no contraction), then v / (p1 + 6.0) + p2 in double as the
+// source's double literal makes it, rounded to float.
+__global__ void __launch_bounds__(256) k_smooth(const AtlasNode* __restrict__ amap, float* __restrict__ interior,
+                                                const float* __restrict__ apron, float p1, float p2) {
+    __shared__ float sm[18 * 18 * 18];
+    const int s = blockIdx.x;
+    if (amap[s].leaf < 0) return;
+    const float* in = interior + (size_t)s * 4096;
+    const float* ap = apron + (size_t)s * kApronStride;
+    for (int v = threadIdx.x; v < 4096; v += blockDim.x) {
+        const int x = v & 15, y = (v >> 4) & 15, z = v >> 8;
+        sm[((z + 1) * 18 + (y + 1)) * 18 + (x + 1)] = in[v];
+    }
+    for (int k = threadIdx.x; k < 1536; k += blockDim.x) {
+        const int f = k >> 8, hi = (k >> 4) & 15, lo = k & 15, far = f & 1 ? 17 : 0;
+        int x, y, z;
+        if (f < 2) { x = far; y = lo + 1; z = hi + 1; }
+        else if (f < 4) { y = far; x = lo + 1; z = hi + 1; }
+        else { z = far; x = lo + 1; y = hi + 1; }
+        sm[(z * 18 + y) * 18 + x] = ap[k];
+    }
+    __syncthreads();
+    const double den = __dadd_rn((double)p1, 6.0);
+    float* out = interior + (size_t)s * 4096;
+    for (int v = threadIdx.x; v < 4096; v += blockDim.x) {
+        const int x = (v & 15) + 1, y = ((v >> 4) & 15) + 1, z = (v >> 8) + 1;
+        const int i = (z * 18 + y) * 18 + x;
+        float a = __fmul_rn(p1, sm[i]);
+        a = __fadd_rn(a, sm[i - 1]);
+        a = __fadd_rn(a, sm[i + 1]);
+        a = __fadd_rn(a, sm[i - 18]);
+        a = __fadd_rn(a, sm[i + 18]);
+        a = __fadd_rn(a, sm[i - 324]);
+        a = __fadd_rn(a, sm[i + 324]);
+        out[v] = __double2float_rn(__dadd_rn(__ddiv_rn((double)a, den), (double)p2));
+    }
+}
+
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 inline unsigned gs_blocks(long long n, int t) {
     long long b = (n + t - 1) / t;
@@ -404,6 +495,24 @@ void launch_slab_unpack(const void* slab, int esize, int ax, int ay, int bz, voi
     else
         k_slab_unpack<__half><<<gs_blocks(n, 256), 256, 0, s>>>((const __half*)slab, ax, ay, bz, (__half*)interior,
                                                                 (__half*)apron);
+}
+void launch_neighbors(const TreeView& t, const LeafGrid& lg, long long n, int d, int* table, cudaStream_t s) {
+    if (n <= 0) return;
+    k_neighbors<<<blocks_for(n, 128), 128, 0, s>>>(t, lg, n, d, table);
+}
+void launch_apron_faces(const Node* leaves, const AtlasNode* amap, int used, int ax, int ay, const int* table,
+                        int esize, void* interior, void* apron, cudaStream_t s) {
+    if (used <= 0) return;
+    if (esize == 4)
+        k_apron_faces<float><<<used, 128, 0, s>>>(leaves, amap, used, ax, ay, table, (float*)interior, (float*)apron);
+    else
+        k_apron_faces<__half><<<used, 128, 0, s>>>(leaves, amap, used, ax, ay, table, (__half*)interior,
+                                                   (__half*)apron);
+}
+void launch_smooth(const AtlasNode* amap, int used, float* interior, const float* apron, float p1, float p2,
+                   cudaStream_t s) {
+    if (used <= 0) return;
+    k_smooth<<<used, 256, 0, s>>>(amap, interior, apron, p1, p2);
 }
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value, cudaStream_t s) {
     if (used <= 0) return;

@@ -135,6 +135,10 @@ struct gbvdb_grid_s {
     DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     unsigned char* pinned = nullptr;
 
+    // neighbour table of UpdateNeighbors (6 leaf indices per leaf) and the leaf count it covers
+    DevBuf nbr_table;
+    long long nbr_count = -1;
+
     // tuning
     int dense_min = 2048;
 
@@ -220,6 +224,7 @@ struct gbvdb_grid_s {
 
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
+        nbr_count = -1;
         lgdom_init = false;
         lgv.cells = nullptr;
         atlas_last = 0;
@@ -816,6 +821,46 @@ struct gbvdb_grid_s {
         return GBVDB_OK;
     }
 
+    // ------------------------------------------------- apron faces and smoothing
+    gbvdb_status update_neighbors() {  // UpdateNeighbors (VG.cpp:2527-2556)
+        long long n = ncnt[0];
+        grow(nbr_table, (size_t)std::max(n, 1ll) * 6 * 4);
+        TreeView t = view();
+        launch_neighbors(t, lgv, n, (int)range[0], ptr<int>(nbr_table), stream);
+        check_launch("neighbors");
+        nbr_count = n;
+        return GBVDB_OK;
+    }
+
+    gbvdb_status update_apron_faces(int chan) {  // UpdateApronFaces (VG.cpp:4461-4496)
+        if (chan < 0 || chan >= 8 || !ch[chan].used) throw StatusError{GBVDB_INVALID_ARG, "bad channel"};
+        if (nbr_count != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "UpdateNeighbors was not called for this topology"};
+        if (atlas_last == 0) return GBVDB_NOOP;
+        launch_apron_faces(ptr<Node>(nodes[0]), ptr<AtlasNode>(amap), atlas_last, ax, ay, ptr<int>(nbr_table),
+                           ch[chan].esize, ch[chan].interior.p, ch[chan].apron_buf.p, stream);
+        check_launch("apron faces");
+        return GBVDB_OK;
+    }
+
+    // Compute(effect, chan, iterations, params, bUpdateApron, skipOverAprons, boundval)
+    // (VG.cpp:4532-4558) for FUNC_SMOOTH; the pass covers the interior voxels of the
+    // assigned slots whatever skipOverAprons says (the reference's smoothing kernel
+    // indexes interiors only)
+    gbvdb_status compute(int effect, int chan, int iterations, const float* prm, bool upd_apron, float boundval) {
+        if (effect != GBVDB_FUNC_SMOOTH) throw StatusError{GBVDB_NOT_SUPPORTED, "Compute: FUNC_SMOOTH only"};
+        if (chan < 0 || chan >= 8 || !ch[chan].used || !prm || iterations < 0)
+            throw StatusError{GBVDB_INVALID_ARG, "Compute: bad channel or parameters"};
+        if (ch[chan].dtype != GBVDB_T_FLOAT) throw StatusError{GBVDB_NOT_SUPPORTED, "Compute: FP32 channels only"};
+        if (atlas_last == 0) return GBVDB_NOOP;
+        for (int it = 0; it < iterations; it++) {
+            launch_smooth(ptr<AtlasNode>(amap), atlas_last, ptr<float>(ch[chan].interior),
+                          ptr<float>(ch[chan].apron_buf), prm[0], prm[1], stream);
+            check_launch("smooth");
+            if (upd_apron) update_apron(chan, boundval);
+        }
+        return GBVDB_OK;
+    }
+
     // ------------------------------------------------------- configuration
     gbvdb_status configure(int nlev, const int* ld) {  // Configure (VG.cpp:2380-2434)
         if (nlev < 2 || nlev > kMaxLev || !ld) return GBVDB_INVALID_ARG;
@@ -1183,7 +1228,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
-                      &g->link_tag, &g->link_slot};
+                      &g->link_tag, &g->link_slot, &g->nbr_table};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1231,6 +1276,38 @@ gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron, int
     GBVDB_END(g)
 }
 
+gbvdb_status gbvdb_update_neighbors(gbvdb_grid g) {
+    GBVDB_GUARD(g)
+    return g->update_neighbors();
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_neighbors(gbvdb_grid g, int32_t* host_out, int64_t cap) {
+    GBVDB_GUARD(g)
+    if (!host_out || g->nbr_count < 0) return GBVDB_INVALID_ARG;
+    if (cap < g->nbr_count * 6) return GBVDB_CAPACITY;
+    if (g->nbr_count == 0) return GBVDB_OK;
+    g->check(cudaMemcpyAsync(host_out, g->nbr_table.p, (size_t)g->nbr_count * 24, cudaMemcpyDeviceToHost, g->stream),
+             "export neighbors");
+    g->sync();
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_update_apron_faces(gbvdb_grid g, int chan) {
+    GBVDB_GUARD(g)
+    return g->update_apron_faces(chan);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_compute(gbvdb_grid g, int effect, int chan, int iterations, const float params[3], int update_apron,
+                           int skip_aprons, float boundval) {
+    GBVDB_GUARD(g)
+    (void)skip_aprons;
+    return g->compute(effect, chan, iterations, params, update_apron != 0, boundval);
+    GBVDB_END(g)
+}
+
 gbvdb_status gbvdb_save_vbx(gbvdb_grid g, const char* path) {
     GBVDB_GUARD(g)
     return g->save_vbx(path);
@@ -1262,12 +1339,14 @@ static float3 f3(const float* v) { return v ? make_float3(v[0], v[1], v[2]) : ma
 
 gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3]) {
     GBVDB_GUARD(g)
+    g->nbr_count = -1;  // the neighbour table describes the previous topology
     return g->rebuild(n, radius, f3(orig), false, 0);
     GBVDB_END(g)
 }
 
 gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3], int min_depth) {
     GBVDB_GUARD(g)
+    g->nbr_count = -1;
     return g->rebuild(n, radius, f3(orig), true, min_depth);
     GBVDB_END(g)
 }
@@ -1542,7 +1621,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
-                            &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot};
+                            &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

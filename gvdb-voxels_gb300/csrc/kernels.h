@@ -70,6 +70,12 @@ void launch_slab_pack(const void* interior, const void* apron, int esize, int ax
                       void* slab, cudaStream_t s);
 void launch_slab_unpack(const void* slab, int esize, int ax, int ay, int bz, void* interior, void* apron,
                         cudaStream_t s);
+// neighbour table (6 leaf indices per leaf), apron faces from it, smoothing pass
+void launch_neighbors(const TreeView& t, const LeafGrid& lg, long long n, int d, int* table, cudaStream_t s);
+void launch_apron_faces(const Node* leaves, const AtlasNode* amap, int used, int ax, int ay, const int* table,
+                        int esize, void* interior, void* apron, cudaStream_t s);
+void launch_smooth(const AtlasNode* amap, int used, float* interior, const float* apron, float p1, float p2,
+                   cudaStream_t s);
 // deterministic FP64 channel sum: per-slot partials, then one fixed-order block
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s);

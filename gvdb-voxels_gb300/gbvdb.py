@@ -37,6 +37,7 @@ EXPORTS = [
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
+    "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -57,6 +58,7 @@ class JobResult(ctypes.Structure):
                 ("checksum", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
                 ("t_end_ms", ctypes.c_double)]
 TUNE_DENSE_MIN = 1
+FUNC_SMOOTH = 113
 
 
 class GbvdbError(RuntimeError):
@@ -117,6 +119,10 @@ def load(path=LIB_PATH):
     L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
+    L.gbvdb_update_neighbors.argtypes = [vp]
+    L.gbvdb_export_neighbors.argtypes = [vp, vp, i64]
+    L.gbvdb_update_apron_faces.argtypes = [vp, i32]
+    L.gbvdb_compute.argtypes = [vp, i32, i32, i32, fp, i32, i32, f32]
     L.gbvdb_load_vbx.argtypes = [vp, ctypes.c_char_p]
     L.gbvdb_server_create.argtypes = [i32, i32, i64, ctypes.POINTER(vp)]
     L.gbvdb_server_submit.argtypes = [vp, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_int64)]
@@ -323,6 +329,26 @@ class Grid:
             self._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nsub + 1,
             pts.ctypes.data if total_len > 0 else None, total_len), "export_subcells")
         return off, pts
+
+    def update_neighbors(self):
+        """UpdateNeighbors (gvdb_volume_gvdb.cpp:2527-2556)."""
+        self._check(self.L.gbvdb_update_neighbors(self._h), "update_neighbors")
+
+    def neighbors(self):
+        """The neighbour table: (leaves, 6) int32 (-x, -y, -z, +x, +y, +z), -1 = none."""
+        n = self.node_counts()[0][0]
+        out = np.zeros((n, 6), dtype=np.int32)
+        self._check(self.L.gbvdb_export_neighbors(self._h, out.ctypes.data, n * 6), "export_neighbors")
+        return out
+
+    def update_apron_faces(self, chan=0):
+        """UpdateApronFaces (gvdb_volume_gvdb.cpp:4461-4496)."""
+        return self._check(self.L.gbvdb_update_apron_faces(self._h, chan), "update_apron_faces")
+
+    def compute(self, effect, chan, iterations, params, update_apron=True, skip_aprons=True, boundval=0.0):
+        """Compute (gvdb_volume_gvdb.cpp:4532-4558); effect FUNC_SMOOTH."""
+        return self._check(self.L.gbvdb_compute(self._h, effect, chan, iterations, _f3(params), int(update_apron),
+                                                int(skip_aprons), float(boundval)), "compute")
 
     def save_vbx(self, path):
         """SaveVBX (gvdb_volume_gvdb.cpp:1626-1767)."""

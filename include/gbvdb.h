@@ -137,6 +137,22 @@ GBVDB_API gbvdb_status gbvdb_export_atlas_map(gbvdb_grid g, void* host_out, int6
  * is unspecified, as in the reference (PT.cuh:266 uses atomicAdd slots) */
 GBVDB_API gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int64_t cap_offsets,
                                              float* points, int64_t cap_points);
+/* UpdateNeighbors (gvdb_volume_gvdb.cpp:2527-2556): per leaf of the pool, the leaves one
+ * brick away along -x, -y, -z, +x, +y, +z (-1 where none); the table serves UpdateApronFaces
+ * until the topology changes.  Export: 6 int32 per leaf. */
+GBVDB_API gbvdb_status gbvdb_update_neighbors(gbvdb_grid g);
+GBVDB_API gbvdb_status gbvdb_export_neighbors(gbvdb_grid g, int32_t* host_out, int64_t cap);
+/* UpdateApronFaces (gvdb_volume_gvdb.cpp:4461-4496, cuda_gvdb_operators.cuh:27-61): the six
+ * apron faces of every assigned slot from its neighbours' interiors (edges and corners are
+ * not written; a missing neighbour leaves the face as it is) */
+GBVDB_API gbvdb_status gbvdb_update_apron_faces(gbvdb_grid g, int chan);
+/* Compute(effect, chan, iterations, params, bUpdateApron, skipOverAprons, boundval)
+ * (gvdb_volume_gvdb.cpp:4532-4558) for effect FUNC_SMOOTH (cuda_gvdb_operators.cuh:383-400):
+ * per pass v = (p1*c + the six face neighbours) / (p1 + 6) + p2 on the interior voxels of
+ * an FP32 channel, then UpdateApron(chan, boundval) when update_apron is set */
+#define GBVDB_FUNC_SMOOTH 113
+GBVDB_API gbvdb_status gbvdb_compute(gbvdb_grid g, int effect, int chan, int iterations, const float params[3],
+                                     int update_apron, int skip_aprons, float boundval);
 /* SaveVBX / LoadVBX (gvdb_volume_gvdb.cpp:1626-1767, 507-683; GVDB_FILESPEC.txt): version
  * 1.11, one grid, identity transform, GVDB topology pools and every channel 0..k-1 in the
  * atlas layout (FP16 / BF16 channels carry their extension type codes 100 / 101).  Loading

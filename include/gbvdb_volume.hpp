@@ -42,6 +42,7 @@ struct DataPtr {
 // channel types and filter constants of gvdb_types.h
 enum { T_UCHAR = GBVDB_T_UCHAR, T_FLOAT = GBVDB_T_FLOAT, T_HALF = GBVDB_T_HALF, T_BFLOAT16 = GBVDB_T_BFLOAT16 };
 enum { F_NEAREST = 0, F_LINEAR = 1, F_MIDPOINT = 2 };
+enum { FUNC_SMOOTH = GBVDB_FUNC_SMOOTH };
 enum { F_CLAMP = 0, F_BORDER = 1, F_WRAP = 2 };
 
 class VolumeGVDB {
@@ -130,6 +131,16 @@ class VolumeGVDB {
         chk(gbvdb_update_apron(g_, chan, boundval), "UpdateApron");
     }
     void FillChannel(uchar chan, float value) { chk(gbvdb_fill_channel(g_, chan, value), "FillChannel"); }
+
+    // UpdateNeighbors / UpdateApronFaces / Compute(FUNC_SMOOTH) (VG.cpp:2527-2556, 4461-4496, 4532-4558)
+    void UpdateNeighbors() { chk(gbvdb_update_neighbors(g_), "UpdateNeighbors"); }
+    void UpdateApronFaces(uchar chan) { chk(gbvdb_update_apron_faces(g_, chan), "UpdateApronFaces"); }
+    void Compute(int effect, uchar chan, int num_iterations, Vector3DF params, bool bUpdateApron,
+                 bool skipOverAprons = true, float boundval = 0.0f) {
+        float p[3] = {params.x, params.y, params.z};
+        chk(gbvdb_compute(g_, effect, chan, num_iterations, p, bUpdateApron ? 1 : 0, skipOverAprons ? 1 : 0, boundval),
+            "Compute");
+    }
 
     // SaveVBX / LoadVBX (VG.cpp:1626-1767, 507-683)
     void SaveVBX(const char* fname) { chk(gbvdb_save_vbx(g_, fname), "SaveVBX"); }

@@ -994,3 +994,125 @@ int og_save_vbx(const OGrid* g, const char* path) {
     fwrite(&goff, 8, 1, f);
     return fclose(f) == 0 ? 0 : -1;
 }
+
+/* ------------------------------------------------------------------------ */
+/* neighbour table, apron faces, smoothing (FP32 bricks)                     */
+
+/* UpdateNeighbors (VG.cpp:2527-2556): for every leaf of the pool, the leaf at its
+ * centre -/+ one brick along x, y, z (order -x, -y, -z, +x, +y, +z), as a pool
+ * index, -1 where there is none.  The reference looks up from mRoot; here from the
+ * traversal top level, as every lookup of this path. */
+void og_update_neighbors(const OGrid* g, int32_t* out) {
+    const int d = (int)g->range[0];
+    const int dir[6][3] = {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (size_t n = 0; n < g->ncnt[0]; n++) {
+        const ONode* nd = &g->nodes[0][n];
+        for (int k = 0; k < 6; k++) {
+            int32_t w[3];
+            for (int a = 0; a < 3; a++) w[a] = nd->pos[a] + d / 2 + dir[k][a] * d;
+            int64_t nl = (w[0] < 0 || w[1] < 0 || w[2] < 0) ? -1 : get_leaf_at_voxel(g, w);
+            out[n * 6 + k] = (int32_t)nl;
+        }
+    }
+}
+
+/* slot owned by leaf nl (its mValue slot, and the atlas map names it), else -1 */
+static int64_t owned_slot(const OGrid* g, int64_t nl) {
+    if (nl < 0 || (size_t)nl >= g->ncnt[0]) return -1;
+    int64_t s = leaf_slot(g, &g->nodes[0][nl]);
+    if (s < 0 || s >= g->atlas_last || g->amap[s].leaf != nl) return -1;
+    return s;
+}
+
+/* UpdateApronFaces (VG.cpp:4461-4496, gvdbUpdateApronFacesF OP.cuh:27-61) on FP32
+ * padded bricks [slot][z][y][x]: for every assigned slot and each of its -x, -y, -z
+ * neighbours (neighbour table), the slot's first interior plane goes to the
+ * neighbour's far apron face and the neighbour's last interior plane to the slot's
+ * near apron face.  Edges and corners are not written; a missing neighbour leaves the
+ * face as it is. */
+void og_apron_faces_f32(const OGrid* g, const int32_t* table, float* bricks) {
+    for (int s = 0; s < g->atlas_last; s++) {
+        int64_t L = g->amap[s].leaf;
+        if (L < 0) continue;
+        for (int side = 0; side < 3; side++) {
+            int64_t ns = owned_slot(g, table[L * 6 + side]);
+            if (ns < 0) continue;
+            float* self = bricks + (size_t)s * 5832;
+            float* nb = bricks + (size_t)ns * 5832;
+            for (int u = 1; u <= 16; u++)
+                for (int v = 1; v <= 16; v++) {
+                    size_t si, sa, ni, na;
+                    if (side == 0) {  /* x: (x, y=u, z=v) */
+                        si = ((size_t)v * 18 + u) * 18 + 1;  sa = ((size_t)v * 18 + u) * 18 + 0;
+                        ni = ((size_t)v * 18 + u) * 18 + 16; na = ((size_t)v * 18 + u) * 18 + 17;
+                    } else if (side == 1) {  /* y: (x=u, y, z=v) */
+                        si = ((size_t)v * 18 + 1) * 18 + u;  sa = ((size_t)v * 18 + 0) * 18 + u;
+                        ni = ((size_t)v * 18 + 16) * 18 + u; na = ((size_t)v * 18 + 17) * 18 + u;
+                    } else {  /* z: (x=u, y=v, z) */
+                        si = ((size_t)1 * 18 + v) * 18 + u;  sa = ((size_t)0 * 18 + v) * 18 + u;
+                        ni = ((size_t)16 * 18 + v) * 18 + u; na = ((size_t)17 * 18 + v) * 18 + u;
+                    }
+                    nb[na] = self[si];
+                    self[sa] = nb[ni];
+                }
+        }
+    }
+}
+
+/* UpdateApron (OP.cuh:72-131) on FP32 padded bricks: every apron voxel = the interior
+ * voxel of the leaf at that index-space position, or boundval. */
+void og_apron_full_f32(const OGrid* g, float* bricks, float boundval) {
+    float* src = (float*)malloc((size_t)g->atlas_last * 5832 * sizeof(float));
+    memcpy(src, bricks, (size_t)g->atlas_last * 5832 * sizeof(float));
+    for (int s = 0; s < g->atlas_last; s++) {
+        if (g->amap[s].leaf < 0) continue;
+        const int32_t* bp = g->amap[s].pos;
+        float* brick = bricks + (size_t)s * 5832;
+        for (int z = 0; z < 18; z++)
+            for (int y = 0; y < 18; y++)
+                for (int x = 0; x < 18; x++) {
+                    if (x > 0 && x < 17 && y > 0 && y < 17 && z > 0 && z < 17) continue;
+                    int32_t w[3] = {bp[0] + x - 1, bp[1] + y - 1, bp[2] + z - 1};
+                    float v = boundval;
+                    int64_t nl = (w[0] < 0 || w[1] < 0 || w[2] < 0) ? -1 : get_leaf_at_voxel(g, w);
+                    if (nl >= 0) {
+                        const ONode* nn = &g->nodes[0][nl];
+                        int64_t ns = leaf_slot(g, nn);
+                        if (ns >= 0) {
+                            int lx = w[0] - nn->pos[0] + 1, ly = w[1] - nn->pos[1] + 1, lz = w[2] - nn->pos[2] + 1;
+                            v = src[(size_t)ns * 5832 + ((size_t)lz * 18 + ly) * 18 + lx];
+                        }
+                    }
+                    brick[((size_t)z * 18 + y) * 18 + x] = v;
+                }
+    }
+    free(src);
+}
+
+/* Compute(FUNC_SMOOTH) one iteration (gvdbOpSmooth, OP.cuh:383-400) on FP32 padded
+ * bricks, interior voxels of every assigned slot, reading the values before the pass:
+ * v = p1*c, then + x-1, x+1, y-1, y+1, z-1, z+1 in FP32; v = v / (p1 + 6.0) + p2 in
+ * double (the source's double literal), rounded to float. */
+void og_smooth_f32(const OGrid* g, float* bricks, float p1, float p2) {
+    float* src = (float*)malloc((size_t)g->atlas_last * 5832 * sizeof(float));
+    memcpy(src, bricks, (size_t)g->atlas_last * 5832 * sizeof(float));
+    for (int s = 0; s < g->atlas_last; s++) {
+        if (g->amap[s].leaf < 0) continue;
+        const float* b = src + (size_t)s * 5832;
+        float* o = bricks + (size_t)s * 5832;
+        for (int z = 1; z < 17; z++)
+            for (int y = 1; y < 17; y++)
+                for (int x = 1; x < 17; x++) {
+                    const size_t i = ((size_t)z * 18 + y) * 18 + x;
+                    volatile float v = p1 * b[i];
+                    v = v + b[i - 1];
+                    v = v + b[i + 1];
+                    v = v + b[i - 18];
+                    v = v + b[i + 18];
+                    v = v + b[i - 324];
+                    v = v + b[i + 324];
+                    o[i] = (float)((double)v / ((double)p1 + 6.0) + (double)p2);
+                }
+    }
+    free(src);
+}

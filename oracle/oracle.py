@@ -98,6 +98,10 @@ def lib():
         L.og_checksum.argtypes = [vp, i32]
         L.og_save_vbx.restype = i32
         L.og_save_vbx.argtypes = [vp, ctypes.c_char_p]
+        L.og_update_neighbors.argtypes = [vp, vp]
+        L.og_apron_faces_f32.argtypes = [vp, vp, vp]
+        L.og_apron_full_f32.argtypes = [vp, vp, f32]
+        L.og_smooth_f32.argtypes = [vp, vp, f32, f32]
         _lib = L
     return _lib
 
@@ -243,6 +247,32 @@ class OracleGrid:
 
     def checksum(self, chan=0):
         return float(lib().og_checksum(self._h, chan))
+
+    def neighbors(self):
+        """UpdateNeighbors restated: (leaves, 6) pool indices (-x, -y, -z, +x, +y, +z), -1 = none."""
+        n = self.node_count(0)
+        out = np.zeros((n, 6), dtype=np.int32)
+        if n:
+            lib().og_update_neighbors(self._h, out.ctypes.data)
+        return out
+
+    @staticmethod
+    def _bricks_arg(bricks):
+        assert bricks.dtype == np.float32 and bricks.flags.c_contiguous and bricks.shape[1:] == (18, 18, 18)
+        return bricks.ctypes.data
+
+    def apron_faces_f32(self, bricks, table):
+        """UpdateApronFaces restated, in place on FP32 padded bricks [slot, z, y, x]."""
+        t = np.ascontiguousarray(table, dtype=np.int32)
+        lib().og_apron_faces_f32(self._h, t.ctypes.data, self._bricks_arg(bricks))
+
+    def apron_full_f32(self, bricks, boundval):
+        """UpdateApron restated, in place on FP32 padded bricks."""
+        lib().og_apron_full_f32(self._h, self._bricks_arg(bricks), float(boundval))
+
+    def smooth_f32(self, bricks, p1, p2):
+        """One Compute(FUNC_SMOOTH) pass restated, in place on FP32 padded bricks."""
+        lib().og_smooth_f32(self._h, self._bricks_arg(bricks), float(p1), float(p2))
 
     def save_vbx(self, path):
         """SaveVBX restated (VG.cpp:1626-1767): FP32 atlas from the FP64 oracle values."""
