@@ -119,6 +119,7 @@ struct gbvdb_grid_s {
     PointSrc sc_pts{nullptr, 0, 12, 0};
     long long sc_nleaf = 0, sc_nbricks = 0, sc_len = 0, sc_orphans = 0;
     bool lists_valid = false;
+    Quant sc_quant{};  // position quantisation of the last insert (FP16 variant)
     DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted;
     DevBuf list_cnt, list_off, list_pts;
     DevBuf offs_buf;
@@ -626,7 +627,7 @@ struct gbvdb_grid_s {
         check_launch("linked");
     }
 
-    gbvdb_status insert_subcell(int sc, long long n, float R, float3 trans, long long* out_len) {
+    gbvdb_status insert_subcell(int sc, long long n, float R, float3 trans, long long* out_len, bool fp16 = false) {
         if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
         if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
         if (sc != 4 || log2dim[0] != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 with 16^3 bricks only"};
@@ -648,7 +649,14 @@ struct gbvdb_grid_s {
         unsigned long long* totals = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 128);
         check(cudaMemsetAsync(totals, 0, 16, stream), "totals clear");
         TreeView t = view();
-        launch_bin_count(t, lgv, p, trans, R, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
+        // InsertPointsSubcell_FP16 quantises over the bounds of the last GetBoundingBox
+        // (VG.cpp:5458-5462: PosRange = PosMax - PosMin)
+        Quant qz{};
+        qz.on = fp16 ? 1 : 0;
+        qz.mn = make_float3(posmin[0], posmin[1], posmin[2]);
+        qz.rg = make_float3(posmax[0] - posmin[0], posmax[1] - posmin[1], posmax[2] - posmin[2]);
+        sc_quant = qz;
+        launch_bin_count(t, lgv, p, trans, R, qz, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
                          ptr<uint32_t>(rank_of), totals, stream);
         check_launch("bin_count");
         grow(scan_tmp, scan_tmp_bytes(nbins));
@@ -667,7 +675,7 @@ struct gbvdb_grid_s {
         sc_nbricks = nb;
         mark();
         grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
-        launch_bin_scatter(p, trans, R, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
+        launch_bin_scatter(p, trans, R, qz, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
                            ptr<float4>(sorted), stream);
         check_launch("bin_scatter");
         mark();
@@ -694,11 +702,12 @@ struct gbvdb_grid_s {
         grow(list_pts, (size_t)std::max(sc_len, 1ll) * 12);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
         TreeView t = view();
-        launch_list_count(t, lgv, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt), stream);
+        launch_list_count(t, lgv, sc_pts, sc_trans, sc_R, sc_quant, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt),
+                          stream);
         grow(scan_tmp, scan_tmp_bytes(nsub));
         scan_exclusive_u32(ptr<uint32_t>(list_cnt), ptr<uint32_t>(list_off), nsub, scan_tmp.p, stream);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
-        launch_list_fill(t, lgv, sc_pts, sc_trans, sc_R, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
+        launch_list_fill(t, lgv, sc_pts, sc_trans, sc_R, sc_quant, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
                          ptr<uint32_t>(list_cnt), ptr<float>(list_pts), stream);
         check_launch("lists");
         lists_valid = true;
@@ -1388,6 +1397,24 @@ gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int sc, int64_t n, float 
     gbvdb_status st = g->insert_subcell(sc, n, radius, f3(trans), &len);
     if (st == GBVDB_OK && out_len) *out_len = len;
     return st;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_insert_points_subcell_fp16(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
+                                              int64_t* out_len) {
+    GBVDB_GUARD(g)
+    long long len = 0;
+    gbvdb_status st = g->insert_subcell(sc, n, radius, f3(trans), &len, true);
+    if (st == GBVDB_OK && out_len) *out_len = len;
+    return st;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_gather_levelset_fp16(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
+                                        int64_t sc_len, int chan, int clr_chan) {
+    GBVDB_GUARD(g)
+    (void)n; (void)trans;
+    return g->gather(1, sc, radius, sc_len, chan, clr_chan, false);
     GBVDB_END(g)
 }
 

@@ -90,10 +90,16 @@ cudaError_t checksum_noalloc(const AtlasNode* amap, int used, int dtype, const v
 
 // ---- points.cu
 void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s);
-void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+// 16-bit position quantisation of the FP16 subcell variants (InsertPointsSubcell_FP16,
+// PT.cuh:154-216): q = trunc((w - mn) / rg * 65535), stored and gathered as q / 65535 * rg + mn
+struct Quant {
+    float3 mn, rg;
+    int on;
+};
+void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                       uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals,
                       cudaStream_t s);
-void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
+void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s);
 
 struct GatherParams {
@@ -113,9 +119,9 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    void* interior, cudaStream_t s);
 // materialized subcell lists (export and the fallback gather)
-void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                        uint32_t* cnt, cudaStream_t s);
-void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                       const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s);
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s);

@@ -44,6 +44,26 @@ __device__ __forceinline__ bool load_valid(PointSrc p, long long i, float3 trans
     return !(x < 0 || y < 0 || z < 0);
 }
 
+// the stored (and gathered) position of a point: w itself, or its 16-bit quantised
+// and dequantised form, one rounding per FP32 operation
+__device__ __forceinline__ float quant16(float w, float mn, float rg) {
+    if (!(rg > 0.0f)) return mn;
+    const float t = __fmul_rn(__fdiv_rn(fsub(w, mn), rg), 65535.0f);
+    const unsigned q = t <= 0.0f ? 0u : (t >= 65535.0f ? 65535u : (unsigned)t);
+    return fadd(__fmul_rn(__fdiv_rn((float)q, 65535.0f), rg), mn);
+}
+__device__ __forceinline__ void stored_pos(const Quant& q, const float* w, float* out) {
+    if (q.on) {
+        out[0] = quant16(w[0], q.mn.x, q.rg.x);
+        out[1] = quant16(w[1], q.mn.y, q.rg.y);
+        out[2] = quant16(w[2], q.mn.z, q.rg.z);
+    } else {
+        out[0] = w[0];
+        out[1] = w[1];
+        out[2] = w[2];
+    }
+}
+
 __global__ void k_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -63,15 +83,18 @@ __device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeV
 
 // Home-subcell counting pass + total subcell-list length (the reference's
 // pSCPntsLength) + orphans (valid points whose home leaf is not linked).
-__global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* __restrict__ scmap,
-                           uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
+__global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
+                            const uint32_t* __restrict__ scmap, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
+                            unsigned long long* totals) {
     unsigned long long members = 0, orphans = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float w[3];
         if (!load_valid(p, i, trans, w[0], w[1], w[2])) { bin_of[i] = -1; continue; }
-        int h[3];
+        float ps[3];
+        stored_pos(qz, w, ps);
+        int h[3];  // home subcell of the stored position
 #pragma unroll
-        for (int a = 0; a < 3; a++) h[a] = ((int)w[a]) & ~(kSc - 1);
+        for (int a = 0; a < 3; a++) h[a] = ((int)ps[a]) & ~(kSc - 1);
         long long leaf = linked_leaf(lg, t, h[0], h[1], h[2]);
         if (leaf < 0) {
             bin_of[i] = -2;
@@ -121,13 +144,13 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
 // i.e. lo <= d <= hi with lo = int(w-R)/4 - H and hi = int(w+1+R)/4 - H.  For
 // R <= 11 (the range the brick-tiled gather serves) lo >= -4 and hi <= 3, so the
 // masks are exact; outside that range they are clipped and not used.
-__device__ __forceinline__ int pack_ranges(const float* w, float R) {
+__device__ __forceinline__ int pack_ranges(const float* w, const float* home, float R) {
     int packed = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         int lo, hi;
         sc_range(w[a], R, lo, hi);
-        int h = ((int)w[a]) >> 2;
+        int h = ((int)home[a]) >> 2;
         int l = max((lo >> 2) - h, -4), u = min((hi >> 2) - h, 4);  // lo, hi are multiples of 4
         if (l <= u) packed |= (int)((((1u << (u - l + 1)) - 1u) << (l + 4)) << (9 * a));
     }
@@ -145,7 +168,7 @@ __device__ __forceinline__ int member_bits(int ox, int oy, int oz) {
     return (1 << (4 - ox)) | (1 << (13 - oy)) | (1 << (22 - oz));
 }
 
-__global__ void k_bin_scatter(PointSrc p, float3 trans, float R, const int* __restrict__ bin_of,
+__global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const int* __restrict__ bin_of,
                               const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
                               float4* __restrict__ sorted) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
@@ -154,7 +177,9 @@ __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, const int* __re
         float x, y, z;
         load_pos(p.base, i, p.stride, p.off, x, y, z);
         float w[3] = {fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z)};
-        sorted[bin_off[b] + rank_of[i]] = make_float4(w[0], w[1], w[2], __int_as_float(pack_ranges(w, R)));
+        float ps[3];
+        stored_pos(qz, w, ps);
+        sorted[bin_off[b] + rank_of[i]] = make_float4(ps[0], ps[1], ps[2], __int_as_float(pack_ranges(w, ps, R)));
     }
 }
 
@@ -536,8 +561,8 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
 // ---- materialized subcell lists (reference-shaped; export + fallback) ----
 
 template <bool kFill>
-__device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
-                            uint32_t* cnt, const uint32_t* off, float* out3) {
+__device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant qz,
+                            const uint32_t* scmap, uint32_t* cnt, const uint32_t* off, float* out3) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float w[3];
         if (!load_valid(p, i, trans, w[0], w[1], w[2])) continue;
@@ -555,21 +580,23 @@ __device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, f
                     unsigned idx = scmap[leaf] * 64u + (unsigned)loc;
                     unsigned k = atomicAdd(cnt + idx, 1u);
                     if (kFill) {
+                        float ps[3];
+                        stored_pos(qz, w, ps);
                         float* o = out3 + 3ull * (off[idx] + k);
-                        o[0] = w[0];
-                        o[1] = w[1];
-                        o[2] = w[2];
+                        o[0] = ps[0];
+                        o[1] = ps[1];
+                        o[2] = ps[2];
                     }
                 }
     }
 }
-__global__ void k_list_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+__global__ void k_list_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz, const uint32_t* scmap,
                              uint32_t* cnt) {
-    list_points<false>(t, lg, p, trans, R, scmap, cnt, nullptr, nullptr);
+    list_points<false>(t, lg, p, trans, R, qz, scmap, cnt, nullptr, nullptr);
 }
-__global__ void k_list_fill(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
+__global__ void k_list_fill(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz, const uint32_t* scmap,
                             const uint32_t* off, uint32_t* cursor, float* out3) {
-    list_points<true>(t, lg, p, trans, R, scmap, cursor, off, out3);
+    list_points<true>(t, lg, p, trans, R, qz, scmap, cursor, off, out3);
 }
 
 // reference-shaped gather over materialized lists: one block per linked leaf,
@@ -611,16 +638,16 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
     if (n <= 0) return;
     k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
 }
-void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R,
+void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
                       unsigned long long* totals, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, scmap, bin_cnt, bin_of, rank_of, totals);
+    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, bin_cnt, bin_of, rank_of, totals);
 }
-void launch_bin_scatter(PointSrc p, float3 trans, float R, const int* bin_of, const uint32_t* rank_of,
+void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, bin_of, rank_of, bin_off, sorted);
+    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted);
 }
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
@@ -636,15 +663,15 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
         k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs,
                                                                             noffs, gp, (__nv_bfloat16*)interior);
 }
-void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R,
+void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                        const uint32_t* scmap, uint32_t* cnt, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, scmap, cnt);
+    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, cnt);
 }
-void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, const uint32_t* scmap,
-                      const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s) {
+void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
+                      const uint32_t* scmap, const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, scmap, off, cursor, out3);
+    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, off, cursor, out3);
 }
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s) {

@@ -38,6 +38,7 @@ EXPORTS = [
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
+    "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -120,6 +121,8 @@ def load(path=LIB_PATH):
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
     L.gbvdb_update_neighbors.argtypes = [vp]
+    L.gbvdb_insert_points_subcell_fp16.argtypes = [vp, i32, i64, f32, fp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_gather_levelset_fp16.argtypes = [vp, i32, i64, f32, fp, i64, i32, i32]
     L.gbvdb_export_neighbors.argtypes = [vp, vp, i64]
     L.gbvdb_update_apron_faces.argtypes = [vp, i32]
     L.gbvdb_compute.argtypes = [vp, i32, i32, i32, fp, i32, i32, f32]
@@ -246,6 +249,18 @@ class Grid:
         st = self._check(self.L.gbvdb_insert_points_subcell(self._h, subcell, n, radius, _f3(trans),
                                                             ctypes.byref(out)), "insert_points_subcell")
         return st, int(out.value)
+
+    def insert_points_subcell_fp16(self, subcell, n, radius, trans=(0, 0, 0)):
+        """InsertPointsSubcell_FP16: 16-bit positions over the point bounds."""
+        out = ctypes.c_int64(-1)
+        st = self._check(self.L.gbvdb_insert_points_subcell_fp16(self._h, subcell, n, radius, _f3(trans),
+                                                                 ctypes.byref(out)), "insert_points_subcell_fp16")
+        return st, int(out.value)
+
+    def gather_levelset_fp16(self, subcell, n, radius, trans, sc_len, chan=0, clr_chan=-1):
+        """GatherLevelSet_FP16 (no accumulation)."""
+        return self._check(self.L.gbvdb_gather_levelset_fp16(self._h, subcell, n, radius, _f3(trans), sc_len, chan,
+                                                             clr_chan), "gather_levelset_fp16")
 
     def gather_density(self, subcell, n, radius, trans, sc_len, chan=0, clr_chan=-1, accum=False):
         return self._check(self.L.gbvdb_gather_density(self._h, subcell, n, radius, _f3(trans), sc_len, chan,

@@ -110,6 +110,16 @@ GBVDB_API gbvdb_status gbvdb_gather_density(gbvdb_grid g, int subcell_size, int6
 GBVDB_API gbvdb_status gbvdb_gather_levelset(gbvdb_grid g, int subcell_size, int64_t n, float radius,
                                              const float trans[3], int64_t sc_len, int chan, int clr_chan,
                                              int accum);
+/* InsertPointsSubcell_FP16 (gvdb_volume_gvdb.cpp:5094-5189, cuda_gvdb_particles.cuh:154-216): as
+ * InsertPointsSubcell, with positions stored at 16 bits per axis over the bounds of the last
+ * RebuildTopology (q = trunc((w - PosMin) / PosRange * 65535)); gathers that follow read the
+ * dequantised positions q / 65535 * PosRange + PosMin. */
+GBVDB_API gbvdb_status gbvdb_insert_points_subcell_fp16(gbvdb_grid g, int subcell_size, int64_t n, float radius,
+                                                        const float trans[3], int64_t* out_len);
+/* GatherLevelSet_FP16 (gvdb_volume_gvdb.cpp:5375-5401, cuda_gvdb_particles.cuh:775-811):
+ * v = min(3, min_j(|p_j - v| - radius)) over the stored positions, no accumulation */
+GBVDB_API gbvdb_status gbvdb_gather_levelset_fp16(gbvdb_grid g, int subcell_size, int64_t n, float radius,
+                                                  const float trans[3], int64_t sc_len, int chan, int clr_chan);
 /* UpdateApron(chan, boundval) (gvdb_volume_gvdb.cpp:4418-4457, cuda_gvdb_operators.cuh:72-131) */
 GBVDB_API gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval);
 /* ClearChannel / FillChannel (gvdb_volume_gvdb.cpp:2456-2485) for the assigned slots */

@@ -125,6 +125,20 @@ class VolumeGVDB {
                                   bAccum ? 1 : 0),
             "GatherLevelSet");
     }
+    // FP16 subcell variants (VG.cpp:5094-5189, 5375-5401)
+    void InsertPointsSubcell_FP16(int subcell_size, int num_pnts, float pRadius, Vector3DF trans, int& pSCPntsLength) {
+        float t[3] = {trans.x, trans.y, trans.z};
+        int64_t len = pSCPntsLength;
+        if (chk(gbvdb_insert_points_subcell_fp16(g_, subcell_size, num_pnts, pRadius, t, &len),
+                "InsertPointsSubcell_FP16") == GBVDB_OK)
+            pSCPntsLength = (int)len;
+    }
+    void GatherLevelSet_FP16(int subcell_size, int num_pnts, float radius, Vector3DF trans, int& pSCPntsLength,
+                             int chanLevelset, int chanClr) {
+        float t[3] = {trans.x, trans.y, trans.z};
+        chk(gbvdb_gather_levelset_fp16(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanLevelset, chanClr),
+            "GatherLevelSet_FP16");
+    }
     // UpdateApron (VG.cpp:4411-4457)
     void UpdateApron(uchar chan, float boundval = 0.0f, bool changeCtx = true) {
         (void)changeCtx;

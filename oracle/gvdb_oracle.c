@@ -705,9 +705,34 @@ static inline void sc_range(float w, float R, int sc, int32_t* lo, int32_t* hi) 
 /* InsertPointsSubcell (VG.cpp:4971-5092): SetFlagSubcell (PT.cuh:109-118), CountSubcell
  * (PT.cuh:275-315), PrefixSum, InsertSubcell (PT.cuh:218-273).  Lists are built in a
  * deterministic order (point order); the reference's order within a list is arbitrary. */
+/* InsertPointsSubcell_FP16 (VG.cpp:5094-5189, gvdbInsertSubcell_fp16 PT.cuh:154-216) stores
+ * each position quantised to 16 bits per axis over the point bounds [PosMin, PosMin +
+ * PosRange] (GetBoundingBox, VG.cpp:5404-5467), q = trunc((w - min) / range * 65535);
+ * GatherLevelSet_FP16 (PT.cuh:775-811) reads q / 65535 * range + min.  The lists here hold
+ * that dequantised position, in FP32 with one rounding per operation. */
+static inline float quant16(float w, float mn, float rg) {
+    if (!(rg > 0.0f)) return mn;
+    float t = ((w - mn) / rg) * 65535.0f;
+    unsigned q = t <= 0.0f ? 0u : (t >= 65535.0f ? 65535u : (unsigned)t);
+    return ((float)q / 65535.0f) * rg + mn;
+}
+
+static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off, float R,
+                          const float trans[3], int64_t* out_len, int fp16);
+
 int og_insert_points_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off,
                              float R, const float trans[3], int64_t* out_len) {
+    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 0);
+}
+int og_insert_points_subcell_fp16(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off,
+                                  float R, const float trans[3], int64_t* out_len) {
+    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 1);
+}
+
+static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off, float R,
+                          const float trans[3], int64_t* out_len, int fp16) {
     const char* pos = (const char*)posv;
+    const float prange[3] = {g->posmax[0] - g->posmin[0], g->posmax[1] - g->posmin[1], g->posmax[2] - g->posmin[2]};
     if (g->nused[0] == 0) return OG_NOOP;
     if (sc <= 0 || (16 % sc) != 0 || og_res(g, 0) != 16) return OG_INVALID_ARG;
     g->sc_size = sc;
@@ -760,9 +785,8 @@ int og_insert_points_subcell(OGrid* g, int sc, const void* posv, int64_t n, int 
                             g->sc_cnt[idx]++;
                         } else {
                             int64_t at = g->sc_off[idx] + g->sc_cnt[idx]++;
-                            g->sc_pts[at * 3 + 0] = w[0];
-                            g->sc_pts[at * 3 + 1] = w[1];
-                            g->sc_pts[at * 3 + 2] = w[2];
+                            for (int a = 0; a < 3; a++)
+                                g->sc_pts[at * 3 + a] = fp16 ? quant16(w[a], g->posmin[a], prange[a]) : w[a];
                         }
                     }
         }

@@ -61,8 +61,9 @@ def lib():
         L.og_rebuild_topology.argtypes = [vp, vp, i64, i32, i32, f32, fp3]
         L.og_accumulate_topology.argtypes = [vp, vp, i64, i32, i32, f32, fp3, i32]
         L.og_update_atlas.argtypes = [vp]
-        L.og_insert_points_subcell.argtypes = [vp, i32, vp, i64, i32, i32, f32, fp3,
-                                               ctypes.POINTER(ctypes.c_int64)]
+        L.og_insert_points_subcell.argtypes = [vp, i32, vp, i64, i32, i32, f32, fp3, ctypes.POINTER(ctypes.c_int64)]
+        L.og_insert_points_subcell_fp16.argtypes = [vp, i32, vp, i64, i32, i32, f32, fp3,
+                                                    ctypes.POINTER(ctypes.c_int64)]
         L.og_gather.argtypes = [vp, i32, f32, i32, i32]
         L.og_update_apron.argtypes = [vp, i32, f32]
         for name in ("og_depth", "og_top_lev", "og_childlist_len"):
@@ -181,6 +182,14 @@ class OracleGrid:
         out = ctypes.c_int64(-1)
         rc = lib().og_insert_points_subcell(self._h, subcell, p.ctypes.data, n, stride, 0,
                                             float(radius), _f3(trans), ctypes.byref(out))
+        return rc, int(out.value)
+
+    def insert_points_subcell_fp16(self, points, radius, subcell=4, trans=(0, 0, 0)):
+        """InsertPointsSubcell_FP16 restated: lists hold 16-bit-quantised positions (dequantised)."""
+        p, n, stride = self._pts(points)
+        out = ctypes.c_int64(-1)
+        rc = lib().og_insert_points_subcell_fp16(self._h, subcell, p.ctypes.data, n, stride, 0,
+                                                 float(radius), _f3(trans), ctypes.byref(out))
         return rc, int(out.value)
 
     def gather_density(self, radius, chan=0, accum=False):

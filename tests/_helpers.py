@@ -14,7 +14,7 @@ ATOL = 1e-6
 
 
 def run_oracle(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
-               boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), accumulate=False, threads=0):
+               boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), accumulate=False, threads=0, fp16_subcells=False):
     import oracle
 
     g = oracle.OracleGrid(log2dims, threads=threads)
@@ -28,7 +28,7 @@ def run_oracle(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rh
             rc = g.rebuild_topology(pts, radius, orig)
         assert rc == 0, rc
         g.update_atlas()
-        rc, ln = g.insert_points_subcell(pts, R)
+        rc, ln = (g.insert_points_subcell_fp16 if fp16_subcells else g.insert_points_subcell)(pts, R)
         if mode == "density":
             g.gather_density(rho)
         else:
@@ -54,7 +54,8 @@ def snapshot_oracle(g, ln):
 
 
 def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
-            boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True):
+            boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True,
+            fp16_subcells=False):
     import torch
 
     import gbvdb
@@ -72,9 +73,11 @@ def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1
         else:
             g.rebuild_topology(n, radius, orig)
         g.update_atlas()
-        st, ln = g.insert_points_subcell(4, n, R)
+        st, ln = (g.insert_points_subcell_fp16 if fp16_subcells else g.insert_points_subcell)(4, n, R)
         if mode == "density":
             g.gather_density(4, n, rho, (0, 0, 0), ln)
+        elif fp16_subcells:
+            g.gather_levelset_fp16(4, n, rho, (0, 0, 0), ln)
         else:
             g.gather_levelset(4, n, rho, (0, 0, 0), ln)
         g.update_apron(0, boundval)

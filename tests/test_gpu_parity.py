@@ -223,3 +223,19 @@ def test_surface_config_storage_types(gpu_lib, dtype, rtol, atol):
     H.compare_subcells(o[0], g[0])
     err = H.compare_values(o[0], g[0], rtol, atol, dtype=dt)
     print("surface crop %s: %d points, max abs error vs FP64 %.3g" % (dtype, pts.shape[0], err))
+
+
+def test_fp16_subcells_levelset(gpu_lib):
+    """InsertPointsSubcell_FP16 + GatherLevelSet_FP16 (the point-cloud sample's path): lists
+    hold 16-bit-quantised positions over the point bounds; membership, lists, values and
+    apron match the oracle's restatement, and quantisation changes some values."""
+    pos, vel = _mini_fluid()
+    frames = [(pos + 0.5 * (k + 1) * vel).astype(np.float32) for k in range(3)]
+    kw = dict(frames=frames, radius=2.0, R=2.0, rho=1.0, mode="levelset", boundval=3.0)
+    _, o = H.run_oracle(None, fp16_subcells=True, **kw)
+    _, g = H.run_gpu(None, fp16_subcells=True, **kw)
+    for k in range(3):
+        _full_check(o[k], g[k], 3.0)
+    _, g32 = H.run_gpu(None, **kw)
+    assert not np.array_equal(g32[-1]["bricks"], g[-1]["bricks"])
+    assert np.abs(g32[-1]["bricks"].astype(np.float64) - g[-1]["bricks"]).max() < 0.05
