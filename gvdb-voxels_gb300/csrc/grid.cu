@@ -136,6 +136,10 @@ struct gbvdb_grid_s {
     DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     unsigned char* pinned = nullptr;
 
+    // legacy InsertPoints: leaf and rank per point, points grouped by leaf
+    DevBuf pnode, pndx, gcnt, goff, psort;
+    long long ins_n = -1, ins_nleaf = -1;
+
     // neighbour table of UpdateNeighbors (6 leaf indices per leaf) and the leaf count it covers
     DevBuf nbr_table;
     long long nbr_count = -1;
@@ -226,6 +230,7 @@ struct gbvdb_grid_s {
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
         nbr_count = -1;
+        ins_n = -1;
         lgdom_init = false;
         lgv.cells = nullptr;
         atlas_last = 0;
@@ -575,6 +580,11 @@ struct gbvdb_grid_s {
             if (!C.used || C.cap_slots >= slots) continue;
             grow(C.interior, (size_t)slots * 4096 * C.esize, (size_t)C.cap_slots * 4096 * C.esize);
             grow(C.apron_buf, (size_t)slots * kApronStride * C.esize, (size_t)C.cap_slots * kApronStride * C.esize);
+            // bricks new to the atlas start at zero, as the channel does
+            const size_t i0 = (size_t)C.cap_slots * 4096 * C.esize, a0 = (size_t)C.cap_slots * kApronStride * C.esize;
+            check(cudaMemsetAsync(ptr<char>(C.interior) + i0, 0, (size_t)slots * 4096 * C.esize - i0, stream), "atlas clear");
+            check(cudaMemsetAsync(ptr<char>(C.apron_buf) + a0, 0, (size_t)slots * kApronStride * C.esize - a0, stream),
+                  "atlas clear");
             C.cap_slots = slots;
         }
     }
@@ -827,6 +837,50 @@ struct gbvdb_grid_s {
         check_launch("apron");
         mark();
         stage_end();
+        return GBVDB_OK;
+    }
+
+    // ------------------------------------------- legacy insert and scatter
+    // InsertPoints (VG.cpp:5219-5267): the leaf of every point and the points grouped by
+    // leaf (always grouped: ScatterDensity reads the groups; bPrefix only names the
+    // reference's optional sort)
+    gbvdb_status insert_points(long long n, float3 trans, bool prefix) {
+        (void)prefix;
+        if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
+        if (!pts.base && n > 0) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
+        if (n < 0 || (pts.n > 0 && n > pts.n)) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
+        long long nl = ncnt[0];
+        grow(pnode, (size_t)std::max(n, 1ll) * 4);
+        grow(pndx, (size_t)std::max(n, 1ll) * 4);
+        grow(gcnt, (size_t)(nl + 1) * 4);
+        grow(goff, (size_t)(nl + 1) * 4);
+        grow(psort, (size_t)std::max(n, 1ll) * 12);
+        check(cudaMemsetAsync(gcnt.p, 0, (size_t)(nl + 1) * 4, stream), "gcnt clear");
+        PointSrc p = pts;
+        p.n = n;
+        TreeView t = view();
+        launch_insert_points(t, lgv, p, trans, ptr<int>(pnode), ptr<uint32_t>(pndx), ptr<uint32_t>(gcnt), stream);
+        check_launch("insert points");
+        grow(scan_tmp, scan_tmp_bytes(nl));
+        scan_exclusive_u32(ptr<uint32_t>(gcnt), ptr<uint32_t>(goff), nl, scan_tmp.p, stream);
+        launch_sort_points(p, trans, ptr<int>(pnode), ptr<uint32_t>(pndx), ptr<uint32_t>(goff), ptr<float>(psort), stream);
+        check_launch("sort points");
+        ins_n = n;
+        ins_nleaf = nl;
+        return GBVDB_OK;
+    }
+
+    // ScatterDensity (VG.cpp:5624-5660, gvdbScatterPointDensity PT.cuh:525-571) into
+    // channel 0 over the groups of the last InsertPoints; amp is unused by the kernel
+    gbvdb_status scatter_density(float radius, bool expand, bool avg_color) {
+        if (avg_color) throw StatusError{GBVDB_NOT_SUPPORTED, "colour channels are not part of this path"};
+        if (ins_n < 0 || ins_nleaf != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "InsertPoints was not called for this topology"};
+        if (!ch[0].used || ch[0].dtype != GBVDB_T_FLOAT) throw StatusError{GBVDB_NOT_SUPPORTED, "ScatterDensity: FP32 channel 0"};
+        if (atlas_last == 0 || ins_nleaf == 0) return GBVDB_NOOP;
+        launch_scatter_density(ptr<Node>(nodes[0]), ins_nleaf, ptr<uint32_t>(goff), ptr<float>(psort), radius,
+                               expand ? 1 : 0, res[0], ax, ay, ptr<float>(ch[0].interior), ptr<float>(ch[0].apron_buf),
+                               stream);
+        check_launch("scatter density");
         return GBVDB_OK;
     }
 
@@ -1207,6 +1261,8 @@ static void keep_pool_memory(int device) {
     done[device] = true;
 }
 
+static float3 f3(const float* v) { return v ? make_float3(v[0], v[1], v[2]) : make_float3(0, 0, 0); }
+
 extern "C" {
 
 gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
@@ -1237,7 +1293,8 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
-                      &g->link_tag, &g->link_slot, &g->nbr_table};
+                      &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
+                      &g->psort};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1282,6 +1339,44 @@ gbvdb_status gbvdb_set_channel_default(gbvdb_grid g, int ax, int ay, int az) {
 gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron, int ax, int ay, int az) {
     GBVDB_GUARD(g)
     return g->add_channel(chan, dtype, apron, ax, ay, az);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_insert_points(gbvdb_grid g, int64_t n, const float trans[3], int prefix) {
+    GBVDB_GUARD(g)
+    return g->insert_points(n, f3(trans), prefix != 0);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_scatter_density(gbvdb_grid g, int64_t n, float radius, float amp, const float trans[3], int expand,
+                                   int avg_color) {
+    GBVDB_GUARD(g)
+    (void)n; (void)amp; (void)trans;
+    return g->scatter_density(radius, expand != 0, avg_color != 0);
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_export_point_leaves(gbvdb_grid g, int32_t* pnode_out, int64_t cap, int64_t* offsets,
+                                       int64_t cap_offsets, float* points, int64_t cap_points) {
+    GBVDB_GUARD(g)
+    if (g->ins_n < 0) return GBVDB_INVALID_ARG;
+    long long n = g->ins_n, nl = g->ins_nleaf;
+    if ((pnode_out && cap < n) || (offsets && cap_offsets < nl + 1)) return GBVDB_CAPACITY;
+    if (pnode_out && n)
+        g->check(cudaMemcpyAsync(pnode_out, g->pnode.p, (size_t)n * 4, cudaMemcpyDeviceToHost, g->stream), "export");
+    std::vector<uint32_t> off((size_t)nl + 1, 0);
+    g->check(cudaMemcpyAsync(off.data(), g->goff.p, (size_t)(nl + 1) * 4, cudaMemcpyDeviceToHost, g->stream), "export");
+    g->sync();
+    if (offsets)
+        for (long long i = 0; i <= nl; i++) offsets[i] = off[(size_t)i];
+    long long tot = off[(size_t)nl];
+    if (points) {
+        if (cap_points < tot * 3) return GBVDB_CAPACITY;
+        if (tot)
+            g->check(cudaMemcpyAsync(points, g->psort.p, (size_t)tot * 12, cudaMemcpyDeviceToHost, g->stream), "export");
+        g->sync();
+    }
+    return GBVDB_OK;
     GBVDB_END(g)
 }
 
@@ -1344,11 +1439,10 @@ gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off,
     GBVDB_END(g)
 }
 
-static float3 f3(const float* v) { return v ? make_float3(v[0], v[1], v[2]) : make_float3(0, 0, 0); }
-
 gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3]) {
     GBVDB_GUARD(g)
-    g->nbr_count = -1;  // the neighbour table describes the previous topology
+    g->nbr_count = -1;  // the neighbour table and point groups describe the previous topology
+    g->ins_n = -1;
     return g->rebuild(n, radius, f3(orig), false, 0);
     GBVDB_END(g)
 }
@@ -1356,6 +1450,7 @@ gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const
 gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3], int min_depth) {
     GBVDB_GUARD(g)
     g->nbr_count = -1;
+    g->ins_n = -1;
     return g->rebuild(n, radius, f3(orig), true, min_depth);
     GBVDB_END(g)
 }
@@ -1648,7 +1743,8 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
-                            &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table};
+                            &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
+                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

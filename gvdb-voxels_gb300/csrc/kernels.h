@@ -76,6 +76,13 @@ void launch_apron_faces(const Node* leaves, const AtlasNode* amap, int used, int
                         int esize, void* interior, void* apron, cudaStream_t s);
 void launch_smooth(const AtlasNode* amap, int used, float* interior, const float* apron, float p1, float p2,
                    cudaStream_t s);
+// legacy InsertPoints (leaf of each point, rank, per-leaf counts), SortPoints and ScatterDensity
+void launch_insert_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, int* pnode, uint32_t* pndx,
+                          uint32_t* gcnt, cudaStream_t s);
+void launch_sort_points(PointSrc p, float3 trans, const int* pnode, const uint32_t* pndx, const uint32_t* goff,
+                        float* out3, cudaStream_t s);
+void launch_scatter_density(const Node* leaves, long long nleaf, const uint32_t* goff, const float* pts3, float radius,
+                            int expand, int res0, int ax, int ay, float* interior, float* apron, cudaStream_t s);
 // deterministic FP64 channel sum: per-slot partials, then one fixed-order block
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s);

@@ -626,6 +626,102 @@ __global__ void k_gather_lists(TreeView t, const int* __restrict__ linked, const
     write_tile<T>(gp, tile, interior + (size_t)slot * 4096);
 }
 
+// ---- legacy InsertPoints + ScatterDensity (brick binning and a splat) ----
+
+// gvdbInsertPoints (PT.cuh:19-35): the leaf holding each point (w = p + trans; NOHIT,
+// negative or outside every leaf -> -1) and the point's rank among its leaf's points
+__global__ void k_insert_points(TreeView t, LeafGrid lg, PointSrc p, float3 trans, int* __restrict__ pnode,
+                                uint32_t* __restrict__ pndx, uint32_t* __restrict__ gcnt) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        int leaf = -1;
+        if (z != kNoHit) {
+            const float w[3] = {fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z)};
+            if (w[0] >= 0 && w[1] >= 0 && w[2] >= 0) {
+                const int vx = (int)w[0], vy = (int)w[1], vz = (int)w[2];
+                long long l = lg.cells ? lookup_leaf(lg, t, vx, vy, vz) : get_leaf_at_voxel(t, vx, vy, vz);
+                leaf = (int)l;
+            }
+        }
+        pnode[i] = leaf;
+        if (leaf >= 0) pndx[i] = atomicAdd(gcnt + leaf, 1u);
+    }
+}
+
+// gvdbSortPoints (PT.cuh:54-68): points grouped by leaf, w = p + trans
+__global__ void k_sort_points(PointSrc p, float3 trans, const int* __restrict__ pnode, const uint32_t* __restrict__ pndx,
+                              const uint32_t* __restrict__ goff, float* __restrict__ out3) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        const int leaf = pnode[i];
+        if (leaf < 0) continue;
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        float* o = out3 + 3ull * (goff[leaf] + pndx[i]);
+        o[0] = fadd(x, trans.x);
+        o[1] = fadd(y, trans.y);
+        o[2] = fadd(z, trans.z);
+    }
+}
+
+// distFunc (PT.cuh:516-523) with one rounding per operation in source order:
+// c = (bx*bx + by*by + bz*bz) / (r*r), 1 + c*(-3 + c*(3 - c))
+__device__ __forceinline__ float dist_func(float px, float py, float pz, float bx, float by, float bz, float r) {
+    bx = fsub(bx, px);
+    by = fsub(by, py);
+    bz = fsub(bz, pz);
+    const float d2 = fadd(fadd(__fmul_rn(bx, bx), __fmul_rn(by, by)), __fmul_rn(bz, bz));
+    const float c = __fdiv_rn(d2, __fmul_rn(r, r));
+    // the source's 1.0 is a double literal: the last addition is in double, then rounded
+    return __double2float_rn(__dadd_rn(1.0, (double)__fmul_rn(c, fadd(-3.0f, __fmul_rn(c, fsub(3.0f, c))))));
+}
+
+// gvdbScatterPointDensity (PT.cuh:525-571), one block per leaf over its grouped points:
+// each point adds distFunc to the voxel it lies in and, with `expand`, to that voxel's
+// six face neighbours inside the leaf's padded 18^3 brick (apron included), so every
+// write stays in one slot.  Contributions are summed in FP64 in shared memory and added
+// to the stored values once (the reference adds them one by one with unsynchronised
+// read-modify-writes of the atlas).
+__global__ void __launch_bounds__(256) k_scatter_density(const Node* __restrict__ leaves, long long nleaf,
+                                                         const uint32_t* __restrict__ goff,
+                                                         const float* __restrict__ pts3, float radius, int expand,
+                                                         int res0, int ax, int ay, float* __restrict__ interior,
+                                                         float* __restrict__ apron) {
+    __shared__ double acc[18 * 18 * 18];
+    const long long leaf = blockIdx.x;
+    if (leaf >= nleaf) return;
+    const uint32_t beg = goff[leaf], end = goff[leaf + 1];
+    if (beg == end) return;
+    const Node nd = leaves[leaf];
+    const int slot = slot_of_value(nd.value, ax, ay);
+    if (slot < 0) return;
+    for (int v = threadIdx.x; v < 5832; v += blockDim.x) acc[v] = 0.0;
+    __syncthreads();
+    const float vmx = (float)nd.pos[0], vmy = (float)nd.pos[1], vmz = (float)nd.pos[2];
+    const int nb[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+    const int nk = expand ? 7 : 1;
+    for (uint32_t j = beg + threadIdx.x; j < end; j += blockDim.x) {
+        const float px = fsub(pts3[3ull * j], vmx), py = fsub(pts3[3ull * j + 1], vmy), pz = fsub(pts3[3ull * j + 2], vmz);
+        const int ix = (int)px, iy = (int)py, iz = (int)pz;
+        if (px < 0 || py < 0 || pz < 0 || ix >= res0 || iy >= res0 || iz >= res0) continue;
+        for (int k = 0; k < nk; k++) {
+            const int qx = ix + nb[k][0], qy = iy + nb[k][1], qz = iz + nb[k][2];
+            const float f = dist_func(px, py, pz, (float)qx, (float)qy, (float)qz, radius);
+            atomicAdd(&acc[((qz + 1) * 18 + (qy + 1)) * 18 + (qx + 1)], (double)f);
+        }
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < 5832; v += blockDim.x) {
+        const double a = acc[v];
+        if (a == 0.0) continue;
+        const int x = v % 18, y = (v / 18) % 18, z = v / 324;
+        float* dst = (x >= 1 && x <= 16 && y >= 1 && y <= 16 && z >= 1 && z <= 16)
+                         ? interior + (size_t)slot * 4096 + ((z - 1) << 8) + ((y - 1) << 4) + (x - 1)
+                         : apron + (size_t)slot * kApronStride + apron_index(x, y, z);
+        *dst = __double2float_rn(__dadd_rn((double)*dst, a));
+    }
+}
+
 inline unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 inline unsigned gs_blocks(long long n, int t) {
     long long b = (n + t - 1) / t;
@@ -634,6 +730,22 @@ inline unsigned gs_blocks(long long n, int t) {
 }
 }  // namespace
 
+void launch_insert_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, int* pnode, uint32_t* pndx,
+                          uint32_t* gcnt, cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_insert_points<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, pnode, pndx, gcnt);
+}
+void launch_sort_points(PointSrc p, float3 trans, const int* pnode, const uint32_t* pndx, const uint32_t* goff,
+                        float* out3, cudaStream_t s) {
+    if (p.n <= 0) return;
+    k_sort_points<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, pnode, pndx, goff, out3);
+}
+void launch_scatter_density(const Node* leaves, long long nleaf, const uint32_t* goff, const float* pts3, float radius,
+                            int expand, int res0, int ax, int ay, float* interior, float* apron, cudaStream_t s) {
+    if (nleaf <= 0) return;
+    k_scatter_density<<<(unsigned)nleaf, 256, 0, s>>>(leaves, nleaf, goff, pts3, radius, expand, res0, ax, ay,
+                                                      interior, apron);
+}
 void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s) {
     if (n <= 0) return;
     k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);

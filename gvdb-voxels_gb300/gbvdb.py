@@ -38,7 +38,8 @@ EXPORTS = [
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
-    "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16",
+    "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
+    "gbvdb_export_point_leaves",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -121,6 +122,9 @@ def load(path=LIB_PATH):
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
     L.gbvdb_update_neighbors.argtypes = [vp]
+    L.gbvdb_insert_points.argtypes = [vp, i64, fp, i32]
+    L.gbvdb_scatter_density.argtypes = [vp, i64, f32, f32, fp, i32, i32]
+    L.gbvdb_export_point_leaves.argtypes = [vp, vp, i64, vp, i64, vp, i64]
     L.gbvdb_insert_points_subcell_fp16.argtypes = [vp, i32, i64, f32, fp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_gather_levelset_fp16.argtypes = [vp, i32, i64, f32, fp, i64, i32, i32]
     L.gbvdb_export_neighbors.argtypes = [vp, vp, i64]
@@ -344,6 +348,27 @@ class Grid:
             self._h, off.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nsub + 1,
             pts.ctypes.data if total_len > 0 else None, total_len), "export_subcells")
         return off, pts
+
+    def insert_points(self, n, trans=(0, 0, 0), prefix=True):
+        """Legacy InsertPoints (gvdb_volume_gvdb.cpp:5219-5267)."""
+        self._check(self.L.gbvdb_insert_points(self._h, n, _f3(trans), int(prefix)), "insert_points")
+
+    def scatter_density(self, n, radius, amp=1.0, trans=(0, 0, 0), expand=True, avg_color=False):
+        """Legacy ScatterDensity (gvdb_volume_gvdb.cpp:5624-5660) into channel 0."""
+        return self._check(self.L.gbvdb_scatter_density(self._h, n, radius, amp, _f3(trans), int(expand),
+                                                        int(avg_color)), "scatter_density")
+
+    def point_leaves(self, n):
+        """(leaf per point, group offsets per leaf, grouped points) of the last insert_points."""
+        nl = self.node_counts()[0][0]
+        pnode = np.zeros(max(n, 1), dtype=np.int32)
+        off = np.zeros(nl + 1, dtype=np.int64)
+        self._check(self.L.gbvdb_export_point_leaves(self._h, pnode.ctypes.data, n, off.ctypes.data, nl + 1, None, 0),
+                    "export_point_leaves")
+        pts = np.zeros((max(int(off[-1]), 1), 3), dtype=np.float32)
+        self._check(self.L.gbvdb_export_point_leaves(self._h, None, 0, None, 0, pts.ctypes.data, pts.size),
+                    "export_point_leaves")
+        return pnode[:n], off, pts[:int(off[-1])]
 
     def update_neighbors(self):
         """UpdateNeighbors (gvdb_volume_gvdb.cpp:2527-2556)."""

@@ -120,6 +120,21 @@ GBVDB_API gbvdb_status gbvdb_insert_points_subcell_fp16(gbvdb_grid g, int subcel
  * v = min(3, min_j(|p_j - v| - radius)) over the stored positions, no accumulation */
 GBVDB_API gbvdb_status gbvdb_gather_levelset_fp16(gbvdb_grid g, int subcell_size, int64_t n, float radius,
                                                   const float trans[3], int64_t sc_len, int chan, int clr_chan);
+/* Legacy InsertPoints(num_pnts, trans, bPrefix) (gvdb_volume_gvdb.cpp:5219-5267,
+ * cuda_gvdb_particles.cuh:19-68): the leaf holding each point (w = p + trans, -1 where none)
+ * and the points grouped by leaf. */
+GBVDB_API gbvdb_status gbvdb_insert_points(gbvdb_grid g, int64_t n, const float trans[3], int prefix);
+/* Legacy ScatterDensity(num_pnts, radius, amp, trans, expand, avgColor) (gvdb_volume_gvdb.cpp
+ * :5624-5660, cuda_gvdb_particles.cuh:516-571): channel 0 (FP32) += distFunc of every point
+ * grouped by the last InsertPoints at the voxel it lies in (and its six face neighbours with
+ * expand), c = d^2 / r^2, 1 + c*(-3 + c*(3 - c)); amp is unused as in the reference kernel,
+ * colour averaging is not supported. */
+GBVDB_API gbvdb_status gbvdb_scatter_density(gbvdb_grid g, int64_t n, float radius, float amp, const float trans[3],
+                                             int expand, int avg_color);
+/* the last InsertPoints: leaf per point (n int32), group offsets (leaves + 1) and grouped points
+ * (float3; order inside a group unspecified, as the reference's atomic ranks); NULL skips one */
+GBVDB_API gbvdb_status gbvdb_export_point_leaves(gbvdb_grid g, int32_t* pnode, int64_t cap, int64_t* offsets,
+                                                 int64_t cap_offsets, float* points, int64_t cap_points);
 /* UpdateApron(chan, boundval) (gvdb_volume_gvdb.cpp:4418-4457, cuda_gvdb_operators.cuh:72-131) */
 GBVDB_API gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval);
 /* ClearChannel / FillChannel (gvdb_volume_gvdb.cpp:2456-2485) for the assigned slots */

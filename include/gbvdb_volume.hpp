@@ -139,6 +139,16 @@ class VolumeGVDB {
         chk(gbvdb_gather_levelset_fp16(g_, subcell_size, num_pnts, radius, t, pSCPntsLength, chanLevelset, chanClr),
             "GatherLevelSet_FP16");
     }
+    // legacy InsertPoints / ScatterDensity (VG.cpp:5219-5267, 5624-5660)
+    void InsertPoints(int num_pnts, Vector3DF trans, bool bPrefix = false) {
+        float t[3] = {trans.x, trans.y, trans.z};
+        chk(gbvdb_insert_points(g_, num_pnts, t, bPrefix ? 1 : 0), "InsertPoints");
+    }
+    void ScatterDensity(int num_pnts, float radius, float amp, Vector3DF trans, bool expand = true,
+                        bool avgColor = false) {
+        float t[3] = {trans.x, trans.y, trans.z};
+        chk(gbvdb_scatter_density(g_, num_pnts, radius, amp, t, expand ? 1 : 0, avgColor ? 1 : 0), "ScatterDensity");
+    }
     // UpdateApron (VG.cpp:4411-4457)
     void UpdateApron(uchar chan, float boundval = 0.0f, bool changeCtx = true) {
         (void)changeCtx;

@@ -1140,3 +1140,73 @@ void og_smooth_f32(const OGrid* g, float* bricks, float p1, float p2) {
     }
     free(src);
 }
+
+/* ------------------------------------------------------------------------ */
+/* legacy InsertPoints + ScatterDensity                                      */
+
+/* gvdbInsertPoints (PT.cuh:19-35): leaf of each point (w = p + trans; NOHIT, negative or
+ * outside every leaf -> -1); counts[leaf] = points in it */
+void og_insert_points(const OGrid* g, const void* posv, int64_t n, int stride, int off, const float trans[3],
+                      int32_t* pnode, int64_t* counts) {
+    const char* pos = (const char*)posv;
+    for (size_t l = 0; l < g->ncnt[0]; l++) counts[l] = 0;
+    for (int64_t i = 0; i < n; i++) {
+        float p[3];
+        load_point(pos, i, stride, off, p);
+        int64_t leaf = -1;
+        if (p[2] != NOHIT) {
+            float w[3] = {p[0] + trans[0], p[1] + trans[1], p[2] + trans[2]};
+            if (w[0] >= 0 && w[1] >= 0 && w[2] >= 0) {
+                int32_t v[3] = {(int32_t)w[0], (int32_t)w[1], (int32_t)w[2]};
+                leaf = get_leaf_at_voxel(g, v);
+            }
+        }
+        pnode[i] = (int32_t)leaf;
+        if (leaf >= 0) counts[leaf]++;
+    }
+}
+
+/* distFunc (PT.cuh:516-523): c = (bx*bx + by*by + bz*bz) / (r*r) in FP32, then
+ * 1.0 + c*(-3 + c*(3 - c)) with the double literal's last addition in double */
+static float dist_func(float px, float py, float pz, float bx, float by, float bz, float r) {
+    bx -= px;
+    by -= py;
+    bz -= pz;
+    float d2 = bx * bx + by * by;
+    d2 = d2 + bz * bz;
+    float c = d2 / (r * r);
+    float t = c * (-3.0f + c * (3.0f - c));
+    return (float)(1.0 + (double)t);
+}
+
+/* gvdbScatterPointDensity (PT.cuh:525-571) into channel 0 (FP64 here): every point of a
+ * leaf with an atlas slot adds distFunc at the voxel it lies in and, with expand, at the
+ * six face neighbours (inside the padded brick, apron included) */
+void og_scatter_density(OGrid* g, const void* posv, int64_t n, int stride, int off, const float trans[3],
+                        float radius, int expand) {
+    const char* pos = (const char*)posv;
+    double* atl = g->chan[0].data;
+    const int nb[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+    const int res0 = g->res[0];
+    for (int64_t i = 0; i < n; i++) {
+        float p[3];
+        load_point(pos, i, stride, off, p);
+        if (p[2] == NOHIT) continue;
+        float w[3] = {p[0] + trans[0], p[1] + trans[1], p[2] + trans[2]};
+        if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
+        int32_t v[3] = {(int32_t)w[0], (int32_t)w[1], (int32_t)w[2]};
+        int64_t leaf = get_leaf_at_voxel(g, v);
+        if (leaf < 0) continue;
+        const ONode* nd = &g->nodes[0][leaf];
+        int64_t s = leaf_slot(g, nd);
+        if (s < 0) continue;
+        float lp[3] = {w[0] - (float)nd->pos[0], w[1] - (float)nd->pos[1], w[2] - (float)nd->pos[2]};
+        int ix = (int)lp[0], iy = (int)lp[1], iz = (int)lp[2];
+        if (lp[0] < 0 || lp[1] < 0 || lp[2] < 0 || ix >= res0 || iy >= res0 || iz >= res0) continue;
+        for (int k = 0; k < (expand ? 7 : 1); k++) {
+            int qx = ix + nb[k][0], qy = iy + nb[k][1], qz = iz + nb[k][2];
+            float f = dist_func(lp[0], lp[1], lp[2], (float)qx, (float)qy, (float)qz, radius);
+            atl[(size_t)s * 5832 + ((size_t)(qz + 1) * 18 + (qy + 1)) * 18 + (qx + 1)] += (double)f;
+        }
+    }
+}

@@ -100,6 +100,8 @@ def lib():
         L.og_save_vbx.restype = i32
         L.og_save_vbx.argtypes = [vp, ctypes.c_char_p]
         L.og_update_neighbors.argtypes = [vp, vp]
+        L.og_insert_points.argtypes = [vp, vp, i64, i32, i32, fp3, vp, vp]
+        L.og_scatter_density.argtypes = [vp, vp, i64, i32, i32, fp3, f32, i32]
         L.og_apron_faces_f32.argtypes = [vp, vp, vp]
         L.og_apron_full_f32.argtypes = [vp, vp, f32]
         L.og_smooth_f32.argtypes = [vp, vp, f32, f32]
@@ -256,6 +258,19 @@ class OracleGrid:
 
     def checksum(self, chan=0):
         return float(lib().og_checksum(self._h, chan))
+
+    def insert_points(self, points, trans=(0, 0, 0)):
+        """Legacy InsertPoints restated: (leaf per point, point count per leaf)."""
+        p, n, stride = self._pts(points)
+        pnode = np.zeros(n, dtype=np.int32)
+        counts = np.zeros(max(self.node_count(0), 1), dtype=np.int64)
+        lib().og_insert_points(self._h, p.ctypes.data, n, stride, 0, _f3(trans), pnode.ctypes.data, counts.ctypes.data)
+        return pnode, counts[:self.node_count(0)]
+
+    def scatter_density(self, points, radius, expand=True, trans=(0, 0, 0)):
+        """Legacy ScatterDensity restated into channel 0 (FP64)."""
+        p, n, stride = self._pts(points)
+        lib().og_scatter_density(self._h, p.ctypes.data, n, stride, 0, _f3(trans), float(radius), int(expand))
 
     def neighbors(self):
         """UpdateNeighbors restated: (leaves, 6) pool indices (-x, -y, -z, +x, +y, +z), -1 = none."""
