@@ -44,6 +44,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def slowest_rank_ms(ms, world, device):
+    """The timed region's length is the slowest replica's (max over ranks; no data exchange)."""
+    if world <= 1:
+        return float(ms)
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(points_per_rank, ms, world):
+    """Whole-job points/s: every rank processed its own frame of points_per_rank points."""
+    return world * points_per_rank / (ms / 1000.0)
+
+
 def fluid_frames(seed):
     import datasets
 
@@ -488,12 +504,8 @@ def bench_ours(args):
         wall = time.perf_counter() - t0
     dev_ms = ev0.elapsed_time(ev1)
     launches = grid.stats()["launches"] - l0
-    ms = dev_ms / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * N_FLUID / (ms / 1000.0)
+    ms = slowest_rank_ms(dev_ms / args.steps, world, dev)
+    value = replica_throughput(N_FLUID, ms, world)
 
     # end to end: host positions -> device, frame, checksum -> host.  Every step copies
     # its frame's positions from pinned host memory; the copy of frame k+1 runs on a copy
@@ -530,12 +542,8 @@ def bench_ours(args):
     e2e_run(args.steps)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": world * N_FLUID / (e2e_ms / 1000.0), "unit": "points/s",
+    e2e_ms = slowest_rank_ms(e0.elapsed_time(e1) / args.steps, world, dev)
+    e2e = {"value": replica_throughput(N_FLUID, e2e_ms, world), "unit": "points/s",
            "h2d_bytes_per_step": N_FLUID * 12, "d2h_bytes_per_step": 8}
 
     # per-stage times and the gather roofline (separate pass: profiling synchronizes per call)
