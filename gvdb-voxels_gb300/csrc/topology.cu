@@ -135,6 +135,12 @@ __device__ __forceinline__ void touch_bit(uint32_t* sbm, bool use_smem, uint32_t
 // ranges of node positions at a level, a warp prefix sum over the lanes' counts
 // lays all (point, position) items out in one list, and the lanes then take
 // consecutive items, so that boxes of 1 to 8 positions do not leave lanes idle.
+// x / 2^lg * 2^lg with C truncation toward zero
+__device__ __forceinline__ int trunc_mult(int x, int lg) {
+    const long long v = x;
+    return (int)(v >= 0 ? (v >> lg) << lg : -(((-v) >> lg) << lg));
+}
+
 __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth, int3 rlo,
                             int3 rhi, KeyDomains dom, uint32_t* touched, long long nwords, int* err) {
     extern __shared__ uint32_t sbm[];
@@ -170,12 +176,12 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
             const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
 #pragma unroll
             for (int a = 0; a < 3; a++) {
-                lo[a] = bmin[a] / rr * rr;  // C truncation, as the reference
-                int hi = bmax[a] / rr * rr;
+                lo[a] = trunc_mult(bmin[a], lg);  // x / rr * rr with C truncation, as the reference
+                int hi = trunc_mult(bmax[a], lg);
                 // positions outside the root are skipped: clip the range to it
-                if (lo[a] < rl[a]) lo[a] += (rl[a] - lo[a] + rr - 1) / rr * rr;
-                if (hi > rh[a]) hi -= (hi - rh[a] + rr - 1) / rr * rr;
-                cnt[a] = valid && hi >= lo[a] ? (hi - lo[a]) / rr + 1 : 0;
+                if (lo[a] < rl[a]) lo[a] += ((rl[a] - lo[a] + rr - 1) >> lg) << lg;
+                if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
+                cnt[a] = valid && hi >= lo[a] ? ((hi - lo[a]) >> lg) + 1 : 0;
             }
             long long mine64 = (long long)cnt[0] * cnt[1] * cnt[2];
             if (mine64 > (1ll << 26)) {  // keeps the warp's item count within int
@@ -206,9 +212,20 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
                 const int olx = __shfl_sync(0xFFFFFFFFu, lo[0], owner);
                 const int oly = __shfl_sync(0xFFFFFFFFu, lo[1], owner);
                 const int olz = __shfl_sync(0xFFFFFFFFu, lo[2], owner);
+                const bool small = __all_sync(0xFFFFFFFFu, ocx <= 2 && ocy <= 2);
                 if (k >= total) continue;
                 const int li = k - excl;
-                const int ix = li % ocx, iy = (li / ocx) % ocy, iz = li / (ocx * ocy);
+                int ix, iy, iz;
+                if (small) {  // 1 or 2 positions along x and y (nearly every box): shifts
+                    const int sx = ocx - 1, sy = ocy - 1, t2 = li >> sx;
+                    ix = li & sx;
+                    iy = t2 & sy;
+                    iz = t2 >> sy;
+                } else {
+                    ix = li % ocx;
+                    iy = (li / ocx) % ocy;
+                    iz = li / (ocx * ocy);
+                }
                 const int nx = olx + ix * rr, ny = oly + iy * rr, nz = olz + iz * rr;
                 // guard: positions outside the root (the reference aliases them)
                 if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;

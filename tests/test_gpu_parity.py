@@ -239,3 +239,55 @@ def test_fp16_subcells_levelset(gpu_lib):
     _, g32 = H.run_gpu(None, **kw)
     assert not np.array_equal(g32[-1]["bricks"], g[-1]["bricks"])
     assert np.abs(g32[-1]["bricks"].astype(np.float64) - g[-1]["bricks"]).max() < 0.05
+
+
+def test_apron_after_other_interior_writers(gpu_lib):
+    """UpdateApron copies the interiors as they are now, whoever wrote them last: after a
+    gather (boundary planes kept beside the bricks), after FillChannel, and after the
+    caller wrote the interior through gbvdb_get_atlas_device."""
+    import ctypes
+
+    import torch
+
+    import gbvdb
+
+    pts = datasets.shell(30_000, seed=91)
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0, gbvdb.T_FLOAT)
+    n = g.set_points(torch.from_numpy(pts).cuda())
+    g.rebuild_topology(n, 1.0)
+    g.update_atlas()
+    _, ln = g.insert_points_subcell(4, n, 1.0)
+    g.gather_density(4, n, 1.0, (0, 0, 0), ln)
+    g.update_apron(0, 0.0)
+    snap = {"bricks": g.atlas_bricks(0), "amap": g.atlas_map()}
+    H.check_apron_self(snap, 0.0)
+    g.fill_channel(0, 0.75)
+    g.update_apron(0, 0.25)
+    snap = {"bricks": g.atlas_bricks(0), "amap": g.atlas_map()}
+    H.check_apron_self(snap, 0.25)
+    assert np.all(snap["bricks"][:, 1:17, 1:17, 1:17] == 0.75)
+    # the caller writes the interior of every slot: voxel value = slot + x / 16
+    ip, ap = ctypes.c_void_p(), ctypes.c_void_p()
+    assert g.L.gbvdb_get_atlas_device(g._h, 0, ctypes.byref(ip), ctypes.byref(ap)) == gbvdb.OK
+    used = g.atlas_info(0)["used"]
+    vals = (torch.arange(used, dtype=torch.float32, device="cuda")[:, None]
+            + (torch.arange(4096, device="cuda") % 16).float()[None, :] / 16.0).contiguous()
+
+
+    class _Dev:  # a zero-copy torch view of the channel's interior storage
+        __cuda_array_interface__ = {"shape": (used, 4096), "typestr": "<f4", "data": (ip.value, False),
+                                    "version": 3}
+
+    interior = torch.as_tensor(_Dev(), device="cuda")
+    torch.cuda.synchronize()
+    interior.copy_(vals)
+    torch.cuda.synchronize()
+    g.gather_density(4, n, 1.0, (0, 0, 0), ln)  # overwritten by a gather, then written again below
+    torch.cuda.synchronize()
+    interior.copy_(vals)
+    torch.cuda.synchronize()
+    g.update_apron(0, -1.0)
+    snap = {"bricks": g.atlas_bricks(0), "amap": g.atlas_map()}
+    H.check_apron_self(snap, -1.0)
+    assert np.array_equal(snap["bricks"][:, 1:17, 1:17, 1:17].reshape(used, -1), vals.cpu().numpy())
