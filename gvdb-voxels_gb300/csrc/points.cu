@@ -171,15 +171,36 @@ __device__ __forceinline__ int member_bits(int ox, int oy, int oz) {
 __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const int* __restrict__ bin_of,
                               const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
                               float4* __restrict__ sorted) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
-        int b = bin_of[i];
-        if (b < 0) continue;
-        float x, y, z;
-        load_pos(p.base, i, p.stride, p.off, x, y, z);
-        float w[3] = {fadd(x, trans.x), fadd(y, trans.y), fadd(z, trans.z)};
-        float ps[3];
-        stored_pos(qz, w, ps);
-        sorted[bin_off[b] + rank_of[i]] = make_float4(ps[0], ps[1], ps[2], __int_as_float(pack_ranges(w, ps, R)));
+    // kU points per thread per step, their loads issued together (the pass is bound by the
+    // latency of the dependent bin_of -> bin_off loads)
+    constexpr int kU = 4;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+        int b[kU];
+        uint32_t rk[kU], off[kU];
+        float x[kU], y[kU], z[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const long long i = i0 + u * stride;
+            b[u] = i < p.n ? bin_of[i] : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const long long i = i0 + u * stride;
+            if (b[u] >= 0) {
+                rk[u] = rank_of[i];
+                off[u] = bin_off[b[u]];
+                load_pos(p.base, i, p.stride, p.off, x[u], y[u], z[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            if (b[u] < 0) continue;
+            float w[3] = {fadd(x[u], trans.x), fadd(y[u], trans.y), fadd(z[u], trans.z)};
+            float ps[3];
+            stored_pos(qz, w, ps);
+            sorted[off[u] + rk[u]] = make_float4(ps[0], ps[1], ps[2], __int_as_float(pack_ranges(w, ps, R)));
+        }
     }
 }
 
