@@ -91,6 +91,7 @@ struct gbvdb_grid_s {
     // pools
     DevBuf nodes[kMaxLev], clist[kMaxLev];
     long long ncnt[kMaxLev] = {0}, nused[kMaxLev] = {0};
+    bool nused0_stale = false;  // nused[0] awaits a count of the flagged leaves
     int rebuild_topo = 1;
     int curr_depth = -1;
     int last_depth = 0;
@@ -229,6 +230,7 @@ struct gbvdb_grid_s {
 
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
+        nused0_stale = false;
         nbr_count = -1;
         ins_n = -1;
         lgdom_init = false;
@@ -520,7 +522,15 @@ struct gbvdb_grid_s {
             check_launch("delink_upper");
         }
         build_leaf_grid();
-        // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148)
+        // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148): counted when next
+        // needed (UpdateAtlas counts the flagged leaves anyway), not with a readback here
+        nused0_stale = true;
+        mark();
+    }
+
+    // the flagged-leaf count, when an incremental rebuild left it to be counted
+    void refresh_nused0() {
+        if (!nused0_stale) return;
         check(cudaMemsetAsync(ptr<char>(misc) + 64, 0, 8, stream), "count clear");
         launch_count_flags(ptr<Node>(nodes[0]), ncnt[0], reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 64),
                            stream);
@@ -528,7 +538,7 @@ struct gbvdb_grid_s {
         unsigned long long used = 0;
         readback(&used, ptr<char>(misc) + 64, 8);
         nused[0] = (long long)used;
-        mark();
+        nused0_stale = false;
     }
 
     gbvdb_status rebuild(long long n, float radius, float3 orig, bool accumulate, int min_depth) {
@@ -592,7 +602,8 @@ struct gbvdb_grid_s {
     gbvdb_status update_atlas() {  // UpdateAtlas (VG.cpp:2630-2704)
         if (!ch[0].used) throw StatusError{GBVDB_INVALID_ARG, "no atlas channel"};
         long long total = ncnt[0];
-        long long used = nused[0];
+        // the flagged-leaf count is F below; an earlier count is only used when it is current
+        long long used = nused0_stale ? 0 : nused[0];
         atlas_last = 0;
         long long layer = (long long)ax * ay;
         if (used > layer * az) az = (int)std::ceil((double)((float)used / (float)layer));
@@ -609,6 +620,10 @@ struct gbvdb_grid_s {
             F = f;
         }
         if (F > layer * az) az = (int)std::ceil((double)((float)F / (float)layer));  // AtlasAlloc growth, AL.cpp:695-698
+        if (nused0_stale) {  // F is the flagged-leaf count
+            nused[0] = F;
+            nused0_stale = false;
+        }
         long long slots = layer * az;
         resize_channels(slots);
         grow(amap, (size_t)slots * sizeof(AtlasNode));
@@ -643,6 +658,7 @@ struct gbvdb_grid_s {
         if (sc != 4 || log2dim[0] != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 with 16^3 bricks only"};
         if (!(R >= 0)) throw StatusError{GBVDB_INVALID_ARG, "negative radius"};
         if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
+        refresh_nused0();
         if (nused[0] == 0) return GBVDB_NOOP;  // VG.cpp:4973-4977
         stage_begin();
         build_linked();
@@ -774,6 +790,7 @@ struct gbvdb_grid_s {
         if (ch[chan].dtype != GBVDB_T_FLOAT && ch[chan].dtype != GBVDB_T_HALF && ch[chan].dtype != GBVDB_T_BFLOAT16)
             throw StatusError{GBVDB_NOT_SUPPORTED, "gathers write float, half or bfloat16 channels"};
         if (clr) throw StatusError{GBVDB_NOT_SUPPORTED, "colour gathers are not implemented"};
+        refresh_nused0();
         if (nused[0] == 0) return GBVDB_NOOP;                       // VG.cpp:5321-5322, 5350-5351
         if (mode == 0 && sc_len_arg == 0) return GBVDB_NOOP;        // VG.cpp:5321
         if (!sc_valid || sc_nleaf != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "InsertPointsSubcell is stale"};
@@ -1566,7 +1583,10 @@ gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used) 
     GBVDB_GUARD(g)
     for (int l = 0; l < kMaxLev; l++) {
         if (total) total[l] = g->ncnt[l];
-        if (used) used[l] = g->nused[l];
+        if (used) {
+            if (l == 0) g->refresh_nused0();
+            used[l] = g->nused[l];
+        }
     }
     return GBVDB_OK;
     GBVDB_END(g)
