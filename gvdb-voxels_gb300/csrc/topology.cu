@@ -169,7 +169,9 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
                 bmax[a] = (int)fadd(fi, hr);
             }
         }
-        for (int lev = 0; lev < depth; lev++) {
+        // level 0 only: the box positions of every upper level are the parents of the
+        // level-0 ones (k_touch_up), since the ranges nest
+        for (int lev = 0; lev < 1; lev++) {
             const int lg = t.lgrange[lev];
             const int rr = 1 << lg;
             int lo[3], cnt[3];
@@ -241,6 +243,33 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
             uint32_t v = sbm[k];
             if (v && (__ldcg(touched + k) & v) != v) atomicOr(touched + k, v);
         }
+    }
+}
+
+// Box positions of level lev from those of lev-1: every touched position's parent.  For
+// one box, trunc(b / R_lev) * R_lev .. trunc(e / R_lev) * R_lev is the set of parents
+// of trunc(b / R_lev-1) * R_lev-1 .. trunc(e / R_lev-1) * R_lev-1 once both are clipped
+// to the root (coordinates >= 0, where truncation is floor and the ranges nest).
+__global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_t* touched, int* err) {
+    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
+    if (w >= nw) return;
+    uint32_t bits = touched[w0 + w];
+    while (bits) {
+        int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        long long li = w * 32 + b;
+        int rz = (int)(li % child.dim[2]);
+        long long q = li / child.dim[2];
+        int ry = (int)(q % child.dim[1]);
+        int rx = (int)(q / child.dim[1]);
+        long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
+                               (child.lo[2] + rz) >> lgres);
+        if (pb < 0) {
+            atomicOr(err, 1);
+            continue;
+        }
+        set_bit(touched, pb);
     }
 }
 
@@ -461,12 +490,16 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
                      uint32_t* bitmap, int* markers, int* err, cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
-    long long nwords = 0;
-    for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
+    // the points touch level 0 (its bits start at bit 0); the upper levels follow from it
+    long long nwords = (dom.d[0].bitbase + dom.d[0].nbits + 31) >> 5;
     size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
     // fewer, fuller blocks when each one flushes a shared bitmap
     unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
     k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
+    for (int lev = 1; lev < depth; lev++) {
+        long long nw = (dom.d[lev - 1].nbits + 31) >> 5;
+        k_touch_up<<<blocks_for(nw, 128), 128, 0, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
+    }
     for (int lev = 0; lev < depth; lev++) {
         long long nw = (dom.d[lev].nbits + 31) >> 5;
         k_resolve_touched<<<blocks_for(nw, 128), 128, 0, s>>>(t, lg, lev, dom.d[lev], touched, bitmap, markers);
