@@ -251,52 +251,50 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
 // of trunc(b / R_lev-1) * R_lev-1 .. trunc(e / R_lev-1) * R_lev-1 once both are clipped
 // to the root (coordinates >= 0, where truncation is floor and the ranges nest).
 __global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_t* touched, int* err) {
-    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
+    // one thread per bit of the child level (a warp per bitmap word)
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = g >> 5, w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
     if (w >= nw) return;
-    uint32_t bits = touched[w0 + w];
-    while (bits) {
-        int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        long long li = w * 32 + b;
-        int rz = (int)(li % child.dim[2]);
-        long long q = li / child.dim[2];
-        int ry = (int)(q % child.dim[1]);
-        int rx = (int)(q / child.dim[1]);
-        long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
-                               (child.lo[2] + rz) >> lgres);
-        if (pb < 0) {
-            atomicOr(err, 1);
-            continue;
-        }
-        set_bit(touched, pb);
+    const int b = (int)(g & 31);
+    if (!((touched[w0 + w] >> b) & 1u)) return;
+    const long long li = w * 32 + b;
+    const int rz = (int)(li % child.dim[2]);
+    const long long q = li / child.dim[2];
+    const int ry = (int)(q % child.dim[1]);
+    const int rx = (int)(q / child.dim[1]);
+    const long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
+                                 (child.lo[2] + rz) >> lgres);
+    if (pb < 0) {
+        atomicOr(err, 1);
+        return;
     }
+    set_bit(touched, pb);
 }
 
-// one thread per touched-bitmap word of level `lev`: getPosParent(pos, lev) for
-// every touched position; missing -> key bit, reachable leaf -> marker
+// a warp per touched-bitmap word of level `lev`, a lane per bit: getPosParent(pos, lev)
+// for every touched position; missing -> key bit, reachable leaf -> marker
 __global__ void k_resolve_touched(TreeView t, LeafGrid lg, int lev, KeyDomain d, const uint32_t* __restrict__ touched,
                                   uint32_t* keys, int* markers) {
-    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long w0 = d.bitbase >> 5, nw = (d.nbits + 31) >> 5;
-    if (w >= nw) return;
-    uint32_t bits = touched[w0 + w];
-    uint32_t miss = 0;
-    const int lgr = t.lgrange[lev];
-    while (bits) {
-        int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        long long li = w * 32 + b;
-        int rz = (int)(li % d.dim[2]);
-        long long q = li / d.dim[2];
-        int ry = (int)(q % d.dim[1]);
-        int rx = (int)(q / d.dim[1]);
-        int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
-        long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
-        if (pid < 0) miss |= 1u << b;
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = g >> 5, w0 = d.bitbase >> 5, nw = (d.nbits + 31) >> 5;
+    if (w >= nw) return;  // whole warps leave together (blockDim is a multiple of 32)
+    const int b = (int)(g & 31);
+    const uint32_t bits = touched[w0 + w];
+    bool miss = false;
+    if ((bits >> b) & 1u) {
+        const int lgr = t.lgrange[lev];
+        const long long li = w * 32 + b;
+        const int rz = (int)(li % d.dim[2]);
+        const long long q = li / d.dim[2];
+        const int ry = (int)(q % d.dim[1]);
+        const int rx = (int)(q / d.dim[1]);
+        const int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
+        const long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
+        if (pid < 0) miss = true;
         else if (lev == 0 && markers) markers[pid] = 1;
     }
-    if (miss) keys[w0 + w] = miss;  // each word has one owner thread
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, miss);
+    if (b == 0 && m) keys[w0 + w] = m;  // each word has one owner warp
 }
 
 __global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32_t* __restrict__ cnt) {
@@ -498,11 +496,11 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
     k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
     for (int lev = 1; lev < depth; lev++) {
         long long nw = (dom.d[lev - 1].nbits + 31) >> 5;
-        k_touch_up<<<blocks_for(nw, 128), 128, 0, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
+        k_touch_up<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
     }
     for (int lev = 0; lev < depth; lev++) {
         long long nw = (dom.d[lev].nbits + 31) >> 5;
-        k_resolve_touched<<<blocks_for(nw, 128), 128, 0, s>>>(t, lg, lev, dom.d[lev], touched, bitmap, markers);
+        k_resolve_touched<<<blocks_for(nw * 32, 128), 128, 0, s>>>(t, lg, lev, dom.d[lev], touched, bitmap, markers);
     }
 }
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
