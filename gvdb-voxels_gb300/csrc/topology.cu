@@ -32,7 +32,27 @@ __device__ __forceinline__ float warp_max(float v) {
 
 __global__ void k_bbox(PointSrc p, float3 orig, int* out6) {
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+    const float o[3] = {orig.x, orig.y, orig.z};
+    long long first = 0;
+    if (p.stride == 12 && p.off == 0 && ((uintptr_t)p.base & 15) == 0) {
+        // packed float3 on a 16-byte boundary: four points per three 16-byte loads
+        const float4* v = reinterpret_cast<const float4*>(p.base);
+        const long long groups = p.n >> 2;
+        for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
+             gi += (long long)gridDim.x * blockDim.x) {
+            const float4 a = __ldg(v + 3 * gi), b = __ldg(v + 3 * gi + 1), c = __ldg(v + 3 * gi + 2);
+            const float e[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int k = 0; k < 12; k++) {
+                const float w = fadd(e[k], o[k % 3]);
+                mn[k % 3] = fminf(mn[k % 3], w);
+                mx[k % 3] = fmaxf(mx[k % 3], w);
+            }
+        }
+        first = groups << 2;
+    }
+    for (long long i = first + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n;
+         i += (long long)gridDim.x * blockDim.x) {
         float x, y, z;
         load_pos(p.base, i, p.stride, p.off, x, y, z);
         float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
@@ -306,37 +326,34 @@ __global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32
 // (SetupNode, VG.cpp:2512-2524) at pool index base + rank
 __global__ void k_alloc_nodes(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ prefix, long long word0,
                               long long nwords, int lev, int lgrange, KeyDomain d, long long base, Node* nodes) {
-    long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // a lane per bit: rank = the word's prefix + the set bits below this one
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = g >> 5;
     if (w >= nwords) return;
-    uint32_t bits = bm[word0 + w];
-    if (!bits) return;
-    long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0];
-    long long level_bit0 = d.bitbase;  // bitbase is word aligned
-    while (bits) {
-        int b = __ffs(bits) - 1;
-        bits &= bits - 1;
-        long long li = (word0 + w) * 32 + b - level_bit0;
-        int rz = (int)(li % d.dim[2]);
-        long long q = li / d.dim[2];
-        int ry = (int)(q % d.dim[1]);
-        int rx = (int)(q / d.dim[1]);
-        long long idx = base + rank;
-        rank++;
-        Node n;
-        n.lev = (uint8_t)lev;
-        n.flags = 1;
-        n.prio = 0;
-        n.pad = 0;
-        n.pos[0] = (d.lo[0] + rx) << lgrange;
-        n.pos[1] = (d.lo[1] + ry) << lgrange;
-        n.pos[2] = (d.lo[2] + rz) << lgrange;
-        n.value[0] = n.value[1] = n.value[2] = -1;
-        n.vrange[0] = n.vrange[1] = n.vrange[2] = 0.f;
-        n.parent = kUndefL;
-        n.childlist = lev > 0 ? elem(1, lev, (unsigned long long)idx) : kUndefL;
-        n.mask = 0;
-        nodes[idx] = n;
-    }
+    const int b = (int)(g & 31);
+    const uint32_t bits = bm[word0 + w];
+    if (!((bits >> b) & 1u)) return;
+    const long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0] + __popc(bits & ((1u << b) - 1u));
+    const long long li = (word0 + w) * 32 + b - d.bitbase;  // bitbase is word aligned
+    const int rz = (int)(li % d.dim[2]);
+    const long long q = li / d.dim[2];
+    const int ry = (int)(q % d.dim[1]);
+    const int rx = (int)(q / d.dim[1]);
+    const long long idx = base + rank;
+    Node n;
+    n.lev = (uint8_t)lev;
+    n.flags = 1;
+    n.prio = 0;
+    n.pad = 0;
+    n.pos[0] = (d.lo[0] + rx) << lgrange;
+    n.pos[1] = (d.lo[1] + ry) << lgrange;
+    n.pos[2] = (d.lo[2] + rz) << lgrange;
+    n.value[0] = n.value[1] = n.value[2] = -1;
+    n.vrange[0] = n.vrange[1] = n.vrange[2] = 0.f;
+    n.parent = kUndefL;
+    n.childlist = lev > 0 ? elem(1, lev, (unsigned long long)idx) : kUndefL;
+    n.mask = 0;
+    nodes[idx] = n;
 }
 
 __global__ void k_write_node(Node* dst, Node v) { *dst = v; }
@@ -516,7 +533,7 @@ void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
     if (nwords <= 0) return;
-    k_alloc_nodes<<<blocks_for(nwords, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
+    k_alloc_nodes<<<blocks_for(nwords * 32, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
 }
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<1, 1, 0, s>>>(dst, v); }
 void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s) {
