@@ -144,6 +144,7 @@ struct gbvdb_grid_s {
     // neighbour table of UpdateNeighbors (6 leaf indices per leaf) and the leaf count it covers
     DevBuf nbr_table;
     long long nbr_count = -1;
+    DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
 
     // tuning
     int dense_min = 2048;
@@ -1311,7 +1312,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
-                      &g->psort};
+                      &g->psort, &g->csum_part};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1696,6 +1697,19 @@ gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
     GBVDB_END(g)
 }
 
+// gbvdb_checksum without the readback: the sum goes to a device pointer on the grid's
+// stream, so a pipelined caller reads it back when it likes (no host synchronisation)
+gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !dev_out) return GBVDB_INVALID_ARG;
+    g->grow(g->csum_part, (size_t)std::max(g->atlas_last, 1) * 8);
+    launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
+                          g->ptr<double>(g->csum_part), dev_out, g->stream);
+    g->check_launch("checksum");
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
 // Allocation-free variant of gbvdb_checksum: see include/gbvdb.h.  It reads the
 // grid's atlas and writes one double to dev_out on the grid's stream; its
 // scratch is the static per-slot array in atlas.cu, so it calls no allocator.
@@ -1764,7 +1778,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
                             &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
-                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort};
+                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

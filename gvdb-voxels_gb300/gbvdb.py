@@ -39,7 +39,7 @@ EXPORTS = [
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
-    "gbvdb_export_point_leaves",
+    "gbvdb_export_point_leaves", "gbvdb_checksum_device",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -122,6 +122,7 @@ def load(path=LIB_PATH):
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
     L.gbvdb_update_neighbors.argtypes = [vp]
+    L.gbvdb_checksum_device.argtypes = [vp, i32, vp]
     L.gbvdb_insert_points.argtypes = [vp, i64, fp, i32]
     L.gbvdb_scatter_density.argtypes = [vp, i64, f32, f32, fp, i32, i32]
     L.gbvdb_export_point_leaves.argtypes = [vp, vp, i64, vp, i64, vp, i64]
@@ -397,6 +398,10 @@ class Grid:
     def load_vbx(self, path):
         """LoadVBX (gvdb_volume_gvdb.cpp:507-683): replaces configuration, pools and channels."""
         self._check(self.L.gbvdb_load_vbx(self._h, os.fsencode(path)), "load_vbx")
+
+    def checksum_device(self, out, chan=0):
+        """FP64 channel sum into `out` (a CUDA float64 tensor element) on the grid's stream."""
+        self._check(self.L.gbvdb_checksum_device(self._h, chan, ctypes.c_void_p(out.data_ptr())), "checksum_device")
 
     def checksum(self, chan=0):
         out = ctypes.c_double()

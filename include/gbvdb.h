@@ -187,6 +187,10 @@ GBVDB_API gbvdb_status gbvdb_save_vbx(gbvdb_grid g, const char* path);
 GBVDB_API gbvdb_status gbvdb_load_vbx(gbvdb_grid g, const char* path);
 /* FP64 sum of the interior voxels of all assigned slots (total-mass check) */
 GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
+/* gbvdb_checksum written to the DEVICE pointer dev_out on the grid's stream, without a
+ * host synchronisation (no counterpart in the reference): for pipelined callers that read
+ * the result back asynchronously.  May allocate (per-slot partials). */
+GBVDB_API gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out);
 /* Allocation-free variant of gbvdb_checksum (no counterpart in the reference).
  * For callers that may not allocate device memory: a host application that owns
  * every device allocation and forbids its plugins to call cudaMalloc, or a

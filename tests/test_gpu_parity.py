@@ -291,3 +291,22 @@ def test_apron_after_other_interior_writers(gpu_lib):
     snap = {"bricks": g.atlas_bricks(0), "amap": g.atlas_map()}
     H.check_apron_self(snap, -1.0)
     assert np.array_equal(snap["bricks"][:, 1:17, 1:17, 1:17].reshape(used, -1), vals.cpu().numpy())
+
+
+def test_checksum_device_matches_checksum(gpu_lib):
+    import torch
+
+    import gbvdb
+
+    pts = datasets.shell(20_000, seed=93)
+    g = gbvdb.Grid(0, (3, 3, 3, 4))
+    g.add_channel(0, gbvdb.T_FLOAT)
+    n = g.set_points(torch.from_numpy(pts).cuda())
+    g.rebuild_topology(n, 1.0)
+    g.update_atlas()
+    _, ln = g.insert_points_subcell(4, n, 1.0)
+    g.gather_density(4, n, 1.0, (0, 0, 0), ln)
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    g.checksum_device(out[1])
+    torch.cuda.synchronize()
+    assert out[1].item() == g.checksum(0) and out[0].item() == 0 and out[2].item() == 0
