@@ -281,6 +281,11 @@ __device__ __forceinline__ f32x2 f2sub(f32x2 a, f32x2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ f32x2 f2add(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
     f32x2 r;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
@@ -289,6 +294,11 @@ __device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
 __device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
     f32x2 r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx(float a) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
     return r;
 }
 __device__ __forceinline__ float fmin3(float a, float b, float c) {
@@ -379,8 +389,9 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
         // voxels within rcut of it on every axis (brick-local voxel box).  The
         // live points of a batch of candidates go to a shared list; then every
         // warp walks the whole list but updates only the 4 tile rows y it owns
-        // (lanes: x = lane & 15, one of 2 rows; z walked in a loop), so no two
-        // threads ever update the same voxel at once and no atomics are needed.
+        // (lanes: 8 columns x 4 rows; x in groups of 8; z walked in a loop over
+        // the group's reach), so no two threads ever update the same voxel at
+        // once and no atomics are needed.
         float4* live_pts = reinterpret_cast<float4*>(scratch);
         for (uint32_t cbase = 0; cbase < ncand; cbase += kLive) {
             if (threadIdx.x == 0) nlive = 0;
@@ -414,7 +425,8 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
             }
             __syncthreads();
             const int nl = nlive;
-            const int xl = lane & 15, yl = lane >> 4;
+            const int xl = lane & 7, yl = lane >> 3;
+            const float rc2 = __fmul_rn(gp.rcut, gp.rcut);
             for (int e = 0; e < nl; e++) {
                 const float4 L = live_pts[e];
                 const int bx = __float_as_int(L.w);
@@ -422,27 +434,42 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
                 const int y0 = max((bx >> 8) & 15, 4 * warp), y1 = min((bx >> 12) & 15, 4 * warp + 3);
                 const int z0 = (bx >> 16) & 15, z1 = (bx >> 20) & 15;
                 if (y0 > y1) continue;
-                const int x = x0 + xl;
-                const float dx = fsub(L.x, (float)(ox + x));
-                for (int ys = y0; ys <= y1; ys += 2) {
-                    const int y = ys + yl;
-                    if (x <= x1 && y <= y1) {
-                        const float dy = fsub(L.y, (float)(oy + y));
+                // brick-local position; the distance from it to the nearest of this
+                // warp's rows (uniform over the warp)
+                const float lx = fsub(L.x, (float)ox), ly = fsub(L.y, (float)oy), lz = fsub(L.z, (float)oz);
+                const float gy = fmaxf(0.0f, fmaxf((float)y0 - ly, ly - (float)y1));
+                const int y = y0 + yl;
+                const float dy = fsub(L.y, (float)(oy + y));
+                for (int xs = x0; xs <= x1; xs += 8) {
+                    // z reach of this group of 8 columns: the sphere of radius rcut cut at
+                    // the group's nearest column (a superset of every voxel with d^2 < T)
+                    const int xe = min(xs + 7, x1);
+                    const float gx = fmaxf(0.0f, fmaxf((float)xs - lx, lx - (float)xe));
+                    const float zr2 = rc2 - __fmaf_rn(gy, gy, gx * gx);
+                    if (!(zr2 >= 0.0f)) continue;
+                    const float zr = sqrt_approx(zr2);  // rcut's margin (>= 0.01) covers its error
+                    const int za = max(z0, (int)ceilf(lz - zr)), zb = min(z1, (int)floorf(lz + zr));
+                    const int x = xs + xl;
+                    if (za <= zb && x <= xe && y <= y1) {
+                        const float dx = fsub(L.x, (float)(ox + x));
                         const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
                         if (__float_as_uint(dxy) < gp.tbits) {
-                            uint32_t* col = tile + (z0 << 8) + (y << 4) + x;
-                            float fz = (float)(oz + z0);  // integer-valued: += 1 is exact
+                            uint32_t* col = tile + (za << 8) + (y << 4) + x;
+                            const float fz = (float)(oz + za);  // integer-valued: steps of 1 and 2 are exact
                             const f32x2 pzz = f2pack(L.z, L.z), dxy2 = f2pack(dxy, dxy);
-                            int z = z0;
-                            for (; z < z1; z += 2, col += 512, fz += 2.0f) {  // two z per step, packed FP32
-                                const f32x2 dz = f2sub(pzz, f2pack(fz, fz + 1.0f));
+                            f32x2 fzz = f2pack(fz, fz + 1.0f);
+                            const f32x2 two = f2pack(2.0f, 2.0f);
+                            int z = za;
+                            for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
+                                const f32x2 dz = f2sub(pzz, fzz);
                                 const f32x2 d = f2fma(dz, dz, dxy2);
+                                fzz = f2add(fzz, two);
                                 const uint32_t d0 = __float_as_uint(f2lo(d)), d1 = __float_as_uint(f2hi(d));
                                 if (d0 < col[0]) col[0] = d0;
                                 if (d1 < col[256]) col[256] = d1;
                             }
-                            if (z == z1) {
-                                const float dz = fsub(L.z, fz);
+                            if (z == zb) {
+                                const float dz = fsub(L.z, f2lo(fzz));
                                 const uint32_t d = __float_as_uint(__fmaf_rn(dz, dz, dxy));
                                 if (d < *col) *col = d;
                             }
