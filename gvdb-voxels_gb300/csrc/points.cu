@@ -307,6 +307,104 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     return r;
 }
 
+// Unit-box pass of the gather form.  Every point within one voxel (per axis) of
+// the brick lowers the voxels floor(p) and floor(p) + 1 on each axis (the only
+// voxels it can be nearer than 1 to, on every axis) with shared atomicMin,
+// member subcells only.  A voxel whose minimum is then below 1 is exact: every
+// member point left out is at least 1 away on some axis, so its d^2 >= 1.  The
+// points are the brick's own (its 64 bins, one range) and the bins of the
+// subcell layer next to the brick in its 7 lower neighbours (61 ranges): a point
+// homed above the brick is at least 1 from its last voxel.
+// Range k of the 64 (62 used): neighbour index into nrank and bin in that brick.
+__device__ __forceinline__ void unit_range(int k, int& nb, int& bin) {
+    if (k == 0) { nb = 13; bin = 0; }                                              // own, all 64 bins
+    else if (k <= 16) { const int j = k - 1; nb = 12; bin = (j >> 2) * 16 + (j & 3) * 4 + 3; }   // -x: lx = 3
+    else if (k <= 32) { const int j = k - 17; nb = 10; bin = (j >> 2) * 16 + 12 + (j & 3); }     // -y: ly = 3
+    else if (k <= 48) { nb = 4; bin = 48 + (k - 33); }                               // -z: lz = 3
+    else if (k <= 52) { nb = 9; bin = (k - 49) * 16 + 15; }                          // -x-y
+    else if (k <= 56) { nb = 3; bin = 48 + (k - 53) * 4 + 3; }                       // -x-z
+    else if (k <= 60) { nb = 1; bin = 60 + (k - 57); }                               // -y-z
+    else { nb = 0; bin = 63; }                                                       // -x-y-z
+}
+
+__device__ __forceinline__ void unit_box_pass(uint32_t* tile, const int* nrank, const uint32_t* __restrict__ bin_off,
+                                              const float4* __restrict__ pts, int ox, int oy, int oz,
+                                              uint32_t* rbeg, uint32_t* rpre) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+        uint32_t beg[2] = {0, 0}, cnt[2] = {0, 0};
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k = lane + 32 * h;
+            if (k < 62) {
+                int nb, bin;
+                unit_range(k, nb, bin);
+                const int r = nrank[nb];
+                if (r >= 0) {
+                    const size_t b0 = (size_t)r * 64 + bin;
+                    beg[h] = __ldg(bin_off + b0);
+                    cnt[h] = __ldg(bin_off + b0 + (k == 0 ? 64 : 1)) - beg[h];
+                }
+            }
+        }
+        uint32_t i0 = cnt[0], i1 = cnt[1];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, i0, o), b = __shfl_up_sync(0xFFFFFFFFu, i1, o);
+            if (lane >= o) { i0 += a; i1 += b; }
+        }
+        const uint32_t t0 = __shfl_sync(0xFFFFFFFFu, i0, 31);
+        rbeg[lane] = beg[0];
+        rbeg[lane + 32] = beg[1];
+        rpre[lane] = i0 - cnt[0];
+        rpre[lane + 32] = t0 + i1 - cnt[1];
+        if (lane == 31) rpre[64] = t0 + i1;
+    }
+    __syncthreads();
+    const uint32_t total = rpre[64];
+    const int org[3] = {ox, oy, oz};
+    for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        int k = 0;  // last range with rpre[k] <= idx (a non-empty one)
+#pragma unroll
+        for (int step = 32; step > 0; step >>= 1)
+            if (rpre[k + step] <= idx) k += step;
+        const float4 q = pts[rbeg[k] + (idx - rpre[k])];
+        const int pk = __float_as_int(q.w);
+        const float pw[3] = {q.x, q.y, q.z};
+        int vl[3];
+        bool ok[3][2];
+        float dd[3][2];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int fl = (int)pw[a];  // floor: stored positions are >= 0
+            const int hs = fl >> 2;     // home subcell
+            vl[a] = fl - org[a];
+            ok[a][0] = (unsigned)vl[a] < 16u && ((pk >> (9 * a + 4)) & 1);
+            ok[a][1] = (unsigned)(vl[a] + 1) < 16u && ((pk >> (9 * a + 4 + (((fl + 1) >> 2) - hs))) & 1);
+            dd[a][0] = fsub(pw[a], (float)fl);
+            dd[a][1] = fsub(pw[a], (float)(fl + 1));
+        }
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            if (!ok[0][i]) continue;
+            const float xx = __fmul_rn(dd[0][i], dd[0][i]);
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                if (!ok[1][j]) continue;
+                const float xy = __fmaf_rn(dd[1][j], dd[1][j], xx);
+#pragma unroll
+                for (int kk = 0; kk < 2; kk++) {
+                    if (!ok[2][kk]) continue;
+                    const uint32_t d = __float_as_uint(__fmaf_rn(dd[2][kk], dd[2][kk], xy));
+                    const int v = ((vl[2] + kk) << 8) | ((vl[1] + j) << 4) | (vl[0] + i);
+                    if (d < tile[v]) atomicMin(tile + v, d);
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // One block per linked leaf.  Setup: the ranks of the 3x3x3 neighbour bricks and
 // their point ranges in the home-binned array (a brick's 64 bins are contiguous).
 // Then one of two forms, chosen per brick by the number of points homed in the
@@ -489,22 +587,48 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
         float* qx = reinterpret_cast<float*>(scratch) + warp * (3 * kQueue);
         float* qy = qx + kQueue;
         float* qz = qy + kQueue;
+        unit_box_pass(tile, nrank, bin_off, pts, ox, oy, oz, reinterpret_cast<uint32_t*>(scratch),
+                      reinterpret_cast<uint32_t*>(scratch) + 64);
         const int nw = blockDim.x >> 5;
         const int hf = lane >> 4, cx = lane & 3, cy = (lane >> 2) & 3;
         const unsigned lt = (1u << lane) - 1u;
+        constexpr uint32_t kOne = 0x3F800000u;  // 1.0f: minima below it are exact after the unit-box pass
         for (int sc = warp; sc < 64; sc += nw) {
             const int lx = sc & 3, ly = (sc >> 2) & 3, lz = sc >> 4;
+            const int tv = ((4 * lz) << 8) | ((4 * ly + cy) << 4) | (4 * lx + cx);
+            float m0 = __uint_as_float(tile[tv]), m1 = __uint_as_float(tile[tv + 256]);
+            float m2 = __uint_as_float(tile[tv + 512]), m3 = __uint_as_float(tile[tv + 768]);
+            // needy voxels (minimum >= 1): the search runs for them alone, over the
+            // points that can come nearer to their bounding box than wmax, the
+            // largest needy minimum
+            // (with a cutoff T <= 1 the unit-box pass alone is exact: d^2 < T needs every axis below 1)
+            const uint32_t nb1 = gp.tbits > kOne ? kOne : 0xFFFFFFFFu;
+            const bool n0 = __float_as_uint(m0) >= nb1, n1 = __float_as_uint(m1) >= nb1;
+            const bool n2 = __float_as_uint(m2) >= nb1, n3 = __float_as_uint(m3) >= nb1;
+            const bool anyn = n0 | n1 | n2 | n3;
+            if (!__any_sync(0xFFFFFFFFu, anyn)) continue;
             const int Sx = sx0 + lx, Sy = sy0 + ly, Sz = sz0 + lz;
-            const float fx = (float)(ox + 4 * lx + cx), fy = (float)(oy + 4 * ly + cy);
-            const float fz = (float)(oz + 4 * lz);
+            const int vx = ox + 4 * lx + cx, vy = oy + 4 * ly + cy, vz = oz + 4 * lz;
+            const float fx = (float)vx, fy = (float)vy;
+            const float fz = (float)vz;
             const f32x2 fxx = f2pack(fx, fx), fyy = f2pack(fy, fy);
             const f32x2 z0 = f2pack(fz, fz), z1 = f2pack(fz + 1.0f, fz + 1.0f);
             const f32x2 z2 = f2pack(fz + 2.0f, fz + 2.0f), z3 = f2pack(fz + 3.0f, fz + 3.0f);
-            const float blx = (float)(4 * Sx), bhx = blx + 3.0f;
-            const float bly = (float)(4 * Sy), bhy = bly + 3.0f;
-            const float blz = (float)(4 * Sz), bhz = blz + 3.0f;
-            float m0 = Tf, m1 = Tf, m2 = Tf, m3 = Tf;
-            float wmax = Tf;
+            const int zlo = n0 ? 0 : (n1 ? 1 : (n2 ? 2 : 3)), zhi = n3 ? 3 : (n2 ? 2 : (n1 ? 1 : 0));
+            const int nlx = __reduce_min_sync(0xFFFFFFFFu, anyn ? vx : INT_MAX);
+            const int nhx = __reduce_max_sync(0xFFFFFFFFu, anyn ? vx : INT_MIN);
+            const int nly = __reduce_min_sync(0xFFFFFFFFu, anyn ? vy : INT_MAX);
+            const int nhy = __reduce_max_sync(0xFFFFFFFFu, anyn ? vy : INT_MIN);
+            const int nlz = __reduce_min_sync(0xFFFFFFFFu, anyn ? vz + zlo : INT_MAX);
+            const int nhz = __reduce_max_sync(0xFFFFFFFFu, anyn ? vz + zhi : INT_MIN);
+            const float blx = (float)nlx, bhx = (float)nhx;
+            const float bly = (float)nly, bhy = (float)nhy;
+            const float blz = (float)nlz, bhz = (float)nhz;
+            auto needy_max = [&]() {
+                const float a = fmaxf(n0 ? m0 : 0.0f, n1 ? m1 : 0.0f), b = fmaxf(n2 ? m2 : 0.0f, n3 ? m3 : 0.0f);
+                return __uint_as_float(__reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(a, b))));
+            };
+            float wmax = needy_max();
             int nq = 0;
             // evaluate the queued points [0, nq) against the column's 4 voxels
             auto drain = [&]() {
@@ -546,7 +670,11 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
                     glb = (float)o.w;
                     gneed = member_bits(o.x, o.y, o.z);
                     const int hx = Sx + o.x, hy = Sy + o.y, hz = Sz + o.z;
-                    if (hx >= 0 && hy >= 0 && hz >= 0) {
+                    // bound for the bin's points [4h, 4h + 4) against the needy box
+                    const int gx = max(0, max(4 * hx - nhx, nlx - 4 * hx - 4));
+                    const int gy = max(0, max(4 * hy - nhy, nly - 4 * hy - 4));
+                    const int gz = max(0, max(4 * hz - nhz, nlz - 4 * hz - 4));
+                    if (hx >= 0 && hy >= 0 && hz >= 0 && (float)(gx * gx + gy * gy + gz * gz) < wmax) {
                         const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
                         const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
                         if (r >= 0) {
@@ -556,6 +684,8 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
                         }
                     }
                 }
+                // sorted by lb^2: a group starting at or beyond wmax ends the subcell
+                if (__shfl_sync(0xFFFFFFFFu, glb, 0) >= wmax) break;
                 unsigned nonempty = __ballot_sync(0xFFFFFFFFu, gcnt > 0);
                 while (nonempty) {
                     const int l = __ffs(nonempty) - 1;
@@ -593,21 +723,19 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
                         if (nq >= 32) drain();
                     }
                     if (nq) drain();
-                    // merge the halves' minima; wmax = the largest voxel minimum
+                    // merge the halves' minima; wmax = the largest needy minimum
                     m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
                     m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
                     m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
                     m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
-                    wmax = __uint_as_float(
-                        __reduce_max_sync(0xFFFFFFFFu, __float_as_uint(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3)))));
+                    wmax = needy_max();
                 }
             }
             if (hf == 0) {
-                const int v = ((4 * lz) << 8) | ((4 * ly + cy) << 4) | (4 * lx + cx);
-                tile[v] = __float_as_uint(m0);
-                tile[v + 256] = __float_as_uint(m1);
-                tile[v + 512] = __float_as_uint(m2);
-                tile[v + 768] = __float_as_uint(m3);
+                tile[tv] = __float_as_uint(m0);
+                tile[tv + 256] = __float_as_uint(m1);
+                tile[tv + 512] = __float_as_uint(m2);
+                tile[tv + 768] = __float_as_uint(m3);
             }
         }
     }

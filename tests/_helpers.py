@@ -55,13 +55,15 @@ def snapshot_oracle(g, ln):
 
 def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
             boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True,
-            fp16_subcells=False):
+            fp16_subcells=False, dense_min=None):
     import torch
 
     import gbvdb
 
     dtype = gbvdb.T_FLOAT if dtype is None else dtype
     g = gbvdb.Grid(0, log2dims)
+    if dense_min is not None:  # force one gather form: 0 = gather form everywhere, 2**31-1 = scatter form
+        g.set_tuning(gbvdb.TUNE_DENSE_MIN, dense_min)
     g.add_channel(0, dtype, 1, axiscnt)
     seq = frames if frames is not None else [points]
     outs = []

@@ -52,6 +52,19 @@ def test_fluid_frames_levelset(gpu_lib):
         _full_check(o[k], g[k], 3.0)
 
 
+@pytest.mark.parametrize("dense_min", [0, 2**31 - 1])
+@pytest.mark.parametrize("mode,rho", [("levelset", 2.0), ("density", 1.0), ("density", 2.5)])
+def test_gather_forms(gpu_lib, dense_min, mode, rho):
+    """Both gather forms on every brick (the form is chosen per brick by point count):
+    the dam (dense: unit-box pass, then the search for voxels left at >= 1) and the
+    scattered particles around it, level set and density, cutoffs below and above 1."""
+    pos, vel = _mini_fluid(n=40000, seed=21)
+    p = np.maximum(pos + 1.5 * vel, 0.0).astype(np.float32)
+    _, o = H.run_oracle(p, radius=4.0, R=4.0, rho=rho, mode=mode, boundval=0.0)
+    _, g = H.run_gpu(p, radius=4.0, R=4.0, rho=rho, mode=mode, boundval=0.0, dense_min=dense_min)
+    _full_check(o[0], g[0], 0.0)
+
+
 def test_accumulate_topology(gpu_lib):
     pos, vel = _mini_fluid(n=20000, seed=5)
     frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
