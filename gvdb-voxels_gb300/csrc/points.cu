@@ -363,12 +363,24 @@ __device__ __forceinline__ void unit_box_pass(uint32_t* tile, const int* nrank, 
     __syncthreads();
     const uint32_t total = rpre[64];
     const int org[3] = {ox, oy, oz};
-    for (uint32_t idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        int k = 0;  // last range with rpre[k] <= idx (a non-empty one)
+    // two points per thread per round, both loads in flight together
+    for (uint32_t i0 = threadIdx.x; i0 < total; i0 += 2 * blockDim.x) {
+        float4 qq[2];
 #pragma unroll
-        for (int step = 32; step > 0; step >>= 1)
-            if (rpre[k + step] <= idx) k += step;
-        const float4 q = pts[rbeg[k] + (idx - rpre[k])];
+        for (int u = 0; u < 2; u++) {
+            const uint32_t idx = i0 + u * blockDim.x;
+            qq[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // w = 0: no member subcell, nothing written
+            if (idx < total) {
+                int k = 0;  // last range with rpre[k] <= idx (a non-empty one)
+#pragma unroll
+                for (int step = 32; step > 0; step >>= 1)
+                    if (rpre[k + step] <= idx) k += step;
+                qq[u] = pts[rbeg[k] + (idx - rpre[k])];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+        const float4 q = qq[u];
         const int pk = __float_as_int(q.w);
         const float pw[3] = {q.x, q.y, q.z};
         int vl[3];
@@ -400,6 +412,7 @@ __device__ __forceinline__ void unit_box_pass(uint32_t* tile, const int* nrank, 
                     if (d < tile[v]) atomicMin(tile + v, d);
                 }
             }
+        }
         }
     }
     __syncthreads();
@@ -437,6 +450,7 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
     // scatter form: the live-point list; gather form: per-warp point queues
     __shared__ __align__(16) unsigned char scratch[kScratch];
     __shared__ int nlive;
+    __shared__ int next_sc;  // gather form: next subcell to search
 
     const int leaf = linked[blockIdx.x];
     const Node nd = t.nodes[0][leaf];
@@ -587,13 +601,19 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
         float* qx = reinterpret_cast<float*>(scratch) + warp * (3 * kQueue);
         float* qy = qx + kQueue;
         float* qz = qy + kQueue;
+        if (threadIdx.x == 0) next_sc = blockDim.x >> 5;  // published by the pass's barriers
         unit_box_pass(tile, nrank, bin_off, pts, ox, oy, oz, reinterpret_cast<uint32_t*>(scratch),
                       reinterpret_cast<uint32_t*>(scratch) + 64);
-        const int nw = blockDim.x >> 5;
         const int hf = lane >> 4, cx = lane & 3, cy = (lane >> 2) & 3;
         const unsigned lt = (1u << lane) - 1u;
         constexpr uint32_t kOne = 0x3F800000u;  // 1.0f: minima below it are exact after the unit-box pass
-        for (int sc = warp; sc < 64; sc += nw) {
+        // subcells are taken in turn from a shared counter (the searches' costs differ widely)
+        auto next_subcell = [&]() {
+            int n = 0;
+            if (lane == 0) n = atomicAdd(&next_sc, 1);
+            return __shfl_sync(0xFFFFFFFFu, n, 0);
+        };
+        for (int sc = warp; sc < 64; sc = next_subcell()) {
             const int lx = sc & 3, ly = (sc >> 2) & 3, lz = sc >> 4;
             const int tv = ((4 * lz) << 8) | ((4 * ly + cy) << 4) | (4 * lx + cx);
             float m0 = __uint_as_float(tile[tv]), m1 = __uint_as_float(tile[tv + 256]);
@@ -698,29 +718,38 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
                     const uint32_t beg = __shfl_sync(0xFFFFFFFFu, gbeg, l);
                     const uint32_t end = beg + __shfl_sync(0xFFFFFFFFu, gcnt, l);
                     const int need = __shfl_sync(0xFFFFFFFFu, gneed, l);
-                    for (uint32_t base = beg; base < end; base += 32) {
-                        const uint32_t j = base + lane;
-                        bool ok = false;
-                        float4 q = make_float4(0, 0, 0, 0);
-                        if (j < end) {
-                            q = pts[j];
-                            if ((__float_as_int(q.w) & need) == need) {
-                                const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q.x), fsub(q.x, bhx)));
-                                const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q.y), fsub(q.y, bhy)));
-                                const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q.z), fsub(q.z, bhz)));
-                                const float lb = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
-                                ok = lb < wmax;
+                    // 64 points per round: both loads in flight before either is filtered
+                    for (uint32_t base = beg; base < end; base += 64) {
+                        float4 q[2];
+                        bool ok[2];
+#pragma unroll
+                        for (int u = 0; u < 2; u++) {
+                            const uint32_t j = base + 32 * u + lane;
+                            ok[u] = j < end;
+                            q[u] = ok[u] ? pts[j] : make_float4(0, 0, 0, 0);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 2; u++) {
+                            if (ok[u]) {
+                                ok[u] = false;
+                                if ((__float_as_int(q[u].w) & need) == need) {
+                                    const float gx = fmaxf(0.0f, fmaxf(fsub(blx, q[u].x), fsub(q[u].x, bhx)));
+                                    const float gy = fmaxf(0.0f, fmaxf(fsub(bly, q[u].y), fsub(q[u].y, bhy)));
+                                    const float gz = fmaxf(0.0f, fmaxf(fsub(blz, q[u].z), fsub(q[u].z, bhz)));
+                                    const float lb = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmul_rn(gx, gx)));
+                                    ok[u] = lb < wmax;
+                                }
                             }
+                            const unsigned live = __ballot_sync(0xFFFFFFFFu, ok[u]);
+                            if (ok[u]) {
+                                const int k = nq + __popc(live & lt);
+                                qx[k] = q[u].x;
+                                qy[k] = q[u].y;
+                                qz[k] = q[u].z;
+                            }
+                            nq += __popc(live);
+                            if (nq >= 32) drain();
                         }
-                        const unsigned live = __ballot_sync(0xFFFFFFFFu, ok);
-                        if (ok) {
-                            const int k = nq + __popc(live & lt);
-                            qx[k] = q.x;
-                            qy[k] = q.y;
-                            qz[k] = q.z;
-                        }
-                        nq += __popc(live);
-                        if (nq >= 32) drain();
                     }
                     if (nq) drain();
                     // merge the halves' minima; wmax = the largest needy minimum
