@@ -470,6 +470,7 @@ def bench_ours(args):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     grid = gbvdb.Grid(local, LOG2DIMS, stream=stream)
+    grid.set_tuning(gbvdb.TUNE_FUSED_APRON, args.fused_apron)
     grid.add_channel(0, gbvdb.T_FLOAT)
 
     state = {"frame": 0}
@@ -646,6 +647,8 @@ def main():
     ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-max-points", type=float, default=4e6)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 500.0, 2000.0])
+    ap.add_argument("--fused-apron", type=int, default=1, choices=[0, 1],
+                    help="gathers write the neighbours' apron voxels (1) or UpdateApron copies them all (0)")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)

@@ -141,6 +141,72 @@ __global__ void __launch_bounds__(256) k_apron(TreeView t, LeafGrid lg, const At
     }
 }
 
+// UpdateApron after a fused-apron gather (k_gather's push_apron): every brick has
+// already copied its boundary voxels into its neighbours' apron records, so only
+// the voxels of missing neighbours are left (the boundary value).  One warp per
+// slot.  The push was made only when the grid passed that gather's push check
+// (k_push_check: linked == flagged == found by the lookup, slot == linked rank),
+// and then every neighbour the lookup finds here pushed into this slot.  If the
+// check failed (*bad) this is the full pass.
+template <typename T>
+__global__ void __launch_bounds__(256) k_apron_fill(TreeView t, LeafGrid lg, const AtlasNode* __restrict__ amap, int used,
+                                                    int ax, int ay, const T* __restrict__ interior,
+                                                    T* __restrict__ apron, T boundval, const int* __restrict__ bad) {
+    __shared__ int nsl[8][27];  // >= 0: copy from that slot; -1: boundary value; -2: written by the gather
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = blockIdx.x * 8 + w;
+    if (s >= used) return;
+    const bool pushed = __ldg(bad) == 0;
+    const AtlasNode an = amap[s];
+    if (an.leaf < 0) return;
+    const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+    int ns = -1;
+    if (lane < 27 && (dx | dy | dz)) {
+        const int px = an.pos[0] + 16 * dx, py = an.pos[1] + 16 * dy, pz = an.pos[2] + 16 * dz;
+        const long long nl = (px < 0 || py < 0 || pz < 0) ? -1 : lookup_leaf(lg, t, px, py, pz);
+        if (pushed) ns = nl >= 0 ? -2 : -1;
+        else if (nl >= 0) ns = slot_of_value(t.nodes[0][nl].value, ax, ay);
+    }
+    if (lane >= 27 || lane == 13) ns = -2;
+    T* out = apron + (size_t)s * kApronStride;
+    if (pushed) {
+        // only the boundary value is left to write, where a neighbour is missing:
+        // whole faces as 16-byte vectors, then the edge and corner voxels
+        const unsigned miss = __ballot_sync(0xFFFFFFFFu, ns == -1);
+        if (!miss) return;
+        uint32_t bb;
+        if constexpr (sizeof(T) == 4) bb = __float_as_uint(*reinterpret_cast<const float*>(&boundval));
+        else bb = (uint32_t)(*reinterpret_cast<const uint16_t*>(&boundval)) * 0x10001u;
+        const uint4 b4 = make_uint4(bb, bb, bb, bb);
+        constexpr int kFaceDir[6] = {12, 14, 10, 16, 4, 22};  // source direction of faces -x +x -y +y -z +z
+        constexpr int kVec = 256 * (int)sizeof(T) / 16;        // 16-byte vectors per face
+#pragma unroll
+        for (int f = 0; f < 6; f++) {
+            if (!((miss >> kFaceDir[f]) & 1u)) continue;
+            uint4* fo = reinterpret_cast<uint4*>(out + f * 256);
+            for (int q = lane; q < kVec; q += 32) fo[q] = b4;
+        }
+        for (int j = lane; j < 200; j += 32)
+            if ((miss >> (26 - (int)(__ldg(kApronEdges.e + j) >> 12))) & 1u) out[1536 + j] = boundval;
+        return;
+    }
+    if (lane < 27) nsl[w][lane] = ns;
+    if (!__ballot_sync(0xFFFFFFFFu, ns != -2)) return;
+    __syncwarp();
+    for (int k = lane; k < 1736; k += 32) {
+        int x, y, z;
+        apron_shell_pos(k, x, y, z);
+        const int ex = x == 0 ? -1 : (x == 17 ? 1 : 0);
+        const int ey = y == 0 ? -1 : (y == 17 ? 1 : 0);
+        const int ez = z == 0 ? -1 : (z == 17 ? 1 : 0);
+        const int n2 = nsl[w][(ez + 1) * 9 + (ey + 1) * 3 + (ex + 1)];
+        if (n2 == -2) continue;
+        out[k] = n2 >= 0 ? interior[(size_t)n2 * 4096 + (((z - 1 - 16 * ez) << 8) | ((y - 1 - 16 * ey) << 4) |
+                                                         (x - 1 - 16 * ex))]
+                         : boundval;
+    }
+}
+
 template <typename T>
 __global__ void k_export_bricks(const T* __restrict__ interior, const T* __restrict__ apron, int used, T* out) {
     long long total = (long long)used * 5832;
@@ -430,17 +496,27 @@ void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s) {
     k_fill_u32<<<gs_blocks(n, 256), 256, 0, s>>>(p, n, v);
 }
 void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, int used, int ax, int ay, int esize,
-                  const void* interior, void* apron, uint32_t boundbits, cudaStream_t s) {
+                  const void* interior, void* apron, uint32_t boundbits, const int* fill_only_bad, cudaStream_t s) {
+    const bool fill_only = fill_only_bad != nullptr;
     if (used <= 0) return;
     if (esize == 4) {
         float b;
         memcpy(&b, &boundbits, 4);
-        k_apron<float><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const float*)interior, (float*)apron, b);
+        if (fill_only && lg.cells)
+            k_apron_fill<float><<<(used + 7) / 8, 256, 0, s>>>(t, lg, amap, used, ax, ay, (const float*)interior,
+                                                               (float*)apron, b, fill_only_bad);
+        else
+            k_apron<float><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const float*)interior, (float*)apron, b);
     } else {
         uint16_t b16 = (uint16_t)boundbits;
         __half_raw hr;
         hr.x = b16;
-        k_apron<__half><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const __half*)interior, (__half*)apron, __half(hr));
+        if (fill_only && lg.cells)
+            k_apron_fill<__half><<<(used + 7) / 8, 256, 0, s>>>(t, lg, amap, used, ax, ay, (const __half*)interior,
+                                                                (__half*)apron, __half(hr), fill_only_bad);
+        else
+            k_apron<__half><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const __half*)interior, (__half*)apron,
+                                                 __half(hr));
     }
 }
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out, cudaStream_t s) {

@@ -245,4 +245,50 @@ __host__ __device__ inline int apron_index(int x, int y, int z) {
     return 1728 + hz * 4 + hy * 2 + hx;
 }
 
+// inverse of apron_index: record index k in [0, 1736) -> padded-brick coordinate
+// on the apron shell.  The voxel comes from the neighbour at direction
+// d = (x==0 ? -1 : x==17 ? 1 : 0, ...), whose local voxel is (x-1-16*dx, ...).
+__host__ __device__ constexpr void apron_shell_pos(int k, int& x, int& y, int& z) {
+    if (k < 1536) {
+        const int f = k >> 8, r = ((k >> 4) & 15) + 1, c = (k & 15) + 1, h = (f & 1) ? 17 : 0;
+        if (f < 2) { x = h; z = r; y = c; }
+        else if (f < 4) { y = h; z = r; x = c; }
+        else { z = h; y = r; x = c; }
+    } else if (k < 1728) {
+        const int e = (k - 1536) >> 4, i = ((k - 1536) & 15) + 1;
+        const int lo = (e & 1) ? 17 : 0, hi = ((e >> 1) & 1) ? 17 : 0;
+        if (e < 4) { x = i; y = lo; z = hi; }
+        else if (e < 8) { y = i; x = lo; z = hi; }
+        else { z = i; x = lo; y = hi; }
+    } else {
+        const int c = k - 1728;
+        x = (c & 1) ? 17 : 0;
+        y = (c & 2) ? 17 : 0;
+        z = (c & 4) ? 17 : 0;
+    }
+}
+
+// Edges and corners of the apron record (records [1536, 1736)): for record
+// 1536 + j, the voxel of the source brick (interior index (z << 8) | (y << 4) | x)
+// and the direction index (dx+1) + 3 (dy+1) + 9 (dz+1) of the brick that receives
+// it, seen from the source; the source, seen from the receiver, is 26 - that.
+struct ApronEdgeTable {
+    uint32_t e[200];  // record 1536 + j: tile index | receiver direction << 12
+};
+constexpr ApronEdgeTable make_apron_edge_table() {
+    ApronEdgeTable t{};
+    for (int j = 0; j < 200; j++) {
+        int x = 0, y = 0, z = 0;
+        apron_shell_pos(1536 + j, x, y, z);
+        const int dx = x == 0 ? -1 : (x == 17 ? 1 : 0);
+        const int dy = y == 0 ? -1 : (y == 17 ? 1 : 0);
+        const int dz = z == 0 ? -1 : (z == 17 ? 1 : 0);
+        const int tile_idx = ((z - 1 - 16 * dz) << 8) | ((y - 1 - 16 * dy) << 4) | (x - 1 - 16 * dx);
+        const int recv = (1 - dz) * 9 + (1 - dy) * 3 + (1 - dx);
+        t.e[j] = (uint32_t)tile_idx | ((uint32_t)recv << 12);
+    }
+    return t;
+}
+static __device__ const ApronEdgeTable kApronEdges = make_apron_edge_table();
+
 }  // namespace gbvdb

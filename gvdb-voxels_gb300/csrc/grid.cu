@@ -145,9 +145,22 @@ struct gbvdb_grid_s {
     DevBuf nbr_table;
     long long nbr_count = -1;
     DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
+    DevBuf push_bad;   // fused apron: the push check's flag (one int)
 
     // tuning
     int dense_min = 2048;
+
+    // Fused apron: a gather also writes each brick's boundary voxels into its
+    // neighbours' apron records, and the next UpdateApron of that channel only
+    // fills the faces whose neighbour is missing.  layout_ver changes with every
+    // topology, atlas or channel change; a channel's pushed_ver is the layout_ver
+    // of the gather that pushed (0: none, or the interior was written since).
+    // Handing out raw atlas pointers turns the fused form off for the grid.
+    bool fused_apron = true;
+    unsigned long long layout_ver = 1;
+    unsigned long long pushed_ver[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    void layout_changed() { layout_ver++; }
+    void interior_written(int c) { if (c >= 0 && c < 8) pushed_ver[c] = 0; }
 
     // profiling
     bool profile = false;
@@ -230,6 +243,7 @@ struct gbvdb_grid_s {
     }
 
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
+        layout_changed();
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
         nused0_stale = false;
         nbr_count = -1;
@@ -543,6 +557,7 @@ struct gbvdb_grid_s {
     }
 
     gbvdb_status rebuild(long long n, float radius, float3 orig, bool accumulate, int min_depth) {
+        layout_changed();
         if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
         if (n <= 0) return GBVDB_NOOP;
         if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
@@ -586,6 +601,7 @@ struct gbvdb_grid_s {
 
     // ------------------------------------------------------------- atlas
     void resize_channels(long long slots) {
+        layout_changed();
         for (int c = 0; c < 8; c++) {
             Channel& C = ch[c];
             if (!C.used || C.cap_slots >= slots) continue;
@@ -601,6 +617,7 @@ struct gbvdb_grid_s {
     }
 
     gbvdb_status update_atlas() {  // UpdateAtlas (VG.cpp:2630-2704)
+        layout_changed();
         if (!ch[0].used) throw StatusError{GBVDB_INVALID_ARG, "no atlas channel"};
         long long total = ncnt[0];
         // the flagged-leaf count is F below; an earlier count is only used when it is current
@@ -824,15 +841,28 @@ struct gbvdb_grid_s {
         int span = 4 + gp.hi_off - gp.lo_off;
         TreeView t = view();
         void* interior = ch[chan].interior.p;
+        interior_written(chan);
         if (sc_orphans > 0 || span > 12) {
             materialize_lists();
             launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
                                 interior, stream);
         } else {
             gp.dense_min = dense_min;
+            // fused apron: needs the dense leaf lookup (the apron pass resolves
+            // neighbours with the same table) and an apron of one voxel
+            const bool push = fused_apron && lgv.cells && ch[chan].apron == 1 && atlas_last > 0;
+            gp.apron = push ? ch[chan].apron_buf.p : nullptr;
             build_offsets(gp.lo_off, gp.hi_off, T, sc_R);
+            if (push) {
+                grow(push_bad, 16);
+                gp.apron_bad = ptr<int>(push_bad);
+                check(cudaMemsetAsync(push_bad.p, 0, 4, stream), "push check clear");
+                launch_push_check(t, lgv, ptr<uint32_t>(scmap), ptr<AtlasNode>(amap), atlas_last, ax, ay, ncnt[0],
+                                  ptr<int>(push_bad), stream);
+            }
             launch_gather(t, lgv, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
                           ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, interior, stream);
+            if (push) pushed_ver[chan] = layout_ver;
         }
         check_launch("gather");
         mark();
@@ -850,8 +880,11 @@ struct gbvdb_grid_s {
         else if (ch[chan].dtype == GBVDB_T_HALF) bb = f2h_bits(boundval);
         else bb = f2bf_bits(boundval);
         TreeView t = view();
+        // after a fused-apron gather of this layout only the faces of missing
+        // neighbours are left to write
+        const bool fill_only = fused_apron && lgv.cells && pushed_ver[chan] == layout_ver;
         launch_apron(t, lgv, ptr<AtlasNode>(amap), atlas_last, ax, ay, ch[chan].esize, ch[chan].interior.p,
-                     ch[chan].apron_buf.p, bb, stream);
+                     ch[chan].apron_buf.p, bb, fill_only ? ptr<int>(push_bad) : nullptr, stream);
         check_launch("apron");
         mark();
         stage_end();
@@ -895,6 +928,7 @@ struct gbvdb_grid_s {
         if (ins_n < 0 || ins_nleaf != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "InsertPoints was not called for this topology"};
         if (!ch[0].used || ch[0].dtype != GBVDB_T_FLOAT) throw StatusError{GBVDB_NOT_SUPPORTED, "ScatterDensity: FP32 channel 0"};
         if (atlas_last == 0 || ins_nleaf == 0) return GBVDB_NOOP;
+        interior_written(0);
         launch_scatter_density(ptr<Node>(nodes[0]), ins_nleaf, ptr<uint32_t>(goff), ptr<float>(psort), radius,
                                expand ? 1 : 0, res[0], ax, ay, ptr<float>(ch[0].interior), ptr<float>(ch[0].apron_buf),
                                stream);
@@ -933,6 +967,7 @@ struct gbvdb_grid_s {
             throw StatusError{GBVDB_INVALID_ARG, "Compute: bad channel or parameters"};
         if (ch[chan].dtype != GBVDB_T_FLOAT) throw StatusError{GBVDB_NOT_SUPPORTED, "Compute: FP32 channels only"};
         if (atlas_last == 0) return GBVDB_NOOP;
+        interior_written(chan);
         for (int it = 0; it < iterations; it++) {
             launch_smooth(ptr<AtlasNode>(amap), atlas_last, ptr<float>(ch[chan].interior),
                           ptr<float>(ch[chan].apron_buf), prm[0], prm[1], stream);
@@ -944,6 +979,7 @@ struct gbvdb_grid_s {
 
     // ------------------------------------------------------- configuration
     gbvdb_status configure(int nlev, const int* ld) {  // Configure (VG.cpp:2380-2434)
+        layout_changed();
         if (nlev < 2 || nlev > kMaxLev || !ld) return GBVDB_INVALID_ARG;
         int d[kMaxLev];
         long long rg = 1;
@@ -971,6 +1007,7 @@ struct gbvdb_grid_s {
     }
 
     gbvdb_status add_channel(int chan, int dtype, int apron, int cax, int cay, int caz) {  // VG.cpp:2437-2453
+        layout_changed();
         if (!configured) return GBVDB_INVALID_ARG;
         if (chan < 0 || chan >= 8) return GBVDB_INVALID_ARG;
         if (apron != 1) return GBVDB_NOT_SUPPORTED;  // the reference's apron kernels assume 1 (VG.cpp:4448)
@@ -1130,6 +1167,7 @@ struct gbvdb_grid_s {
     }
 
     gbvdb_status load_vbx(const char* path) {
+        layout_changed();
         if (!path) return GBVDB_INVALID_ARG;
         File F;
         F.f = fopen(path, "rb");
@@ -1312,7 +1350,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
-                      &g->psort, &g->csum_part};
+                      &g->psort, &g->csum_part, &g->push_bad};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1558,6 +1596,7 @@ gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value) {
     if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
     if (g->atlas_last == 0) return GBVDB_NOOP;
     Channel& C = g->ch[chan];
+    g->interior_written(chan);
     launch_fill_interior(g->ptr<AtlasNode>(g->amap), g->atlas_last, C.dtype, C.interior.p, value, g->stream);
     uint32_t bb = C.esize == 4 ? gbvdb_grid_s::bits_of(value)
                                : (C.dtype == GBVDB_T_HALF ? f2h_bits(value) : f2bf_bits(value));
@@ -1736,6 +1775,10 @@ gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, voi
     if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
     if (interior) *interior = g->ch[chan].interior.p;
     if (apron) *apron = g->ch[chan].apron_buf.p;
+    // the caller may write the interior at any time from now on: every UpdateApron
+    // of this grid copies the interiors as they are (no fused apron)
+    g->fused_apron = false;
+    for (int c = 0; c < 8; c++) g->interior_written(c);
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -1745,6 +1788,12 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
     if (param == GBVDB_TUNE_DENSE_MIN) {
         if (value < 0 || value > (1ll << 31)) return GBVDB_INVALID_ARG;
         g->dense_min = (int)value;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_FUSED_APRON) {
+        if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
+        g->fused_apron = value != 0;
+        for (int c = 0; c < 8; c++) g->interior_written(c);
         return GBVDB_OK;
     }
     return GBVDB_INVALID_ARG;
@@ -1778,7 +1827,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
                             &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
-                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part};
+                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

@@ -61,8 +61,9 @@ void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag,
 void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
                          cudaStream_t s);
 void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s);
+// fill_only: after a fused-apron gather of this layout (bad: that gather's push check flag)
 void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, int used, int ax, int ay, int esize,
-                  const void* interior, void* apron, uint32_t boundbits, cudaStream_t s);
+                  const void* interior, void* apron, uint32_t boundbits, const int* fill_only_bad, cudaStream_t s);
 void launch_export_bricks(const void* interior, const void* apron, int used, int esize, void* out,
                           cudaStream_t s);
 // one brick layer (18 voxel slices) of the reference's atlas layout <-> interior + apron records
@@ -120,7 +121,14 @@ struct GatherParams {
     int lo_off, hi_off;  // home-bin offset range H - S (subcell units)
     int dense_min;     // bricks with more candidate points use the gather form
     float rcut;        // per-axis distance at or beyond which d^2 >= cutoff (conservative)
+    // fused apron: when apron is non-null each brick also writes its boundary
+    // voxels into the apron records of its 26 neighbours (see k_gather)
+    void* apron;
+    const int* apron_bad;  // set by the push check: the grid is not in the state the push assumes
 };
+// fused-apron precondition (one thread per leaf); *bad must be 0 before the launch
+void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,
+                       int ax, int ay, long long n, int* bad, cudaStream_t s);
 // offs: candidate home-bin offsets {dx, dy, dz, lb2} (H - S, subcell units), ascending lb2
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,

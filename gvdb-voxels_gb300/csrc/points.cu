@@ -227,8 +227,59 @@ __device__ __forceinline__ float finish_c(const GatherParams& gp, float c, float
     return fminf(gp.accum ? old : 3.0f, fsub(c, gp.rho));
 }
 
+// Fused apron.  After the tile write, the tile holds the final values' storage
+// bits and each brick copies its boundary voxels into the apron records of the
+// neighbours that hold them (pslot[d]: slot of the neighbour at direction d =
+// (dx+1) + 3 (dy+1) + 9 (dz+1), -1 for none).  Apron voxel k of a brick comes
+// from the neighbour at direction d(k) (apron_shell_pos), so this brick writes
+// voxel k of the brick at -d(k).  Every apron voxel of the atlas has one source
+// brick: no two blocks write the same element.  Face records are in the order of
+// the source plane (x faces [z][y], y faces [z][x], z faces [y][x]) and go as
+// 4-voxel vectors; edges and corners take kApronEdges (tile index, receiver).
+
 template <typename T>
-__device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out) {
+__device__ __forceinline__ void push_apron(const uint32_t* tile, const int* pslot, T* apron) {
+    const int tid = threadIdx.x;
+    // faces: 6 x 64 vectors, iteration a = axis (x, y, z); the first 64 threads take
+    // the minus face of the receiver (source plane 15, receiver at +axis), the
+    // others the plus face (source plane 0, receiver at -axis)
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int plus = (tid >> 6) & 1, f = 2 * a + plus;
+        const int e0 = (tid & 63) << 2, row = e0 >> 4, col = e0 & 15, h = plus ? 0 : 15;
+        const int step = a == 0 ? 1 : (a == 1 ? 3 : 9);
+        const int tgt = pslot[13 + (plus ? -step : step)];
+        if (tgt < 0) continue;
+        uint4 b;
+        if (a == 0) {  // x face [z][y]: 4 voxels down a column of the source plane
+            const uint32_t* c = tile + ((row << 8) | (col << 4) | h);
+            b = make_uint4(c[0], c[16], c[32], c[48]);
+        } else if (a == 1) {  // y face [z][x]
+            b = *reinterpret_cast<const uint4*>(tile + ((row << 8) | (h << 4) | col));
+        } else {  // z face [y][x]
+            b = *reinterpret_cast<const uint4*>(tile + ((h << 8) | (row << 4) | col));
+        }
+        const size_t e = (size_t)tgt * kApronStride + (size_t)f * 256 + e0;
+        if constexpr (sizeof(T) == 4)
+            *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(apron) + e) = b;
+        else
+            *reinterpret_cast<uint2*>(reinterpret_cast<uint16_t*>(apron) + e) = make_uint2(b.x | (b.y << 16), b.z | (b.w << 16));
+    }
+    for (int j = tid; j < 200; j += blockDim.x) {  // edges and corners
+        const uint32_t te = __ldg(kApronEdges.e + j);
+        const int tgt = pslot[te >> 12];
+        if (tgt < 0) continue;
+        const uint32_t b = tile[te & 4095u];
+        const size_t e = (size_t)tgt * kApronStride + 1536 + j;
+        if constexpr (sizeof(T) == 4) reinterpret_cast<uint32_t*>(apron)[e] = b;
+        else reinterpret_cast<uint16_t*>(apron)[e] = (uint16_t)b;
+    }
+}
+
+// Final values from the tile of minima, one coalesced write of the brick.  keep:
+// the final values' storage bits replace the minima in the tile (fused apron).
+template <typename T>
+__device__ void write_tile(const GatherParams& gp, uint32_t* tile, T* out, bool keep) {
     // voxels no point reached hold the cutoff: their sqrt is one per thread
     const float sqrtT = __fsqrt_rn(__uint_as_float(gp.tbits));
     for (int v4 = threadIdx.x; v4 < 1024; v4 += blockDim.x) {
@@ -250,6 +301,9 @@ __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out)
         }
         if constexpr (sizeof(T) == 4) {
             reinterpret_cast<float4*>(out)[v4] = make_float4(r[0], r[1], r[2], r[3]);
+            if (keep)
+                reinterpret_cast<uint4*>(tile)[v4] = make_uint4(__float_as_uint(r[0]), __float_as_uint(r[1]),
+                                                                __float_as_uint(r[2]), __float_as_uint(r[3]));
         } else {
             T h[4];
 #pragma unroll
@@ -258,6 +312,8 @@ __device__ void write_tile(const GatherParams& gp, const uint32_t* tile, T* out)
             pk.x = (uint32_t)(*reinterpret_cast<uint16_t*>(&h[0])) | ((uint32_t)(*reinterpret_cast<uint16_t*>(&h[1])) << 16);
             pk.y = (uint32_t)(*reinterpret_cast<uint16_t*>(&h[2])) | ((uint32_t)(*reinterpret_cast<uint16_t*>(&h[3])) << 16);
             reinterpret_cast<uint2*>(out)[v4] = pk;
+            if (keep)
+                reinterpret_cast<uint4*>(tile)[v4] = make_uint4(pk.x & 0xFFFFu, pk.x >> 16, pk.y & 0xFFFFu, pk.y >> 16);
         }
     }
 }
@@ -418,6 +474,31 @@ __device__ __forceinline__ void unit_box_pass(uint32_t* tile, const int* nrank, 
     __syncthreads();
 }
 
+// Fused-apron check, one thread per leaf.  The gather's push and the apron fill
+// assume that the grid is in the state every frame of the path leaves it in:
+// a leaf is linked (mParent defined) exactly when it is flagged and exactly when
+// the dense lookup finds it at its own position, its atlas slot is its rank among
+// the linked leaves (so scmap gives neighbours' slots) and the slot maps back to
+// it, and the linked count equals the assigned slots.  Any leaf that breaks this
+// sets *bad, and both the push and the fill are then skipped for the whole grid.
+__global__ void k_push_check(TreeView t, LeafGrid lg, const uint32_t* __restrict__ scmap,
+                             const AtlasNode* __restrict__ amap, int used, int ax, int ay, long long n, int* bad) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && (long long)scmap[n] != (long long)used) *bad = 1;
+    if (i >= n) return;
+    const Node nd = t.nodes[0][i];
+    const bool lk = nd.parent != kUndef64;
+    const bool fl = nd.flags != 0;
+    const bool fd = lg.cells && nd.pos[0] >= 0 && nd.pos[1] >= 0 && nd.pos[2] >= 0 &&
+                    lookup_leaf(lg, t, nd.pos[0], nd.pos[1], nd.pos[2]) == i;
+    bool ok = lk == fl && lk == fd;
+    if (ok && lk) {
+        const int s = slot_of_value(nd.value, ax, ay);
+        ok = s >= 0 && s < used && (uint32_t)s == scmap[i] && amap[s].leaf == (int)i;
+    }
+    if (!ok) *bad = 1;
+}
+
 // One block per linked leaf.  Setup: the ranks of the 3x3x3 neighbour bricks and
 // their point ranges in the home-binned array (a brick's 64 bins are contiguous).
 // Then one of two forms, chosen per brick by the number of points homed in the
@@ -451,6 +532,7 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
     __shared__ __align__(16) unsigned char scratch[kScratch];
     __shared__ int nlive;
     __shared__ int next_sc;  // gather form: next subcell to search
+    __shared__ int pslot[27];  // fused apron: slot of the neighbour at each direction, -1: none / no push
 
     const int leaf = linked[blockIdx.x];
     const Node nd = t.nodes[0][leaf];
@@ -465,6 +547,9 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
     if (warp == 0) {
         int r = -1;
         uint32_t beg = 0, cnt = 0;
+        // fused apron: the grid passed the push check (k_push_check), so a linked
+        // leaf's rank is its atlas slot
+        const bool push_ok = gp.apron != nullptr && __ldg(gp.apron_bad) == 0;
         if (lane < 27) {
             int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
             if ((dx | dy | dz) == 0) {
@@ -482,6 +567,7 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
             }
             nrank[lane] = r;
             nb_beg[lane] = beg;
+            pslot[lane] = (push_ok && lane != 13) ? r : -1;
         }
         uint32_t incl = cnt;
 #pragma unroll
@@ -769,7 +855,12 @@ __global__ void __launch_bounds__(kGatherThreads, 9) k_gather(TreeView t, LeafGr
         }
     }
     __syncthreads();
-    write_tile<T>(gp, tile, interior + (size_t)slot * 4096);
+    const bool push = gp.apron != nullptr;
+    write_tile<T>(gp, tile, interior + (size_t)slot * 4096, push);
+    if (push) {
+        __syncthreads();
+        push_apron<T>(tile, pslot, reinterpret_cast<T*>(gp.apron));
+    }
 }
 
 // ---- materialized subcell lists (reference-shaped; export + fallback) ----
@@ -837,7 +928,7 @@ __global__ void k_gather_lists(TreeView t, const int* __restrict__ linked, const
         tile[v] = m;
     }
     __syncthreads();
-    write_tile<T>(gp, tile, interior + (size_t)slot * 4096);
+    write_tile<T>(gp, tile, interior + (size_t)slot * 4096, false);
 }
 
 // ---- legacy InsertPoints + ScatterDensity (brick binning and a splat) ----
@@ -974,6 +1065,10 @@ void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* b
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
     if (p.n <= 0) return;
     k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted);
+}
+void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,
+                       int ax, int ay, long long n, int* bad, cudaStream_t s) {
+    k_push_check<<<blocks_for(std::max(n, 1ll), 256), 256, 0, s>>>(t, lg, scmap, amap, used, ax, ay, n, bad);
 }
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,

@@ -60,6 +60,7 @@ class JobResult(ctypes.Structure):
                 ("checksum", ctypes.c_double), ("t_submit_ms", ctypes.c_double), ("t_start_ms", ctypes.c_double),
                 ("t_end_ms", ctypes.c_double)]
 TUNE_DENSE_MIN = 1
+TUNE_FUSED_APRON = 2
 FUNC_SMOOTH = 113
 
 

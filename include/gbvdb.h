@@ -204,11 +204,20 @@ GBVDB_API gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev
  * that first call before any stream capture.  All calls share the array: calls
  * that overlap on the GPU (different streams or grids without ordering) race. */
 GBVDB_API gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out);
-/* device pointers of the atlas storage (interior bricks, apron records) for consumers */
+/* device pointers of the atlas storage (interior bricks, apron records) for consumers.
+ * A caller holding these pointers may write the interior at any time, so from this
+ * call on every UpdateApron of the grid copies the interiors as they are (the
+ * fused apron of GBVDB_TUNE_FUSED_APRON is turned off for the grid). */
 GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron);
 /* tuning parameters (no counterpart in the reference) */
 #define GBVDB_TUNE_DENSE_MIN 1   /* candidate points per brick above which gathers use the warp-per-subcell
                                     form instead of the scatter form (default 2048) */
+#define GBVDB_TUNE_FUSED_APRON 2 /* 1 (default): a gather (binned form, apron 1, dense leaf lookup) also
+                                    writes every brick's boundary voxels into its neighbours' apron records,
+                                    and the next UpdateApron of that channel, with no topology, atlas or
+                                    interior change in between, only writes the faces of missing neighbours
+                                    (boundval); the atlas ends bit-identical to a full UpdateApron.  0: every
+                                    UpdateApron copies all apron voxels (the reference's kernel). */
 GBVDB_API gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value);
 /* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
 GBVDB_API gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable);

@@ -65,6 +65,41 @@ def test_gather_forms(gpu_lib, dense_min, mode, rho):
     _full_check(o[0], g[0], 0.0)
 
 
+@pytest.mark.parametrize("case", ["fluid_levelset", "shell_density_half", "surface_bf16", "accumulate"])
+def test_fused_apron_matches_full_apron(gpu_lib, case):
+    """The fused apron (each gather brick writes its boundary voxels into its
+    neighbours' apron records; UpdateApron then only writes the faces of missing
+    neighbours) leaves every padded brick bit-identical to the full UpdateApron
+    pass, frame after frame (full, full, incremental rebuilds) and for 16-bit storage."""
+    import gbvdb
+
+    kw = {}
+    if case == "fluid_levelset":
+        pos, vel = _mini_fluid(n=40000, seed=31)
+        frames = [(pos + 0.5 * k * vel).astype(np.float32) for k in range(1, 5)]
+        kw = dict(frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    elif case == "shell_density_half":
+        kw = dict(points=datasets.shell(50_000, seed=32), radius=1.0, R=1.0, rho=1.0, mode="density",
+                  boundval=0.5, dtype=gbvdb.T_HALF)
+    elif case == "surface_bf16":
+        kw = dict(points=datasets.sphere_surface(60_000, seed=33), radius=1.5, R=1.5, rho=1.5, mode="density",
+                  boundval=0.0, dtype=gbvdb.T_BFLOAT16)
+    else:
+        pos, vel = _mini_fluid(n=20000, seed=34)
+        frames = [np.maximum(f, 0.0).astype(np.float32)
+                  for f in (pos, pos + 3.0 * vel, pos - 3.0 * vel)]
+        kw = dict(frames=frames, radius=2.0, R=2.0, rho=1.5, accumulate=True)
+    pts = kw.pop("points", None)
+    _, a = H.run_gpu(pts, fused_apron=1, export_subcells=False, **kw)
+    _, b = H.run_gpu(pts, fused_apron=0, export_subcells=False, **kw)
+    assert len(a) == len(b)
+    for sa, sb in zip(a, b):
+        assert np.array_equal(sa["amap"], sb["amap"])
+        assert sa["bricks"].dtype == sb["bricks"].dtype
+        assert np.array_equal(sa["bricks"].view(np.uint8), sb["bricks"].view(np.uint8))
+        H.check_apron_self(sa, kw["boundval"] if "boundval" in kw else 0.0)
+
+
 def test_accumulate_topology(gpu_lib):
     pos, vel = _mini_fluid(n=20000, seed=5)
     frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
@@ -256,8 +291,9 @@ def test_fp16_subcells_levelset(gpu_lib):
 
 def test_apron_after_other_interior_writers(gpu_lib):
     """UpdateApron copies the interiors as they are now, whoever wrote them last: after a
-    gather (boundary planes kept beside the bricks), after FillChannel, and after the
-    caller wrote the interior through gbvdb_get_atlas_device."""
+    gather (whose fused apron already wrote the neighbours' boundary voxels), after
+    FillChannel, and after the caller wrote the interior through gbvdb_get_atlas_device
+    (which turns the fused apron off for the grid)."""
     import ctypes
 
     import torch
