@@ -146,6 +146,7 @@ struct gbvdb_grid_s {
     long long nbr_count = -1;
     DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
     DevBuf push_bad;   // fused apron: the push check's flag (one int)
+    DevBuf nbmask;     // linked flags of the 27 bricks around each leaf (InsertPointsSubcell)
 
     // tuning
     int dense_min = 2048;
@@ -700,7 +701,15 @@ struct gbvdb_grid_s {
         qz.mn = make_float3(posmin[0], posmin[1], posmin[2]);
         qz.rg = make_float3(posmax[0] - posmin[0], posmax[1] - posmin[1], posmax[2] - posmin[2]);
         sc_quant = qz;
-        launch_bin_count(t, lgv, p, trans, R, qz, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
+        // R <= 11: the list-length count reads the linked flags of the 27 bricks around
+        // each home brick from a per-leaf mask instead of looking each brick up
+        const uint32_t* nbm = nullptr;
+        if (R <= 11.0f) {
+            grow(nbmask, (size_t)std::max(ncnt[0], 1ll) * 4);
+            launch_nb_mask(t, lgv, ncnt[0], ptr<uint32_t>(nbmask), stream);
+            nbm = ptr<uint32_t>(nbmask);
+        }
+        launch_bin_count(t, lgv, p, trans, R, qz, ptr<uint32_t>(scmap), nbm, ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
                          ptr<uint32_t>(rank_of), totals, stream);
         check_launch("bin_count");
         grow(scan_tmp, scan_tmp_bytes(nbins));
@@ -1350,7 +1359,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
-                      &g->psort, &g->csum_part, &g->push_bad};
+                      &g->psort, &g->csum_part, &g->push_bad, &g->nbmask};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1827,7 +1836,8 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
                             &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
-                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad};
+                            &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
+                            &g->nbmask};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

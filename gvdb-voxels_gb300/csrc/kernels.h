@@ -104,9 +104,12 @@ struct Quant {
     float3 mn, rg;
     int on;
 };
+// linked flags of the 27 bricks around every linked leaf (bit (dz+1)*9 + (dy+1)*3 + (dx+1))
+void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s);
+// nbmask (or null): from launch_nb_mask; only for R <= 11, where member ranges stay within those 27 bricks
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
-                      uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals,
-                      cudaStream_t s);
+                      const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
+                      unsigned long long* totals, cudaStream_t s);
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s);
 

@@ -83,47 +83,137 @@ __device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeV
 
 // Home-subcell counting pass + total subcell-list length (the reference's
 // pSCPntsLength) + orphans (valid points whose home leaf is not linked).
+// Which of the 27 bricks around each linked leaf (itself included) are linked
+// leaves: bit (dz+1)*9 + (dy+1)*3 + (dx+1); positions with a negative coordinate
+// count as not linked, as in the list-length count.
+__global__ void k_nb_mask(TreeView t, LeafGrid lg, long long n, uint32_t* __restrict__ nbmask) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Node& nd = t.nodes[0][i];
+    if (nd.parent == kUndef64) return;
+    uint32_t m = 0;
+    for (int d = 0; d < 27; d++) {
+        const int px = nd.pos[0] + 16 * (d % 3 - 1), py = nd.pos[1] + 16 * ((d / 3) % 3 - 1), pz = nd.pos[2] + 16 * (d / 9 - 1);
+        if (px < 0 || py < 0 || pz < 0) continue;
+        if (linked_leaf(lg, t, px, py, pz) >= 0) m |= 1u << d;
+    }
+    nbmask[i] = m;
+}
+
+// subcells of the member range [lo, hi] (multiples of 4) inside the brick at origin o
+__device__ __forceinline__ int range_in_brick(int lo, int hi, int o) {
+    const int a = max(lo, o), b = min(hi, o + 12);
+    return b >= a ? ((b - a) >> 2) + 1 : 0;
+}
+
 __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
-                            const uint32_t* __restrict__ scmap, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
-                            unsigned long long* totals) {
+                            const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ nbmask,
+                            uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
+    // kU points per thread per step: the position loads, the home-leaf lookups, the
+    // rank loads and the counting atomics of the kU points are each issued together
+    // (the pass is bound by the latency of that dependent chain)
+    constexpr int kU = 4;
     unsigned long long members = 0, orphans = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
-        float w[3];
-        if (!load_valid(p, i, trans, w[0], w[1], w[2])) { bin_of[i] = -1; continue; }
-        float ps[3];
-        stored_pos(qz, w, ps);
-        int h[3];  // home subcell of the stored position
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+        float w[kU][3];
+        bool ok[kU];
 #pragma unroll
-        for (int a = 0; a < 3; a++) h[a] = ((int)ps[a]) & ~(kSc - 1);
-        long long leaf = linked_leaf(lg, t, h[0], h[1], h[2]);
-        if (leaf < 0) {
-            bin_of[i] = -2;
-            orphans++;
-        } else {
-            const Node& nd = t.nodes[0][leaf];
-            int loc = (((h[2] - nd.pos[2]) >> 2) << 4) | (((h[1] - nd.pos[1]) >> 2) << 2) | ((h[0] - nd.pos[0]) >> 2);
-            unsigned bin = scmap[leaf] * 64u + (unsigned)loc;
-            rank_of[i] = atomicAdd(bin_cnt + bin, 1u);
-            bin_of[i] = (int)bin;
+        for (int u = 0; u < kU; u++) {
+            const long long i = i0 + u * stride;
+            ok[u] = i < p.n && load_valid(p, i, trans, w[u][0], w[u][1], w[u][2]);
         }
-        // number of (subcell, point) list entries this point creates
-        int lo[3], hi[3];
-        bool any = true;
+        long long leaf[kU];
+        unsigned loc[kU];
+        int hb[kU][3];  // origin of the home brick
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            sc_range(w[a], R, lo[a], hi[a]);
-            if (lo[a] < 0) lo[a] = 0;  // guard: negative subcells are skipped
-            if (hi[a] < lo[a]) any = false;
+        for (int u = 0; u < kU; u++) {
+            leaf[u] = -1;
+            loc[u] = 0;
+            if (!ok[u]) continue;
+            float ps[3];
+            stored_pos(qz, w[u], ps);
+            int h[3];  // home subcell of the stored position
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                h[a] = ((int)ps[a]) & ~(kSc - 1);
+                hb[u][a] = h[a] & ~15;
+            }
+            leaf[u] = linked_leaf(lg, t, h[0], h[1], h[2]);
+            // subcell within the 16^3 leaf that contains h (leaf origin = h rounded down to 16)
+            loc[u] = (unsigned)((((h[2] >> 2) & 3) << 4) | (((h[1] >> 2) & 3) << 2) | ((h[0] >> 2) & 3));
         }
-        if (!any) continue;
-        for (int bx = lo[0] >> 4; bx <= hi[0] >> 4; bx++) {
-            int x0 = max(lo[0], bx << 4), x1 = min(hi[0], (bx << 4) + 12);
-            for (int by = lo[1] >> 4; by <= hi[1] >> 4; by++) {
-                int y0 = max(lo[1], by << 4), y1 = min(hi[1], (by << 4) + 12);
-                for (int bz = lo[2] >> 4; bz <= hi[2] >> 4; bz++) {
-                    int z0 = max(lo[2], bz << 4), z1 = min(hi[2], (bz << 4) + 12);
-                    if (linked_leaf(lg, t, bx << 4, by << 4, bz << 4) < 0) continue;
-                    members += (unsigned long long)(((x1 - x0) >> 2) + 1) * (((y1 - y0) >> 2) + 1) * (((z1 - z0) >> 2) + 1);
+        unsigned bin[kU];
+        uint32_t nbm[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            bin[u] = leaf[u] >= 0 ? __ldg(scmap + leaf[u]) * 64u + loc[u] : 0u;
+            nbm[u] = (nbmask && leaf[u] >= 0) ? __ldg(nbmask + leaf[u]) : 0u;
+        }
+        uint32_t rk[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) rk[u] = leaf[u] >= 0 ? atomicAdd(bin_cnt + bin[u], 1u) : 0u;
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const long long i = i0 + u * stride;
+            if (i >= p.n) continue;
+            if (!ok[u]) {
+                bin_of[i] = -1;
+            } else if (leaf[u] < 0) {
+                bin_of[i] = -2;
+                orphans++;
+            } else {
+                rank_of[i] = rk[u];
+                bin_of[i] = (int)bin[u];
+            }
+        }
+        // number of (subcell, point) list entries each point creates
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            if (!ok[u]) continue;
+            int lo[3], hi[3];
+            bool any = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                sc_range(w[u][a], R, lo[a], hi[a]);
+                if (lo[a] < 0) lo[a] = 0;  // guard: negative subcells are skipped
+                if (hi[a] < lo[a]) any = false;
+            }
+            if (!any) continue;
+            if (nbmask && leaf[u] >= 0) {
+                // R <= 11: the member range reaches only the 27 bricks around the home
+                // brick; their linked flags are nbm (k_nb_mask)
+                int c[3][3];
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int d = 0; d < 3; d++) c[a][d] = range_in_brick(lo[a], hi[a], hb[u][a] + 16 * (d - 1));
+                if (nbm[u] == 0x7FFFFFFu) {
+                    members += (unsigned long long)(c[0][0] + c[0][1] + c[0][2]) * (unsigned)(c[1][0] + c[1][1] + c[1][2]) *
+                               (unsigned)(c[2][0] + c[2][1] + c[2][2]);
+                } else {
+                    unsigned long long m = 0;
+#pragma unroll
+                    for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+                        for (int dy = 0; dy < 3; dy++) {
+                            const int row = (nbm[u] >> (dz * 9 + dy * 3)) & 7;
+                            const int sx = ((row & 1) ? c[0][0] : 0) + ((row & 2) ? c[0][1] : 0) + ((row & 4) ? c[0][2] : 0);
+                            m += (unsigned long long)(sx * c[1][dy] * c[2][dz]);
+                        }
+                    members += m;
+                }
+                continue;
+            }
+            for (int bx = lo[0] >> 4; bx <= hi[0] >> 4; bx++) {
+                int x0 = max(lo[0], bx << 4), x1 = min(hi[0], (bx << 4) + 12);
+                for (int by = lo[1] >> 4; by <= hi[1] >> 4; by++) {
+                    int y0 = max(lo[1], by << 4), y1 = min(hi[1], (by << 4) + 12);
+                    for (int bz = lo[2] >> 4; bz <= hi[2] >> 4; bz++) {
+                        int z0 = max(lo[2], bz << 4), z1 = min(hi[2], (bz << 4) + 12);
+                        if (linked_leaf(lg, t, bx << 4, by << 4, bz << 4) < 0) continue;
+                        members += (unsigned long long)(((x1 - x0) >> 2) + 1) * (((y1 - y0) >> 2) + 1) * (((z1 - z0) >> 2) + 1);
+                    }
                 }
             }
         }
@@ -1055,11 +1145,16 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
     if (n <= 0) return;
     k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
 }
+void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s) {
+    if (n <= 0) return;
+    k_nb_mask<<<blocks_for(n, 256), 256, 0, s>>>(t, lg, n, nbmask);
+}
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
-                      const uint32_t* scmap, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
+                      const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
                       unsigned long long* totals, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, bin_cnt, bin_of, rank_of, totals);
+    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of,
+                                                    totals);
 }
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
