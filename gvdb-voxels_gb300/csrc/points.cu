@@ -85,19 +85,21 @@ __device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeV
 // pSCPntsLength) + orphans (valid points whose home leaf is not linked).
 // Which of the 27 bricks around each linked leaf (itself included) are linked
 // leaves: bit (dz+1)*9 + (dy+1)*3 + (dx+1); positions with a negative coordinate
-// count as not linked, as in the list-length count.
+// count as not linked, as in the list-length count.  One warp per leaf, a lane
+// per direction.
 __global__ void k_nb_mask(TreeView t, LeafGrid lg, long long n, uint32_t* __restrict__ nbmask) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int d = threadIdx.x & 31;
     if (i >= n) return;
     const Node& nd = t.nodes[0][i];
     if (nd.parent == kUndef64) return;
-    uint32_t m = 0;
-    for (int d = 0; d < 27; d++) {
+    bool on = false;
+    if (d < 27) {
         const int px = nd.pos[0] + 16 * (d % 3 - 1), py = nd.pos[1] + 16 * ((d / 3) % 3 - 1), pz = nd.pos[2] + 16 * (d / 9 - 1);
-        if (px < 0 || py < 0 || pz < 0) continue;
-        if (linked_leaf(lg, t, px, py, pz) >= 0) m |= 1u << d;
+        on = px >= 0 && py >= 0 && pz >= 0 && linked_leaf(lg, t, px, py, pz) >= 0;
     }
-    nbmask[i] = m;
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, on);
+    if (d == 0) nbmask[i] = m;
 }
 
 // subcells of the member range [lo, hi] (multiples of 4) inside the brick at origin o
@@ -1147,7 +1149,7 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
 }
 void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s) {
     if (n <= 0) return;
-    k_nb_mask<<<blocks_for(n, 256), 256, 0, s>>>(t, lg, n, nbmask);
+    k_nb_mask<<<blocks_for(n * 32, 256), 256, 0, s>>>(t, lg, n, nbmask);
 }
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
