@@ -300,7 +300,11 @@ __global__ void k_slot_sums(const AtlasNode* __restrict__ amap, int used, const 
                             double* __restrict__ partials) {
     __shared__ double red[32];
     constexpr int V = 16 / sizeof(T);  // elements per 16-byte load
-    for (int s = blockIdx.x; s < used; s += gridDim.x) {
+    // highest slots first: a gather writes the bricks roughly in slot order, so the
+    // last-written ones may still be in L2 (the partials are summed in slot order
+    // afterwards, so the visiting order does not change the result)
+    for (int j = blockIdx.x; j < used; j += gridDim.x) {
+        const int s = used - 1 - j;
         float hi = 0.0f, lo = 0.0f;
         if (amap[s].leaf >= 0) {
             // all of this thread's 16-byte loads of the brick in flight together
