@@ -113,8 +113,10 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
                             uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
     // kU points per thread per step: the position loads, the home-leaf lookups, the
     // rank loads and the counting atomics of the kU points are each issued together
-    // (the pass is bound by the latency of that dependent chain)
-    constexpr int kU = 4;
+    // (the pass is bound by the latency of that dependent chain).  Measured on the
+    // fluid frame: kU = 1 or 2 (54 / 63 registers) beat 3 and 4 (72 / 80 registers,
+    // fewer resident warps) by about 10 us.
+    constexpr int kU = 2;
     unsigned long long members = 0, orphans = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
