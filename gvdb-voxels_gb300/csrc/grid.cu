@@ -147,6 +147,7 @@ struct gbvdb_grid_s {
     DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
     DevBuf push_bad;   // fused apron: the push check's flag (one int)
     DevBuf nbmask;     // linked flags of the 27 bricks around each leaf (InsertPointsSubcell)
+    DevBuf gtab;       // per-brick gather setup (neighbour ranks and bin ranges, origin, slot)
 
     // tuning
     int dense_min = 2048;
@@ -869,8 +870,9 @@ struct gbvdb_grid_s {
                 launch_push_check(t, lgv, ptr<uint32_t>(scmap), ptr<AtlasNode>(amap), atlas_last, ax, ay, ncnt[0],
                                   ptr<int>(push_bad), stream);
             }
+            grow(gtab, (size_t)std::max(sc_nbricks, 1ll) * 32 * 16);
             launch_gather(t, lgv, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
-                          ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, interior, stream);
+                          ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, ptr<int4>(gtab), interior, stream);
             if (push) pushed_ver[chan] = layout_ver;
         }
         check_launch("gather");
@@ -1359,7 +1361,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
-                      &g->psort, &g->csum_part, &g->push_bad, &g->nbmask};
+                      &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab};
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
@@ -1837,7 +1839,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
-                            &g->nbmask};
+                            &g->nbmask, &g->gtab};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

@@ -133,9 +133,10 @@ struct GatherParams {
 void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,
                        int ax, int ay, long long n, int* bad, cudaStream_t s);
 // offs: candidate home-bin offsets {dx, dy, dz, lb2} (H - S, subcell units), ascending lb2
+// gtab: scratch of nbricks * 32 int4 (the per-brick setup, filled by the launcher's prep kernel)
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
-                   void* interior, cudaStream_t s);
+                   int4* gtab, void* interior, cudaStream_t s);
 // materialized subcell lists (export and the fallback gather)
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                        uint32_t* cnt, cudaStream_t s);

@@ -593,6 +593,44 @@ __global__ void k_push_check(TreeView t, LeafGrid lg, const uint32_t* __restrict
     if (!ok) *bad = 1;
 }
 
+// Per-brick setup of the gather, one warp per linked leaf (lane = direction d =
+// (dx+1) + 3 (dy+1) + 9 (dz+1)): the linked rank of the neighbour brick at d and
+// the range of its 64 home bins in the binned points; entry 27 holds the brick's
+// origin and atlas slot.  Done here with every warp's loads in flight at once,
+// so that a gather block starts from one coalesced 512-byte read instead of a
+// chain of dependent lookups.
+__global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ linked, long long nbricks,
+                              const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ bin_off, int ax, int ay,
+                              int4* __restrict__ gtab) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (b >= nbricks) return;
+    const int leaf = linked[b];
+    const Node& nd = t.nodes[0][leaf];
+    const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+    int4 e = make_int4(-1, 0, 0, 0);
+    if (lane < 27) {
+        const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+        int r = -1;
+        if ((dx | dy | dz) == 0) {
+            r = (int)scmap[leaf];
+        } else {
+            const int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
+            if (px >= 0 && py >= 0 && pz >= 0) {
+                const long long l = linked_leaf(lg, t, px, py, pz);
+                if (l >= 0) r = (int)scmap[l];
+            }
+        }
+        if (r >= 0) {
+            const uint32_t beg = __ldg(bin_off + (size_t)r * 64);
+            e = make_int4(r, (int)beg, (int)(__ldg(bin_off + (size_t)r * 64 + 64) - beg), 0);
+        }
+    } else if (lane == 27) {
+        e = make_int4(ox, oy, oz, slot_of_value(nd.value, ax, ay));
+    }
+    if (lane < 28) gtab[b * 32 + lane] = e;
+}
+
 // One block per linked leaf.  Setup: the ranks of the 3x3x3 neighbour bricks and
 // their point ranges in the home-binned array (a brick's 64 bins are contiguous).
 // Then one of two forms, chosen per brick by the number of points homed in the
@@ -614,8 +652,7 @@ __global__ void k_push_check(TreeView t, LeafGrid lg, const uint32_t* __restrict
 template <typename T>
 // 10 blocks per SM (48 registers; the 20.9 KiB of shared memory per block allows
 // 10): measured 0.774 ms on the fluid frame against 0.787 at 9 and 0.798 at 8
-__global__ void __launch_bounds__(kGatherThreads, 10) k_gather(TreeView t, LeafGrid lg, const int* __restrict__ linked,
-                                                           const uint32_t* __restrict__ scmap,
+__global__ void __launch_bounds__(kGatherThreads, 10) k_gather(TreeView t, LeafGrid lg, const int4* __restrict__ gtab,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
                                                            const int4* __restrict__ offs, int noffs,
@@ -630,11 +667,11 @@ __global__ void __launch_bounds__(kGatherThreads, 10) k_gather(TreeView t, LeafG
     __shared__ int next_sc;  // gather form: next subcell to search
     __shared__ int pslot[27];  // fused apron: slot of the neighbour at each direction, -1: none / no push
 
-    const int leaf = linked[blockIdx.x];
-    const Node nd = t.nodes[0][leaf];
-    const int slot = slot_of_value(nd.value, gp.ax, gp.ay);
+    const int4* rec = gtab + (size_t)blockIdx.x * 32;  // this brick's setup (k_gather_prep)
+    const int4 head = __ldg(rec + 27);
+    const int slot = head.w;
     if (slot < 0) return;
-    const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+    const int ox = head.x, oy = head.y, oz = head.z;
     const int sx0 = ox >> 2, sy0 = oy >> 2, sz0 = oz >> 2;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
@@ -647,20 +684,10 @@ __global__ void __launch_bounds__(kGatherThreads, 10) k_gather(TreeView t, LeafG
         // leaf's rank is its atlas slot
         const bool push_ok = gp.apron != nullptr && __ldg(gp.apron_bad) == 0;
         if (lane < 27) {
-            int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
-            if ((dx | dy | dz) == 0) {
-                r = (int)scmap[leaf];
-            } else {
-                int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
-                if (px >= 0 && py >= 0 && pz >= 0) {
-                    long long l = linked_leaf(lg, t, px, py, pz);
-                    if (l >= 0) r = (int)scmap[l];
-                }
-            }
-            if (r >= 0) {
-                beg = __ldg(bin_off + (size_t)r * 64);
-                cnt = __ldg(bin_off + (size_t)r * 64 + 64) - beg;
-            }
+            const int4 e = __ldg(rec + lane);
+            r = e.x;
+            beg = (uint32_t)e.y;
+            cnt = (uint32_t)e.z;
             nrank[lane] = r;
             nb_beg[lane] = beg;
             pslot[lane] = (push_ok && lane != 13) ? r : -1;
@@ -1173,17 +1200,19 @@ void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* sc
 }
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
-                   void* interior, cudaStream_t s) {
+                   int4* gtab, void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
+    k_gather_prep<<<blocks_for(nbricks * 32, 256), 256, 0, s>>>(t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay,
+                                                                gtab);
     if (gp.dtype == 3)
-        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs, noffs, gp,
+        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
                                                                      (float*)interior);
     else if (gp.dtype == 100)
-        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs, noffs, gp,
+        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
                                                                       (__half*)interior);
     else
-        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, linked, scmap, bin_off, pts, offs,
-                                                                            noffs, gp, (__nv_bfloat16*)interior);
+        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
+                                                                            (__nv_bfloat16*)interior);
 }
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                        const uint32_t* scmap, uint32_t* cnt, cudaStream_t s) {
