@@ -100,6 +100,38 @@ def test_fused_apron_matches_full_apron(gpu_lib, case):
         H.check_apron_self(sa, kw["boundval"] if "boundval" in kw else 0.0)
 
 
+def test_fused_apron_falls_back_when_the_grid_is_not_in_frame_state(gpu_lib):
+    """When the grid is not in the state a frame of the path leaves (here: a second
+    rebuild added leaves and UpdateAtlas was not called, so new leaves have no slot
+    and slots no longer equal linked ranks), the gather's push check fails, nothing
+    is pushed and UpdateApron copies every apron voxel: the atlas is bit-identical to
+    the one the full apron pass leaves."""
+    import torch
+
+    import gbvdb
+
+    pos, vel = _mini_fluid(n=30000, seed=51)
+    f1 = np.maximum(pos, 0.0).astype(np.float32)
+    f2 = np.maximum(pos + 3.0 * vel, 0.0).astype(np.float32)
+    snaps = []
+    for fused in (1, 0):
+        g = gbvdb.Grid(0, (3, 3, 3, 4))
+        g.set_tuning(gbvdb.TUNE_FUSED_APRON, fused)
+        g.add_channel(0)
+        for k, f in enumerate((f1, f1, f2)):
+            n = g.set_points(torch.from_numpy(f).cuda())
+            g.rebuild_topology(n, 2.0)
+            if k < 2:
+                g.update_atlas()
+            _, ln = g.insert_points_subcell(4, n, 2.0)
+            g.gather_levelset(4, n, 1.5, (0, 0, 0), ln)
+            g.update_apron(0, 3.0)
+        torch.cuda.synchronize()
+        snaps.append((g.atlas_map(), g.atlas_bricks(0)))
+    assert np.array_equal(snaps[0][0], snaps[1][0])
+    assert np.array_equal(snaps[0][1].view(np.uint8), snaps[1][1].view(np.uint8))
+
+
 def test_accumulate_topology(gpu_lib):
     pos, vel = _mini_fluid(n=20000, seed=5)
     frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
