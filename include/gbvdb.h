@@ -48,7 +48,7 @@ typedef enum {
     GBVDB_DEPTH_UNSUPPORTED = 4,  /* point extents < 1 brick or > 5 levels (VG.cpp:1187-1194) */
     GBVDB_CAPACITY = 5,           /* a device capacity was exceeded; retry was not possible */
     GBVDB_TIMEOUT = 6,            /* a bounded device wait gave up */
-    GBVDB_NOT_SUPPORTED = 7,      /* configuration outside what this build implements */
+    GBVDB_NOT_SUPPORTED = 7,      /* configuration outside what this library implements */
     GBVDB_NOOP = 8                /* nothing to do (the reference returns early here) */
 } gbvdb_status;
 

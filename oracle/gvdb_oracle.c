@@ -2,8 +2,8 @@
  * gvdb_oracle.c -- CPU oracle for the GVDB point-driven dynamic-topology path.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is a plain-C restatement of the
- * reference's algorithm, used by tests/, by __graft_entry__.smoke() as the
- * checker, and by bench.py as the timed CPU baseline ("port").  It is never
+ * reference's algorithm, used by tests/, by __graft_entry__.smoke() to check
+ * its result, and by bench.py as the timed CPU baseline ("port").  It is never
  * linked into, loaded by, or called from the product library.
  *
  * Every function cites the reference file:line it restates.  Abbreviations:

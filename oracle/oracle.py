@@ -1,7 +1,7 @@
 """ctypes front end for the CPU oracle (oracle/gvdb_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
-checker and by bench.py for the timed CPU baseline.  The product library never
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to check
+its result and by bench.py for the timed CPU baseline.  The product library never
 imports this module.
 
 `OracleGrid` mirrors the reference's VolumeGVDB call sequence for the
