@@ -1311,7 +1311,7 @@ struct gbvdb_grid_s {
     }
 
 // Grids allocate with cudaMallocAsync from the device's default memory pool.  By
-// default that pool returns freed memory to the driver at every synchronisation,
+// default that pool returns freed memory to the CUDA driver at every synchronisation,
 // so a grid that is rebuilt or replaced pays for fresh driver allocations; keep
 // the freed memory in the pool instead (a setting of this process's pool only).
 static void keep_pool_memory(int device) {

@@ -4,7 +4,7 @@
   from its source file kernels/cuda_gvdb_module.cu with the flags of its CMake
   project (PTX, --use_fast_math).  Built only where the reference sources are
   present; the PTX is text, so it also runs on a GPU machine without those
-  sources, where the driver JIT-compiles it.  It is loaded and launched, never
+  sources, where the CUDA driver JIT-compiles it.  It is loaded and launched, never
   read.
 - oracle/_ref/libref_harness.so: oracle/ref_harness.cu (our restatement of the
   reference's host orchestration) built with nvcc; built on demand.
