@@ -631,8 +631,9 @@ __global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ l
     if (lane < 28) gtab[b * 32 + lane] = e;
 }
 
-// One block per linked leaf.  Setup: the ranks of the 3x3x3 neighbour bricks and
-// their point ranges in the home-binned array (a brick's 64 bins are contiguous).
+// One block per linked leaf.  Setup: the brick's record from k_gather_prep (the
+// ranks of the 3x3x3 neighbour bricks and their point ranges in the home-binned
+// array, a brick's 64 bins being contiguous; the origin and the atlas slot).
 // Then one of two forms, chosen per brick by the number of points homed in the
 // neighbourhood (either form is exact; the choice only affects speed):
 //
@@ -652,7 +653,7 @@ __global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ l
 template <typename T>
 // 10 blocks per SM (48 registers; the 20.9 KiB of shared memory per block allows
 // 10): measured 0.774 ms on the fluid frame against 0.787 at 9 and 0.798 at 8
-__global__ void __launch_bounds__(kGatherThreads, 10) k_gather(TreeView t, LeafGrid lg, const int4* __restrict__ gtab,
+__global__ void __launch_bounds__(kGatherThreads, 10) k_gather(const int4* __restrict__ gtab,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
                                                            const int4* __restrict__ offs, int noffs,
@@ -1205,13 +1206,13 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
     k_gather_prep<<<blocks_for(nbricks * 32, 256), 256, 0, s>>>(t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay,
                                                                 gtab);
     if (gp.dtype == 3)
-        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
+        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
                                                                      (float*)interior);
     else if (gp.dtype == 100)
-        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
+        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
                                                                       (__half*)interior);
     else
-        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(t, lg, gtab, bin_off, pts, offs, noffs, gp,
+        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
                                                                             (__nv_bfloat16*)interior);
 }
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
