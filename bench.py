@@ -189,9 +189,20 @@ def cpu_baseline(pos, vel, steps=2):
         tot_t += time.perf_counter() - t0
         tot_pts += pts.shape[0]
     cores = os.cpu_count()
+    # the reference's own host topology path (RebuildTopologyCPU / ActivateSpace, one
+    # thread by design) on the whole first frame: topology only, no gather or apron
+    full = (pos + 0.5 * vel).astype(np.float32)
+    cg = oracle.OracleGrid(LOG2DIMS)
+    t0 = time.perf_counter()
+    reached = cg.rebuild_topology_cpu(full)
+    t_cpu = time.perf_counter() - t0
     return {"value": tot_pts / tot_t, "unit": "points/s", "cores": cores, "kind": "port",
             "sample": "fluid frames 2-%d cropped to x < 32 (%d points/frame, density-preserving), FP64 oracle, "
-                      "OpenMP %d threads" % (steps + 1, pts0.shape[0], cores)}
+                      "OpenMP %d threads" % (steps + 1, pts0.shape[0], cores),
+            "reference_host_topology": {"value": full.shape[0] / t_cpu, "unit": "points/s", "cores": 1,
+                                        "kind": "port", "leaves": cg.node_count(0), "points_reached": reached,
+                                        "what": "RebuildTopologyCPU / ActivateSpace restated (each point "
+                                                "activates its leaf), frame 1, topology only"}}
 
 
 def ref_cuda_inputs_safe(frames):

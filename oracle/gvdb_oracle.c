@@ -100,6 +100,9 @@ typedef struct OGrid {
     int64_t sc_len;
     size_t sc_nleaf;          /* leaf count when the lists were built */
     int nthreads;
+    /* the reference's CPU topology path (og_rebuild_topology_cpu) */
+    uint64_t cpu_root;        /* mRoot, an Elem reference; UNDEFL when empty */
+    size_t cl_used[OG_MAXLEV]; /* child lists taken from pool 1 per level */
 } OGrid;
 
 /* ------------------------------------------------------------------------ */
@@ -422,6 +425,7 @@ OGrid* og_create(int levs, const int* log2dim_leaf_first) {
     g->def_ax = 16; g->def_ay = 16; g->def_az = 1; /* VG.cpp:2348 */
     g->sc_size = 4;
     g->nthreads = 0;
+    g->cpu_root = UNDEFL;
     return g;
 }
 
@@ -1210,3 +1214,184 @@ void og_scatter_density(OGrid* g, const void* posv, int64_t n, int stride, int o
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* The reference's CPU topology path: RebuildTopologyCPU -> ActivateSpace    */
+/* (VG.cpp:1220-1227, 2766-2855, 2726-2763, 2707-2723, 2980-3027, 2915-2931, */
+/* 2858-2875, 3079-3091; getPosFromBit / getBitPos VG.h:598-608).  Each      */
+/* point activates the leaf that contains it, creating the nodes on the way  */
+/* down; a point outside the root grows the tree upwards (Reparent).  Node    */
+/* references are Elem(0, lev, index); a node's child list is taken from      */
+/* pool 1 at its first child (InsertChild, no bitmasks) and filled with 0xFF. */
+/* This is the host path the reference uses without a GPU topology pass; it   */
+/* runs on an empty grid and is the CPU baseline timed beside the GPU path.   */
+
+static int ref_lev(uint64_t e) { return (int)((e >> 8) & 0xFF); }
+static size_t ref_ndx(uint64_t e) { return (size_t)(e >> 16); }
+static ONode* cpu_node(OGrid* g, uint64_t id) { return &g->nodes[ref_lev(id)][ref_ndx(id)]; }
+
+/* AllocateNode + SetupNode (VG.cpp:2506-2524): marker (mFlags) = true */
+static uint64_t cpu_alloc(OGrid* g, int lev, const int32_t pos[3]) {
+    pool_reserve(g, lev, g->ncnt[lev] + 1);
+    size_t i = g->ncnt[lev]++;
+    g->nused[lev]++;
+    ONode* n = &g->nodes[lev][i];
+    memset(n, 0, sizeof(ONode));
+    n->lev = (uint8_t)lev;
+    n->pos[0] = pos[0]; n->pos[1] = pos[1]; n->pos[2] = pos[2];
+    n->childlist = UNDEFL;
+    n->parent = UNDEFL;
+    n->value[0] = n->value[1] = n->value[2] = -1;
+    n->flags = 1;
+    return Elem(0, lev, i);
+}
+
+/* GetCoveringNode (VG.cpp:2915-2931); levels past the configured ones have no
+ * range here (the reference reads unset level dimensions): 0 = no cover */
+static int cpu_cover(const OGrid* g, int lev, const int32_t pos[3], int32_t out[3]) {
+    if (lev == OG_MAXLEV - 1) { out[0] = out[1] = out[2] = 0; return 1; }
+    if (lev >= g->levs) return 0;
+    int64_t rg = og_range(g, lev);
+    for (int a = 0; a < 3; a++) {
+        int64_t np = (int64_t)pos[a] / rg * rg; /* C truncation */
+        if (pos[a] < np) np -= rg;
+        out[a] = (int32_t)np;
+    }
+    return 1;
+}
+
+/* getPosInNode (VG.cpp:2858-2875) */
+static int cpu_pos_in_node(const OGrid* g, const ONode* n, const int32_t pos[3], uint32_t* bit) {
+    int lev = n->lev;
+    int64_t rg = og_range(g, lev);
+    int64_t r = og_res(g, lev);
+    int64_t p[3];
+    for (int a = 0; a < 3; a++) {
+        p[a] = (int64_t)pos[a] - n->pos[a];
+        if (p[a] < 0 || p[a] >= rg) { *bit = 0; return 0; }
+    }
+    for (int a = 0; a < 3; a++) p[a] = p[a] * r / rg;
+    *bit = (uint32_t)((p[2] * r + p[1]) * r + p[0]);
+    return 1;
+}
+
+/* getChildNode (VG.cpp:3079-3091) */
+static uint64_t cpu_get_child(const OGrid* g, const ONode* n, uint32_t b) {
+    if (n->childlist == UNDEFL) return UNDEF64;
+    return g->clist[n->lev][ref_ndx(n->childlist) * og_cl_len(g, n->lev) + b];
+}
+
+/* InsertChild (VG.cpp:2980-3027), the child-list (non-bitmask) form */
+static uint64_t cpu_insert_child(OGrid* g, uint64_t nodeid, uint64_t childid, uint32_t i) {
+    cpu_node(g, childid)->parent = nodeid;
+    ONode* cur = cpu_node(g, nodeid);
+    int lev = cur->lev;
+    size_t cl = og_cl_len(g, lev);
+    if (cur->childlist == UNDEFL) {
+        size_t k = g->cl_used[lev]++; /* PoolAlloc(1, lev): k < node count of the level */
+        cur->childlist = Elem(1, lev, k);
+        memset(g->clist[lev] + k * cl, 0xFF, cl * sizeof(uint64_t));
+    }
+    g->clist[lev][ref_ndx(cur->childlist) * cl + i] = childid;
+    return childid;
+}
+
+/* AddChildNode (VG.cpp:2707-2723) with getPosFromBit (VG.h:602-608) */
+static uint64_t cpu_add_child(OGrid* g, uint64_t nodeid, uint32_t b) {
+    const ONode* par = cpu_node(g, nodeid);
+    int plev = par->lev;
+    int logr = g->log2dim[plev];
+    uint32_t mask = (1u << logr) - 1u;
+    int64_t crg = og_range(g, plev - 1);
+    int32_t pos[3] = {(int32_t)(par->pos[0] + (int64_t)(b & mask) * crg),
+                      (int32_t)(par->pos[1] + (int64_t)((b >> logr) & mask) * crg),
+                      (int32_t)(par->pos[2] + (int64_t)((b >> (2 * logr)) & mask) * crg)};
+    uint64_t child = cpu_alloc(g, plev - 1, pos);
+    return cpu_insert_child(g, nodeid, child, b);
+}
+
+static uint64_t cpu_activate(OGrid* g, uint64_t nodeid, const int32_t pos[3], int* bnew, uint64_t stopnode,
+                             int stoplev);
+
+/* Reparent (VG.cpp:2726-2763) */
+static uint64_t cpu_reparent(OGrid* g, int lev, uint64_t prevroot, const int32_t pos[3], int* bnew) {
+    const ONode* pr = cpu_node(g, prevroot);
+    int32_t prevpos[3] = {pr->pos[0], pr->pos[1], pr->pos[2]};
+    int32_t p1[3] = {0, 0, 0}, p2[3];
+    int cover = 0;
+    while (!cover && lev < OG_MAXLEV) {
+        lev++;
+        if (!cpu_cover(g, lev, pos, p1) || !cpu_cover(g, lev, prevpos, p2)) { lev = OG_MAXLEV; break; }
+        cover = p1[0] == p2[0] && p1[1] == p2[1] && p1[2] == p2[2];
+    }
+    if (lev >= OG_MAXLEV) return UNDEFL; /* level limit: the existing root stays */
+    uint64_t newroot = cpu_alloc(g, lev, p1);
+    int bn = 0;
+    cpu_activate(g, newroot, prevpos, &bn, prevroot, 0); /* the stop node joins the old root */
+    uint64_t leaf = cpu_activate(g, newroot, pos, bnew, UNDEFL, 0);
+    g->cpu_root = newroot;
+    if (leaf == UNDEFL) return UNDEFL;
+    return cpu_node(g, leaf)->parent;
+}
+
+/* ActivateSpace(nodeid, pos, bNew, stopnode, stoplev) (VG.cpp:2795-2855) */
+static uint64_t cpu_activate(OGrid* g, uint64_t nodeid, const int32_t pos[3], int* bnew, uint64_t stopnode,
+                             int stoplev) {
+    for (int guard = 0; guard < 4 * OG_MAXLEV; guard++) {
+        if (g->cpu_root == UNDEFL && nodeid == g->cpu_root) { /* new root covering pos */
+            int32_t p[3];
+            if (!cpu_cover(g, stoplev, pos, p)) return UNDEFL;
+            g->cpu_root = cpu_alloc(g, stoplev, p);
+            nodeid = g->cpu_root;
+        }
+        const ONode* cur = cpu_node(g, nodeid);
+        uint32_t b;
+        if (cpu_pos_in_node(g, cur, pos, &b)) {
+            const int lev = cur->lev;
+            if (stopnode != UNDEFL) {
+                const ONode* sn = cpu_node(g, stopnode);
+                if (pos[0] == sn->pos[0] && pos[1] == sn->pos[1] && pos[2] == sn->pos[2] &&
+                    cpu_get_child(g, cur, b) == UNDEF64 && lev == sn->lev + 1)
+                    return cpu_insert_child(g, nodeid, stopnode, b);
+            }
+            if (lev == stoplev) return nodeid;
+            uint64_t child;
+            if (cpu_get_child(g, cur, b) == UNDEF64) {
+                child = cpu_add_child(g, nodeid, b);
+                if (lev == 1) *bnew = 1;
+            } else {
+                child = cpu_get_child(g, cur, b);
+            }
+            if (ref_lev(child) == 0) return child; /* isLeaf */
+            nodeid = child;
+        } else {
+            uint64_t parent = cur->parent;
+            if (parent == UNDEFL) {
+                parent = cpu_reparent(g, cur->lev, nodeid, pos, bnew);
+                if (parent == UNDEFL) return UNDEFL;
+            }
+            nodeid = parent;
+        }
+    }
+    return UNDEFL;
+}
+
+/* RebuildTopologyCPU (VG.cpp:1220-1227): p = pos + orig, ActivateSpace(Vector3DF p),
+ * whose Vector3DF -> Vector3DI conversion truncates each coordinate.  Returns the
+ * number of points that reached a leaf. */
+int64_t og_rebuild_topology_cpu(OGrid* g, const void* posv, int64_t n, int stride, int off, const float orig[3]) {
+    const char* pos = (const char*)posv;
+    int64_t ok = 0;
+    for (int64_t i = 0; i < n; i++) {
+        float p[3];
+        load_point(pos, i, stride, off, p);
+        float w[3] = {p[0] + orig[0], p[1] + orig[1], p[2] + orig[2]};
+        int32_t v[3] = {(int32_t)w[0], (int32_t)w[1], (int32_t)w[2]};
+        int bnew = 0;
+        if (cpu_activate(g, g->cpu_root, v, &bnew, UNDEFL, 0) != UNDEFL) ok++;
+    }
+    return ok;
+}
+/* level of the CPU path's root (-1 when empty) */
+int og_cpu_root_level(const OGrid* g) { return g->cpu_root == UNDEFL ? -1 : ref_lev(g->cpu_root); }
+

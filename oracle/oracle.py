@@ -105,6 +105,10 @@ def lib():
         L.og_apron_faces_f32.argtypes = [vp, vp, vp]
         L.og_apron_full_f32.argtypes = [vp, vp, f32]
         L.og_smooth_f32.argtypes = [vp, vp, f32, f32]
+        L.og_rebuild_topology_cpu.restype = i64
+        L.og_rebuild_topology_cpu.argtypes = [vp, vp, i64, i32, i32, fp3]
+        L.og_cpu_root_level.restype = i32
+        L.og_cpu_root_level.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -170,6 +174,16 @@ class OracleGrid:
     def rebuild_topology(self, points, radius, orig=(0, 0, 0)):
         p, n, stride = self._pts(points)
         return lib().og_rebuild_topology(self._h, p.ctypes.data, n, stride, 0, float(radius), _f3(orig))
+
+    def rebuild_topology_cpu(self, points, orig=(0, 0, 0)):
+        """The reference's host path RebuildTopologyCPU / ActivateSpace (every point
+        activates the leaf containing it; the root grows upwards) on an empty grid.
+        Returns the number of points that reached a leaf."""
+        p, n, stride = self._pts(points)
+        return int(lib().og_rebuild_topology_cpu(self._h, p.ctypes.data, n, stride, 0, _f3(orig)))
+
+    def cpu_root_level(self):
+        return int(lib().og_cpu_root_level(self._h))
 
     def accumulate_topology(self, points, radius, orig=(0, 0, 0), min_depth=1):
         p, n, stride = self._pts(points)
