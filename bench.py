@@ -37,11 +37,8 @@ N_FLUID = 4_194_304
 FRAMES = 10
 LOG2DIMS = (3, 3, 3, 4)
 R_TOPO, R_INSERT, RHO, BOUND = 4.0, 4.0, 2.0, 3.0
-# dense-form threshold per workload (candidate points per brick above which the gather
-# takes the warp-per-subcell form), from sweeps on GB300: the fluid frame is flat from
-# 3072 to 8192 (2048: +1%); the surface workload is 10% faster at 4096 than at 2048 and
-# flat above; the library default (2048) suits the 200,000-point shell (4096: 2.8x slower)
-DENSE_MIN_FLUID, DENSE_MIN_SURFACE = 4096, 4096
+# the gather's dense-form threshold is chosen by the library's autotuner (the warm-up
+# frames measure its candidates)
 SAMPLE_BOX = ((0.0, 0.0, 0.0), (32.0, 512.0, 512.0))  # CPU sample: the x < 32 slab of each frame
 
 
@@ -414,7 +411,6 @@ def bench_surface(args, steps=5):
     for name, dt in (("f32", gbvdb.T_FLOAT), ("f16", gbvdb.T_HALF), ("bf16", gbvdb.T_BFLOAT16)):
         g = gbvdb.Grid(0, (4, 4, 3, 4), stream=stream)
         g.set_channel_default(64, 64, 1)
-        g.set_tuning(gbvdb.TUNE_DENSE_MIN, DENSE_MIN_SURFACE)
         g.add_channel(0, dt)
         n = g.set_points(d)
 
@@ -490,7 +486,6 @@ def bench_ours(args):
     stream = torch.cuda.current_stream()
     grid = gbvdb.Grid(local, LOG2DIMS, stream=stream)
     grid.set_tuning(gbvdb.TUNE_FUSED_APRON, args.fused_apron)
-    grid.set_tuning(gbvdb.TUNE_DENSE_MIN, DENSE_MIN_FLUID)
     grid.add_channel(0, gbvdb.T_FLOAT)
 
     state = {"frame": 0}

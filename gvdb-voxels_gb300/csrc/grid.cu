@@ -151,6 +151,51 @@ struct gbvdb_grid_s {
 
     // tuning
     int dense_min = 2048;
+    // Dense-form threshold autotuner (on until GBVDB_TUNE_DENSE_MIN is set): the
+    // gathers of a workload try each candidate once, timed with events on the
+    // grid's stream, and the faster one is kept; a linked-brick count that moves
+    // by more than 2x starts a new round.  Both forms give the same bits, so only
+    // the time depends on the choice.  Which value wins depends on how the points
+    // are spread (measured: a thick shell wants 2048, the fluid frame and the
+    // surface workload 4096).
+    static constexpr int kTuneN = 2;
+    static constexpr int kTuneCand[kTuneN] = {2048, 4096};
+    bool tune_auto = true;
+    bool tune_pending = false;
+    int tune_step = kTuneN;  // candidates measured in the current round (kTuneN: none running)
+    long long tune_bricks = -1;
+    cudaEvent_t tune_ev[2 * kTuneN] = {};
+
+    // the threshold for this gather, and the candidate slot it measures (-1: none)
+    int tune_pick(long long bricks, int* slot) {
+        *slot = -1;
+        if (!tune_auto) return dense_min;
+        if (tune_pending) {  // the last round's timings, once its events have completed
+            if (cudaEventQuery(tune_ev[2 * kTuneN - 1]) == cudaSuccess) {
+                float best = 0.0f;
+                int bi = -1;
+                for (int i = 0; i < kTuneN; i++) {
+                    float ms = 0.0f;
+                    if (cudaEventElapsedTime(&ms, tune_ev[2 * i], tune_ev[2 * i + 1]) != cudaSuccess) { bi = -1; break; }
+                    if (bi < 0 || ms < best) { best = ms; bi = i; }
+                }
+                cudaGetLastError();
+                if (bi >= 0) dense_min = kTuneCand[bi];
+                tune_pending = false;
+            } else {
+                cudaGetLastError();  // not ready yet (cudaErrorNotReady): decide at a later gather
+            }
+        }
+        if (!tune_pending && tune_step >= kTuneN && (tune_bricks < 0 || bricks > 2 * tune_bricks || 2 * bricks < tune_bricks)) {
+            tune_step = 0;  // a new workload: measure the candidates again
+            tune_bricks = bricks;
+        }
+        if (tune_step < kTuneN && !tune_pending) {
+            *slot = tune_step;
+            return kTuneCand[tune_step];
+        }
+        return dense_min;
+    }
 
     // Fused apron: a gather also writes each brick's boundary voxels into its
     // neighbours' apron records, and the next UpdateApron of that channel only
@@ -857,7 +902,8 @@ struct gbvdb_grid_s {
             launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
                                 interior, stream);
         } else {
-            gp.dense_min = dense_min;
+            int tslot = -1;
+            gp.dense_min = tune_pick(sc_nbricks, &tslot);
             // fused apron: needs the dense leaf lookup (the apron pass resolves
             // neighbours with the same table) and an apron of one voxel
             const bool push = fused_apron && lgv.cells && ch[chan].apron == 1 && atlas_last > 0;
@@ -871,8 +917,13 @@ struct gbvdb_grid_s {
                                   ptr<int>(push_bad), stream);
             }
             grow(gtab, (size_t)std::max(sc_nbricks, 1ll) * 32 * 16);
+            if (tslot >= 0) check(cudaEventRecord(tune_ev[2 * tslot], stream), "tune event");
             launch_gather(t, lgv, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(scmap), ptr<uint32_t>(bin_off),
                           ptr<float4>(sorted), ptr<int4>(offs_buf), noffs, gp, ptr<int4>(gtab), interior, stream);
+            if (tslot >= 0) {
+                check(cudaEventRecord(tune_ev[2 * tslot + 1], stream), "tune event");
+                if (++tune_step == kTuneN) tune_pending = true;
+            }
             if (push) pushed_ver[chan] = layout_ver;
         }
         check_launch("gather");
@@ -1350,6 +1401,7 @@ gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
         return GBVDB_OUT_OF_MEMORY;
     }
     for (int i = 0; i < 64; i++) cudaEventCreate(&g->ev[i]);
+    for (int i = 0; i < 2 * gbvdb_grid_s::kTuneN; i++) cudaEventCreate(&g->tune_ev[i]);
     *out = g;
     return GBVDB_OK;
 }
@@ -1367,6 +1419,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
     cudaStreamSynchronize(g->stream);
     for (int i = 0; i < 64; i++) cudaEventDestroy(g->ev[i]);
+    for (int i = 0; i < 2 * gbvdb_grid_s::kTuneN; i++) cudaEventDestroy(g->tune_ev[i]);
     cudaFreeHost(g->pinned);
     delete g;
     return GBVDB_OK;
@@ -1799,6 +1852,16 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
     if (param == GBVDB_TUNE_DENSE_MIN) {
         if (value < 0 || value > (1ll << 31)) return GBVDB_INVALID_ARG;
         g->dense_min = (int)value;
+        g->tune_auto = false;  // an explicit threshold ends the autotuner
+        g->tune_pending = false;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_AUTOTUNE) {
+        if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
+        g->tune_auto = value != 0;
+        g->tune_pending = false;
+        g->tune_step = gbvdb_grid_s::kTuneN;
+        g->tune_bricks = -1;
         return GBVDB_OK;
     }
     if (param == GBVDB_TUNE_FUSED_APRON) {

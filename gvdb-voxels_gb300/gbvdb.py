@@ -61,6 +61,7 @@ class JobResult(ctypes.Structure):
                 ("t_end_ms", ctypes.c_double)]
 TUNE_DENSE_MIN = 1
 TUNE_FUSED_APRON = 2
+TUNE_AUTOTUNE = 3
 FUNC_SMOOTH = 113
 
 

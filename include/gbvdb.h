@@ -211,7 +211,12 @@ GBVDB_API gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* de
 GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** interior, void** apron);
 /* tuning parameters (no counterpart in the reference) */
 #define GBVDB_TUNE_DENSE_MIN 1   /* candidate points per brick above which gathers use the warp-per-subcell
-                                    form instead of the scatter form (default 2048) */
+                                    form instead of the scatter form (default 2048; setting it turns the
+                                    autotuner off) */
+#define GBVDB_TUNE_AUTOTUNE 3    /* 1 (default): the gathers of a workload try 2048 and 4096 for the
+                                    threshold above, timed with events on the grid's stream, and keep the
+                                    faster; a linked-brick count that changes by more than 2x starts a new
+                                    round.  Both forms give the same bits.  0: the threshold stays fixed. */
 #define GBVDB_TUNE_FUSED_APRON 2 /* 1 (default): a gather (binned form, apron 1, dense leaf lookup) also
                                     writes every brick's boundary voxels into its neighbours' apron records,
                                     and the next UpdateApron of that channel, with no topology, atlas or

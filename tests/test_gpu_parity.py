@@ -132,6 +132,23 @@ def test_fused_apron_falls_back_when_the_grid_is_not_in_frame_state(gpu_lib):
     assert np.array_equal(snaps[0][1].view(np.uint8), snaps[1][1].view(np.uint8))
 
 
+def test_autotuned_threshold_gives_the_same_atlas(gpu_lib):
+    """The dense-form threshold autotuner only changes which gather form a brick takes;
+    both forms give the same bits, so frames with the autotuner (measuring its
+    candidates, then keeping one) equal frames at each fixed threshold bit for bit."""
+    import gbvdb
+
+    pos, vel = _mini_fluid(n=40000, seed=61)
+    frames = [(pos + 0.5 * k * vel).astype(np.float32) for k in range(1, 6)]
+    kw = dict(frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0, export_subcells=False)
+    _, auto = H.run_gpu(None, **kw)
+    for dm in (2048, 4096):
+        _, fixed = H.run_gpu(None, dense_min=dm, **kw)
+        for a, b in zip(auto, fixed):
+            assert np.array_equal(a["bricks"].view(np.uint8), b["bricks"].view(np.uint8))
+            assert a["checksum"] == b["checksum"]
+
+
 def test_accumulate_topology(gpu_lib):
     pos, vel = _mini_fluid(n=20000, seed=5)
     frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
