@@ -417,7 +417,7 @@ constexpr int kQueue = 64;  // per-warp point queue of the gather form (SoA x, y
 constexpr int kLive = 256;  // live points per batch of the scatter form
 constexpr int kScratch = kLive * 16 > (kGatherThreads / 32) * 3 * kQueue * 4 ? kLive * 16
                                                                               : (kGatherThreads / 32) * 3 * kQueue * 4;
-static_assert(kGatherThreads == 128, "the scatter form gives each of the 4 warps 4 tile rows");
+static_assert(kGatherThreads == 128, "push_apron maps 128 threads onto the two faces of an axis");
 
 // packed FP32 pairs (f32x2 arithmetic, round-to-nearest, no contraction)
 typedef unsigned long long f32x2;
@@ -709,11 +709,10 @@ __global__ void __launch_bounds__(kGatherThreads, 10) k_gather(const int4* __res
         // ------------------------------------------------------ scatter form
         // A point's reach inside this brick: its member subcells, cut to the
         // voxels within rcut of it on every axis (brick-local voxel box).  The
-        // live points of a batch of candidates go to a shared list; then every
-        // warp walks the whole list but updates only the 4 tile rows y it owns
-        // (lanes: 8 columns x 4 rows; x in groups of 8; z walked in a loop over
-        // the group's reach), so no two threads ever update the same voxel at
-        // once and no atomics are needed.
+        // live points of a batch of candidates go to a shared list; then the warps
+        // take the list's entries in turn, each covering its entry's whole reach
+        // (lanes: 8 columns x 4 rows; rows in groups of 4, x in groups of 8, z
+        // walked two at a time over the group's reach) with shared atomicMin.
         float4* live_pts = reinterpret_cast<float4*>(scratch);
         for (uint32_t cbase = 0; cbase < ncand; cbase += kLive) {
             if (threadIdx.x == 0) nlive = 0;
@@ -749,56 +748,58 @@ __global__ void __launch_bounds__(kGatherThreads, 10) k_gather(const int4* __res
             const int nl = nlive;
             const int xl = lane & 7, yl = lane >> 3;
             const float rc2 = __fmul_rn(gp.rcut, gp.rcut);
-            for (int e = 0; e < nl; e++) {
+            // warps take the live entries in turn; a warp covers all of its entry's
+            // reach (rows in groups of 4), so an entry is decoded once, not once per
+            // warp, and warps may update the same voxel: shared atomicMin
+            for (int e = warp; e < nl; e += kGatherThreads / 32) {
                 const float4 L = live_pts[e];
                 const int bx = __float_as_int(L.w);
                 const int x0 = bx & 15, x1 = (bx >> 4) & 15;
-                const int y0 = max((bx >> 8) & 15, 4 * warp), y1 = min((bx >> 12) & 15, 4 * warp + 3);
+                const int Y0 = (bx >> 8) & 15, Y1 = (bx >> 12) & 15;
                 const int z0 = (bx >> 16) & 15, z1 = (bx >> 20) & 15;
-                if (y0 > y1) continue;
-                // brick-local position; the distance from it to the nearest of this
-                // warp's rows (uniform over the warp)
+                // brick-local position
                 const float lx = fsub(L.x, (float)ox), ly = fsub(L.y, (float)oy), lz = fsub(L.z, (float)oz);
-                const float gy = fmaxf(0.0f, fmaxf((float)y0 - ly, ly - (float)y1));
-                const int y = y0 + yl;
-                const float dy = fsub(L.y, (float)(oy + y));
-                for (int xs = x0; xs <= x1; xs += 8) {
-                    // z reach of this group of 8 columns: the sphere of radius rcut cut at
-                    // the group's nearest column (a superset of every voxel with d^2 < T)
-                    const int xe = min(xs + 7, x1);
-                    const float gx = fmaxf(0.0f, fmaxf((float)xs - lx, lx - (float)xe));
-                    const float zr2 = rc2 - __fmaf_rn(gy, gy, gx * gx);
-                    if (!(zr2 >= 0.0f)) continue;
-                    const float zr = sqrt_approx(zr2);  // rcut's margin (>= 0.01) covers its error
-                    const int za = max(z0, (int)ceilf(lz - zr)), zb = min(z1, (int)floorf(lz + zr));
-                    const int x = xs + xl;
-                    if (za <= zb && x <= xe && y <= y1) {
-                        const float dx = fsub(L.x, (float)(ox + x));
-                        const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                        if (__float_as_uint(dxy) < gp.tbits) {
-                            uint32_t* col = tile + (za << 8) + (y << 4) + x;
-                            const float fz = (float)(oz + za);  // integer-valued: steps of 1 and 2 are exact
-                            const f32x2 pzz = f2pack(L.z, L.z), dxy2 = f2pack(dxy, dxy);
-                            f32x2 fzz = f2pack(fz, fz + 1.0f);
-                            const f32x2 two = f2pack(2.0f, 2.0f);
-                            int z = za;
-                            for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
-                                const f32x2 dz = f2sub(pzz, fzz);
-                                const f32x2 d = f2fma(dz, dz, dxy2);
-                                fzz = f2add(fzz, two);
-                                const uint32_t d0 = __float_as_uint(f2lo(d)), d1 = __float_as_uint(f2hi(d));
-                                if (d0 < col[0]) col[0] = d0;
-                                if (d1 < col[256]) col[256] = d1;
-                            }
-                            if (z == zb) {
-                                const float dz = fsub(L.z, f2lo(fzz));
-                                const uint32_t d = __float_as_uint(__fmaf_rn(dz, dz, dxy));
-                                if (d < *col) *col = d;
+                for (int ys = Y0; ys <= Y1; ys += 4) {
+                    const int ye = min(ys + 3, Y1);
+                    // distance from the point to the nearest row of this group (warp-uniform)
+                    const float gy = fmaxf(0.0f, fmaxf((float)ys - ly, ly - (float)ye));
+                    const int y = ys + yl;
+                    const float dy = fsub(L.y, (float)(oy + y));
+                    for (int xs = x0; xs <= x1; xs += 8) {
+                        // z reach of this group of 8 columns: the sphere of radius rcut cut at
+                        // the group's nearest column (a superset of every voxel with d^2 < T)
+                        const int xe = min(xs + 7, x1);
+                        const float gx = fmaxf(0.0f, fmaxf((float)xs - lx, lx - (float)xe));
+                        const float zr2 = rc2 - __fmaf_rn(gy, gy, gx * gx);
+                        if (!(zr2 >= 0.0f)) continue;
+                        const float zr = sqrt_approx(zr2);  // rcut's margin (>= 0.01) covers its error
+                        const int za = max(z0, (int)ceilf(lz - zr)), zb = min(z1, (int)floorf(lz + zr));
+                        const int x = xs + xl;
+                        if (za <= zb && x <= xe && y <= ye) {
+                            const float dx = fsub(L.x, (float)(ox + x));
+                            const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                            if (__float_as_uint(dxy) < gp.tbits) {
+                                uint32_t* col = tile + (za << 8) + (y << 4) + x;
+                                const float fz = (float)(oz + za);  // integer-valued: steps of 1 and 2 are exact
+                                const f32x2 pzz = f2pack(L.z, L.z), dxy2 = f2pack(dxy, dxy);
+                                f32x2 fzz = f2pack(fz, fz + 1.0f);
+                                const f32x2 two = f2pack(2.0f, 2.0f);
+                                int z = za;
+                                for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
+                                    const f32x2 dz = f2sub(pzz, fzz);
+                                    const f32x2 d = f2fma(dz, dz, dxy2);
+                                    fzz = f2add(fzz, two);
+                                    atomicMin(col, __float_as_uint(f2lo(d)));
+                                    atomicMin(col + 256, __float_as_uint(f2hi(d)));
+                                }
+                                if (z == zb) {
+                                    const float dz = fsub(L.z, f2lo(fzz));
+                                    atomicMin(col, __float_as_uint(__fmaf_rn(dz, dz, dxy)));
+                                }
                             }
                         }
                     }
                 }
-                __syncwarp();  // this entry's updates are visible to every lane before the next
             }
             __syncthreads();  // the list is refilled by the next batch
         }
