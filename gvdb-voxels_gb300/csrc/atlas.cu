@@ -338,8 +338,19 @@ __global__ void k_slot_sums(const AtlasNode* __restrict__ amap, int used, const 
 // single block: fixed-order sum of the per-slot partials
 __global__ void k_sum_partials(const double* __restrict__ partials, int used, double* __restrict__ out) {
     __shared__ double red[32];
-    double acc = 0.0;
-    for (int s = threadIdx.x; s < used; s += blockDim.x) acc += partials[s];
+    // four running sums per thread so that four loads are in flight at a time;
+    // a fixed order, so the result is deterministic
+    const int bd = (int)blockDim.x;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int s = threadIdx.x;
+    for (; s + 3 * bd < used; s += 4 * bd) {
+        a0 += partials[s];
+        a1 += partials[s + bd];
+        a2 += partials[s + 2 * bd];
+        a3 += partials[s + 3 * bd];
+    }
+    for (; s < used; s += bd) a0 += partials[s];
+    double acc = (a0 + a1) + (a2 + a3);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
