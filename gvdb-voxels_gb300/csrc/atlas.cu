@@ -228,26 +228,6 @@ __device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 __device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
 
 template <typename T>
-__global__ void k_checksum(const AtlasNode* __restrict__ amap, int used, const T* __restrict__ interior, double* out) {
-    double acc = 0;
-    long long total = (long long)used * 4096;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        int s = (int)(i >> 12);
-        if (amap[s].leaf < 0) continue;
-        acc += (double)to_f32(interior[i]);
-    }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
-    __shared__ double red[32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-        if (threadIdx.x == 0) atomicAdd(out, v);
-    }
-}
-
-template <typename T>
 __device__ __forceinline__ T from_f32(float v);
 template <>
 __device__ __forceinline__ float from_f32<float>(float v) { return v; }
@@ -543,16 +523,6 @@ void launch_export_bricks(const void* interior, const void* apron, int used, int
     else
         k_export_bricks<__half><<<gs_blocks(total, 256), 256, 0, s>>>((const __half*)interior, (const __half*)apron,
                                                                        used, (__half*)out);
-}
-void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* interior, double* out, cudaStream_t s) {
-    if (used <= 0) return;
-    long long total = (long long)used * 4096;
-    if (dtype == 3)
-        k_checksum<float><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const float*)interior, out);
-    else if (dtype == 100)
-        k_checksum<__half><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __half*)interior, out);
-    else
-        k_checksum<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, out);
 }
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s) {

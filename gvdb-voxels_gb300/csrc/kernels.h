@@ -87,8 +87,6 @@ void launch_scatter_density(const Node* leaves, long long nleaf, const uint32_t*
 // deterministic FP64 channel sum: per-slot partials, then one fixed-order block
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s);
-void launch_checksum(const AtlasNode* amap, int used, int dtype, const void* interior, double* out,
-                     cudaStream_t s);
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value,
                           cudaStream_t s);
 // allocation-free checksum: scratch in a static device array (max slots noalloc_max_slots())
