@@ -610,17 +610,10 @@ cudaError_t checksum_noalloc(const AtlasNode* amap, int used, int dtype, const v
         partials = addr[dev];
     }
     if (used < 0 || used > kNoAllocMaxSlots) return cudaErrorInvalidValue;
-    if (used > 0) {
-        unsigned blocks = (unsigned)std::min(used, 152 * 8);
-        if (dtype == 3)
-            k_slot_sums<float><<<blocks, 256, 0, s>>>(amap, used, (const float*)interior, partials);
-        else if (dtype == 100)
-            k_slot_sums<__half><<<blocks, 256, 0, s>>>(amap, used, (const __half*)interior, partials);
-        else
-            k_slot_sums<__nv_bfloat16><<<blocks, 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
-    }
-    k_sum_partials<<<1, 1024, 0, s>>>(partials, used, dev_out);
-    return cudaGetLastError();
+    // the same launches as gbvdb_checksum, so both give the same bits; launch errors
+    // are checked by the caller like every other launch of the grid
+    launch_checksum_slots(amap, used, dtype, interior, partials, dev_out, s);
+    return cudaSuccess;
 }
 
 }  // namespace gbvdb

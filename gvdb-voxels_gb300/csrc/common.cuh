@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gbvdb_device.cuh"
+
 namespace gbvdb {
 
 constexpr int kMaxLev = 10;
@@ -227,23 +229,10 @@ __device__ __forceinline__ void load_pos(const char* base, long long i, int stri
 //   edges  [1536 + e*16, +16) e = 0..3 along x (y,z in {0,17}), 4..7 along y
 //          (x,z), 8..11 along z (x,y); bit order (high coordinate == 17);
 //   corners [1728 + c) c = (z==17)*4 + (y==17)*2 + (x==17).
-// padded-brick coordinate (x,y,z in [0,18)) on the apron shell -> record index
-__host__ __device__ inline int apron_index(int x, int y, int z) {
-    const bool bx = x == 0 || x == 17, by = y == 0 || y == 17, bz = z == 0 || z == 17;
-    const int hx = x == 17, hy = y == 17, hz = z == 17;
-    const int nb = (int)bx + (int)by + (int)bz;
-    if (nb == 1) {
-        if (bx) return (0 + hx) * 256 + (z - 1) * 16 + (y - 1);
-        if (by) return (2 + hy) * 256 + (z - 1) * 16 + (x - 1);
-        return (4 + hz) * 256 + (y - 1) * 16 + (x - 1);
-    }
-    if (nb == 2) {
-        if (!bx) return 1536 + (hz * 2 + hy) * 16 + (x - 1);
-        if (!by) return 1536 + (4 + hz * 2 + hx) * 16 + (y - 1);
-        return 1536 + (8 + hy * 2 + hx) * 16 + (z - 1);
-    }
-    return 1728 + hz * 4 + hy * 2 + hx;
-}
+// padded-brick coordinate (x,y,z in [0,18)) on the apron shell -> record index; the
+// layout is the public one of include/gbvdb_device.cuh, which consumer kernels use
+__host__ __device__ inline int apron_index(int x, int y, int z) { return gbvdb_apron_index(x, y, z); }
+static_assert(kApronStride == GBVDB_APRON_STRIDE, "apron record stride");
 
 // inverse of apron_index: record index k in [0, 1736) -> padded-brick coordinate
 // on the apron shell.  The voxel comes from the neighbour at direction

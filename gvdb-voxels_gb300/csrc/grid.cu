@@ -98,12 +98,13 @@ struct gbvdb_grid_s {
     int root_lev = -1;
     int root_pos[3] = {0, 0, 0};
     float posmin[3] = {0, 0, 0}, posmax[3] = {0, 0, 0};
-    int bounds[6] = {0, 0, 0, 0, 0, 0};
+    int bounds[6] = {0, 0, 0, 0, 0, 0};  // ComputeBounds of the last FinishTopology (mObjMin, mObjMax)
+    bool bounds_valid = false;
 
     // points (SetPoints, VG.cpp:4900-4908)
     PointSrc pts{nullptr, 0, 12, 0};
     const void* vel = nullptr;
-    const void* clr = nullptr;
+    ClrSrc clr{nullptr, 4, 0};  // point colours (RGBA8 uint per point), base null: none
 
     // atlas
     int def_ax = 16, def_ay = 16, def_az = 1;  // SetChannelDefault(16,16,1), VG.cpp:2348
@@ -121,8 +122,9 @@ struct gbvdb_grid_s {
     long long sc_nleaf = 0, sc_nbricks = 0, sc_len = 0, sc_orphans = 0;
     bool lists_valid = false;
     Quant sc_quant{};  // position quantisation of the last insert (FP16 variant)
-    DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted;
-    DevBuf list_cnt, list_off, list_pts;
+    ClrSrc sc_clr{nullptr, 4, 0};  // colours the last insert carried (base null: none)
+    DevBuf scmap, linked, bin_cnt, bin_off, bin_of, rank_of, sorted, sorted_clr;
+    DevBuf list_cnt, list_off, list_pts, list_clr;
     DevBuf offs_buf;
     // dense leaf lookup over the brick box of every leaf created since the last Clear
     DevBuf lgrid;
@@ -723,6 +725,8 @@ struct gbvdb_grid_s {
         if (sc != 4 || log2dim[0] != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 with 16^3 bricks only"};
         if (!(R >= 0)) throw StatusError{GBVDB_INVALID_ARG, "negative radius"};
         if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
+        if (fp16 && clr.base)
+            throw StatusError{GBVDB_NOT_SUPPORTED, "InsertPointsSubcell_FP16 with point colours"};
         refresh_nused0();
         if (nused[0] == 0) return GBVDB_NOOP;  // VG.cpp:4973-4977
         stage_begin();
@@ -774,8 +778,11 @@ struct gbvdb_grid_s {
         sc_nbricks = nb;
         mark();
         grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
+        // the list entries carry the points' colours when SetPoints gave a colour buffer
+        // (InsertPointsSubcell, VG.cpp:5063-5075)
+        if (clr.base) grow(sorted_clr, (size_t)std::max<uint32_t>(binned, 1) * 4);
         launch_bin_scatter(p, trans, R, qz, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
-                           ptr<float4>(sorted), stream);
+                           ptr<float4>(sorted), clr, ptr<uint32_t>(sorted_clr), stream);
         check_launch("bin_scatter");
         mark();
         sc_valid = true;
@@ -783,6 +790,7 @@ struct gbvdb_grid_s {
         sc_R = R;
         sc_trans = trans;
         sc_pts = p;
+        sc_clr = clr;
         sc_nleaf = ncnt[0];
         sc_len = (long long)tot[0];
         sc_orphans = (long long)tot[1];
@@ -799,6 +807,7 @@ struct gbvdb_grid_s {
         grow(list_cnt, (size_t)(nsub + 1) * 4);
         grow(list_off, (size_t)(nsub + 1) * 4);
         grow(list_pts, (size_t)std::max(sc_len, 1ll) * 12);
+        if (sc_clr.base) grow(list_clr, (size_t)std::max(sc_len, 1ll) * 4);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
         TreeView t = view();
         launch_list_count(t, lgv, sc_pts, sc_trans, sc_R, sc_quant, ptr<uint32_t>(scmap), ptr<uint32_t>(list_cnt),
@@ -807,7 +816,7 @@ struct gbvdb_grid_s {
         scan_exclusive_u32(ptr<uint32_t>(list_cnt), ptr<uint32_t>(list_off), nsub, scan_tmp.p, stream);
         check(cudaMemsetAsync(list_cnt.p, 0, (size_t)(nsub + 1) * 4, stream), "list clear");
         launch_list_fill(t, lgv, sc_pts, sc_trans, sc_R, sc_quant, ptr<uint32_t>(scmap), ptr<uint32_t>(list_off),
-                         ptr<uint32_t>(list_cnt), ptr<float>(list_pts), stream);
+                         ptr<uint32_t>(list_cnt), ptr<float>(list_pts), sc_clr, ptr<uint32_t>(list_clr), stream);
         check_launch("lists");
         lists_valid = true;
     }
@@ -843,6 +852,17 @@ struct gbvdb_grid_s {
         offs_T = bits_of(T);
     }
 
+    // a float in channel c's storage type: FP32 bits, FP16 / BF16 bits, or for T_UCHAR4
+    // make_uchar4(v, v, v, v) (UpdateApronC4's boundary value, OP.cuh:140-143)
+    uint32_t storage_bits(int c, float v) const {
+        if (ch[c].dtype == GBVDB_T_UCHAR4) {
+            const uint32_t b = !(v == v) || v <= 0.0f ? 0u : (v >= 255.0f ? 255u : (uint32_t)v);
+            return b | (b << 8) | (b << 16) | (b << 24);
+        }
+        if (ch[c].esize == 4) return bits_of(v);
+        return ch[c].dtype == GBVDB_T_HALF ? f2h_bits(v) : f2bf_bits(v);
+    }
+
     static uint32_t bits_of(float f) {
         uint32_t u;
         memcpy(&u, &f, 4);
@@ -857,16 +877,18 @@ struct gbvdb_grid_s {
     }
 
     gbvdb_status gather(int mode, int sc, float rho, long long sc_len_arg, int chan, int clr_chan, bool accum) {
-        (void)clr_chan;
         if (sc != 4) throw StatusError{GBVDB_NOT_SUPPORTED, "subcell size 4 only"};
         if (chan < 0 || chan >= 8 || !ch[chan].used) throw StatusError{GBVDB_INVALID_ARG, "bad channel"};
         if (ch[chan].dtype != GBVDB_T_FLOAT && ch[chan].dtype != GBVDB_T_HALF && ch[chan].dtype != GBVDB_T_BFLOAT16)
             throw StatusError{GBVDB_NOT_SUPPORTED, "gathers write float, half or bfloat16 channels"};
-        if (clr) throw StatusError{GBVDB_NOT_SUPPORTED, "colour gathers are not implemented"};
         refresh_nused0();
         if (nused[0] == 0) return GBVDB_NOOP;                       // VG.cpp:5321-5322, 5350-5351
         if (mode == 0 && sc_len_arg == 0) return GBVDB_NOOP;        // VG.cpp:5321
         if (!sc_valid || sc_nleaf != ncnt[0]) throw StatusError{GBVDB_INVALID_ARG, "InsertPointsSubcell is stale"};
+        // colours: averaged into chanClr when the insert carried point colours (PT.cuh:728, 768)
+        const bool colour = sc_clr.base != nullptr;
+        if (colour && (clr_chan < 0 || clr_chan >= 8 || !ch[clr_chan].used || ch[clr_chan].dtype != GBVDB_T_UCHAR4))
+            throw StatusError{GBVDB_INVALID_ARG, "the points carry colours: chanClr must be a T_UCHAR4 channel"};
         stage_begin();
         GatherParams gp{};
         gp.mode = mode;
@@ -901,6 +923,12 @@ struct gbvdb_grid_s {
             materialize_lists();
             launch_gather_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off), ptr<float>(list_pts), gp,
                                 interior, stream);
+            if (colour) {
+                interior_written(clr_chan);
+                launch_gather_colour_lists(t, ptr<int>(linked), sc_nbricks, ptr<uint32_t>(list_off),
+                                           ptr<uint32_t>(list_clr), ax, ay, gp.accum, ptr<uint32_t>(ch[clr_chan].interior),
+                                           stream);
+            }
         } else {
             int tslot = -1;
             gp.dense_min = tune_pick(sc_nbricks, &tslot);
@@ -925,6 +953,14 @@ struct gbvdb_grid_s {
                 if (++tune_step == kTuneN) tune_pending = true;
             }
             if (push) pushed_ver[chan] = layout_ver;
+            if (colour) {
+                // member offsets H - S: S - H lies in [floor(-R/4), floor((5+R)/4)] on every axis
+                const int dlo = (int)std::floor(-(double)sc_R / 4.0), dhi = (int)std::floor((5.0 + sc_R) / 4.0);
+                interior_written(clr_chan);
+                launch_gather_colour(ptr<int4>(gtab), sc_nbricks, ptr<uint32_t>(bin_off), ptr<float4>(sorted),
+                                     ptr<uint32_t>(sorted_clr), -dhi, -dlo, gp.accum,
+                                     ptr<uint32_t>(ch[clr_chan].interior), stream);
+            }
         }
         check_launch("gather");
         mark();
@@ -937,10 +973,7 @@ struct gbvdb_grid_s {
         if (ch[chan].apron == 0) return GBVDB_NOOP;
         if (ncnt[0] == 0 || atlas_last == 0) return GBVDB_NOOP;
         stage_begin();
-        uint32_t bb;
-        if (ch[chan].esize == 4) bb = bits_of(boundval);
-        else if (ch[chan].dtype == GBVDB_T_HALF) bb = f2h_bits(boundval);
-        else bb = f2bf_bits(boundval);
+        const uint32_t bb = storage_bits(chan, boundval);
         TreeView t = view();
         // after a fused-apron gather of this layout only the faces of missing
         // neighbours are left to write
@@ -1075,7 +1108,7 @@ struct gbvdb_grid_s {
         if (apron != 1) return GBVDB_NOT_SUPPORTED;  // the reference's apron kernels assume 1 (VG.cpp:4448)
         if (log2dim[0] != 4) return GBVDB_NOT_SUPPORTED;
         int es;
-        if (dtype == GBVDB_T_FLOAT) es = 4;
+        if (dtype == GBVDB_T_FLOAT || dtype == GBVDB_T_UCHAR4) es = 4;
         else if (dtype == GBVDB_T_HALF || dtype == GBVDB_T_BFLOAT16) es = 2;
         else return GBVDB_NOT_SUPPORTED;
         if (cax == 0 && cay == 0 && caz == 0) {  // VG.cpp:2441-2444
@@ -1547,14 +1580,15 @@ gbvdb_status gbvdb_load_vbx(gbvdb_grid g, const char* path) {
 gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off, int stride, const void* vel,
                               int vel_off, int vel_stride, const void* clr, int clr_off, int clr_stride) {
     GBVDB_GUARD(g)
-    (void)vel_off; (void)vel_stride; (void)clr_off; (void)clr_stride;
+    (void)vel_off; (void)vel_stride;
     if ((!pos && n > 0) || n < 0 || stride < 12 || off < 0 || (off % 4) || (stride % 4)) return GBVDB_INVALID_ARG;
+    if (clr && (clr_off < 0 || clr_stride < 4 || (clr_off % 4) || (clr_stride % 4))) return GBVDB_INVALID_ARG;
     g->pts.base = reinterpret_cast<const char*>(pos);
     g->pts.n = n;
     g->pts.off = off;
     g->pts.stride = stride;
     g->vel = vel;
-    g->clr = clr;
+    g->clr = ClrSrc{reinterpret_cast<const char*>(clr), clr ? clr_stride : 4, clr ? clr_off : 0};
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -1586,14 +1620,12 @@ gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bo
     GBVDB_GUARD(g)
     (void)commit_pool;  // pools live on the device only; nothing to commit
     if (compute_bounds && g->ncnt[0] > 0) {  // ComputeBounds (VG.cpp:1792-1816)
-        int init[6] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000, (int)0x80000000};
         g->grow(g->misc, 256);
         int* d6 = g->ptr<int>(g->misc) + 16;
-        memcpy(g->pinned, init, sizeof(init));
-        g->check(cudaMemcpyAsync(d6, g->pinned, sizeof(init), cudaMemcpyHostToDevice, g->stream), "bounds init");
         launch_leaf_bounds(g->ptr<Node>(g->nodes[0]), g->ncnt[0], g->lgrange[0], d6, g->stream);
         g->check_launch("bounds");
         g->readback(g->bounds, d6, sizeof(g->bounds));
+        g->bounds_valid = true;
     }
     return GBVDB_OK;
     GBVDB_END(g)
@@ -1655,22 +1687,42 @@ gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval) {
     GBVDB_END(g)
 }
 
-gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value) {
+gbvdb_status gbvdb_fill_channel4(gbvdb_grid g, int chan, const float value[4]) {
     GBVDB_GUARD(g)
-    if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
-    if (g->atlas_last == 0) return GBVDB_NOOP;
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !value) return GBVDB_INVALID_ARG;
     Channel& C = g->ch[chan];
     g->interior_written(chan);
-    launch_fill_interior(g->ptr<AtlasNode>(g->amap), g->atlas_last, C.dtype, C.interior.p, value, g->stream);
-    uint32_t bb = C.esize == 4 ? gbvdb_grid_s::bits_of(value)
-                               : (C.dtype == GBVDB_T_HALF ? f2h_bits(value) : f2bf_bits(value));
-    long long n = (long long)g->atlas_last * kApronStride;
-    if (C.esize == 4) {
-        launch_fill_u32(g->ptr<uint32_t>(C.apron_buf), n, bb, g->stream);
+    // every slot of the atlas, interior and apron (the reference's FUNC_FILL_* pass over
+    // the whole atlas volume, VG.cpp:2456-2470, OP.cuh:353-380)
+    const long long slots = std::min<long long>(C.cap_slots, (long long)g->ax * g->ay * g->az);
+    uint32_t bb;
+    if (C.dtype == GBVDB_T_UCHAR4) {  // CLR2INT(make_float4(p1, p2, p3, 1.0)) (OP.cuh:20, 372)
+        bb = ((uint32_t)(1.0f * 255.0f) << 24) | ((uint32_t)(value[2] * 255.0f) << 16) |
+             ((uint32_t)(value[1] * 255.0f) << 8) | (uint32_t)(value[0] * 255.0f);
     } else {
-        launch_fill_u32(g->ptr<uint32_t>(C.apron_buf), n / 2, bb | (bb << 16), g->stream);
+        bb = g->storage_bits(chan, value[0]);
+        if (C.esize == 2) bb |= bb << 16;
     }
+    launch_fill_u32(g->ptr<uint32_t>(C.interior), slots * 4096 * C.esize / 4, bb, g->stream);
+    launch_fill_u32(g->ptr<uint32_t>(C.apron_buf), slots * kApronStride * C.esize / 4, bb, g->stream);
     g->check_launch("fill");
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value) {
+    const float v[4] = {value, 0.0f, 0.0f, 0.0f};
+    return gbvdb_fill_channel4(g, chan, v);
+}
+
+gbvdb_status gbvdb_clear_channel(gbvdb_grid g, int chan) {
+    GBVDB_GUARD(g)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used) return GBVDB_INVALID_ARG;
+    Channel& C = g->ch[chan];
+    g->interior_written(chan);
+    const size_t slots = (size_t)C.cap_slots;
+    g->check(cudaMemsetAsync(C.interior.p, 0, slots * 4096 * C.esize, g->stream), "clear channel");
+    g->check(cudaMemsetAsync(C.apron_buf.p, 0, slots * kApronStride * C.esize, g->stream), "clear channel");
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -1692,6 +1744,15 @@ gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used) 
             used[l] = g->nused[l];
         }
     }
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_vol_bounds(gbvdb_grid g, float* out6) {
+    GBVDB_GUARD(g)
+    if (!out6) return GBVDB_INVALID_ARG;
+    if (!g->bounds_valid) return GBVDB_NOOP;
+    for (int a = 0; a < 6; a++) out6[a] = (float)g->bounds[a];
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -1789,6 +1850,7 @@ gbvdb_status gbvdb_export_subcells(gbvdb_grid g, int64_t* offsets, int64_t cap_o
 gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
     GBVDB_GUARD(g)
     if (chan < 0 || chan >= 8 || !g->ch[chan].used || !out) return GBVDB_INVALID_ARG;
+    if (g->ch[chan].dtype == GBVDB_T_UCHAR4) return GBVDB_NOT_SUPPORTED;  // sums of float channels only
     g->grow(g->misc, 256);
     g->grow(g->xfer, (size_t)std::max(g->atlas_last, 1) * 8);
     double* d = reinterpret_cast<double*>(g->ptr<char>(g->misc) + 192);
@@ -1805,6 +1867,7 @@ gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out) {
 gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out) {
     GBVDB_GUARD(g)
     if (chan < 0 || chan >= 8 || !g->ch[chan].used || !dev_out) return GBVDB_INVALID_ARG;
+    if (g->ch[chan].dtype == GBVDB_T_UCHAR4) return GBVDB_NOT_SUPPORTED;  // sums of float channels only
     g->grow(g->csum_part, (size_t)std::max(g->atlas_last, 1) * 8);
     launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
                           g->ptr<double>(g->csum_part), dev_out, g->stream);
@@ -1819,6 +1882,7 @@ gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out) {
 gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out) {
     GBVDB_GUARD(g)
     if (chan < 0 || chan >= 8 || !g->ch[chan].used || !dev_out) return GBVDB_INVALID_ARG;
+    if (g->ch[chan].dtype == GBVDB_T_UCHAR4) return GBVDB_NOT_SUPPORTED;  // sums of float channels only
     if (g->atlas_last > noalloc_max_slots()) {
         g->err = "checksum_noalloc: " + std::to_string(g->atlas_last) + " atlas slots exceed the static scratch limit of " +
                  std::to_string(noalloc_max_slots()) + " slots";
@@ -1830,6 +1894,50 @@ gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out) {
         g->err = std::string("checksum_noalloc: ") + cudaGetErrorString(e);
         return GBVDB_CUDA_ERROR;
     }
+    g->check_launch("checksum_noalloc");
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_get_vdb_info(gbvdb_grid g, void* host_out, int64_t bytes) {
+    GBVDB_GUARD(g)
+    if (!host_out || bytes < (int64_t)sizeof(gbvdb_vdb_info)) return GBVDB_INVALID_ARG;
+    g->refresh_nused0();
+    // a consumer may write the interiors through these pointers at any time, so every
+    // later UpdateApron copies the interiors as they are (as with gbvdb_get_atlas_device)
+    g->fused_apron = false;
+    gbvdb_vdb_info v;
+    memset(&v, 0, sizeof(v));
+    for (int n = 0; n < g->levs && n < 10; n++) {  // PrepareVDB (VG.cpp:3946-3989)
+        v.dim[n] = g->log2dim[n];
+        v.res[n] = g->res[n];
+        const float rg = (float)g->range[n];
+        v.vdel[n] = make_float3(rg / (float)g->res[n], rg / (float)g->res[n], rg / (float)g->res[n]);
+        v.noderange[n] = make_int3((int)g->range[n], (int)g->range[n], (int)g->range[n]);
+        v.nodecnt[n] = (int)g->ncnt[n];
+        v.nodewid[n] = (int)sizeof(Node);
+        v.childwid[n] = (int)(g->cl_len(n) * 8);
+        v.nodelist[n] = g->ptr<char>(g->nodes[n]);
+        v.childlist[n] = g->ptr<char>(g->clist[n]);
+    }
+    v.atlas_map = g->ptr<gbvdb_atlas_node>(g->amap);
+    v.atlas_cnt = make_int3(g->ax, g->ay, g->az);
+    v.atlas_res = make_int3(g->ax * kPad, g->ay * kPad, g->az * kPad);
+    v.atlas_apron = 1;
+    v.brick_res = kPad;
+    for (int c = 0; c < 8; c++) {
+        if (!g->ch[c].used) continue;
+        v.apron_table[c] = g->ch[c].esize;
+        v.volIn[c] = (unsigned long long)(uintptr_t)g->ch[c].interior.p;
+        v.volOut[c] = (unsigned long long)(uintptr_t)g->ch[c].apron_buf.p;
+    }
+    v.top_lev = g->top_lev();
+    v.clr_chan = 255;  // CHAN_UNDEF
+    if (g->bounds_valid) {
+        v.bmin = make_float3((float)g->bounds[0], (float)g->bounds[1], (float)g->bounds[2]);
+        v.bmax = make_float3((float)g->bounds[3], (float)g->bounds[4], (float)g->bounds[5]);
+    }
+    memcpy(host_out, &v, sizeof(v));
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -1893,12 +2001,20 @@ gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4) {
 }
 
 // device bytes held by the grid's buffers (pools, atlas, scratch): the server's memory accounting
+size_t gbvdb_internal_device_bytes(gbvdb_grid g);
+gbvdb_status gbvdb_get_device_bytes(gbvdb_grid g, int64_t* out) {
+    if (!g || !out) return GBVDB_INVALID_ARG;
+    *out = (int64_t)gbvdb_internal_device_bytes(g);
+    return GBVDB_OK;
+}
+
 size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     if (!g) return 0;
     std::lock_guard<std::mutex> lk(g->mu);
     size_t b = 0;
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                            &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid,
+                            &g->sorted, &g->sorted_clr, &g->list_cnt, &g->list_off, &g->list_pts, &g->list_clr,
+                            &g->offs_buf, &g->lgrid,
                             &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,

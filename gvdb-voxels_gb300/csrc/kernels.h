@@ -26,6 +26,13 @@ struct PointSrc {
     int stride;
     int off;
 };
+// point colours (SetPoints' colour DataPtr): the uint32 RGBA8 at base + i*stride + off;
+// base == nullptr: none
+struct ClrSrc {
+    const char* base;
+    int stride;
+    int off;
+};
 
 // ---- scan.cu
 size_t scan_tmp_bytes(long long n);
@@ -108,8 +115,9 @@ void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                       const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
                       unsigned long long* totals, cudaStream_t s);
+// sorted_clr (or null): the binned points' colours from clr, in the order of `sorted`
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
-                        const uint32_t* bin_off, float4* sorted, cudaStream_t s);
+                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, cudaStream_t s);
 
 struct GatherParams {
     int mode;          // 0 density, 1 level set
@@ -138,9 +146,18 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
 // materialized subcell lists (export and the fallback gather)
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                        uint32_t* cnt, cudaStream_t s);
+// out_clr (or null): the list entries' colours from clr
 void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
-                      const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s);
+                      const uint32_t* off, uint32_t* cursor, float* out3, ClrSrc clr, uint32_t* out_clr, cudaStream_t s);
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s);
+// Colour averages of the gathers (T_UCHAR4 channel, 4096 uint32 per slot): every voxel of
+// a subcell gets the mean of the subcell's member colours (plus its old colour with accum,
+// else (0, 0, 0, 1)).  Binned form: gtab from the value gather of the same insert;
+// member offsets H - S per axis in [olo, ohi].  List form: materialized lists + colours.
+void launch_gather_colour(const int4* gtab, long long nbricks, const uint32_t* bin_off, const float4* pts,
+                          const uint32_t* pclr, int olo, int ohi, int accum, uint32_t* out, cudaStream_t s);
+void launch_gather_colour_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
+                                const uint32_t* clr, int ax, int ay, int accum, uint32_t* out, cudaStream_t s);
 
 }  // namespace gbvdb

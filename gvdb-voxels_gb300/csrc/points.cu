@@ -264,7 +264,7 @@ __device__ __forceinline__ int member_bits(int ox, int oy, int oz) {
 
 __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const int* __restrict__ bin_of,
                               const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
-                              float4* __restrict__ sorted) {
+                              float4* __restrict__ sorted, ClrSrc clr, uint32_t* __restrict__ sorted_clr) {
     // kU points per thread per step, their loads issued together (the pass is bound by the
     // latency of the dependent bin_of -> bin_off loads)
     constexpr int kU = 4;
@@ -294,6 +294,10 @@ __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const
             float ps[3];
             stored_pos(qz, w, ps);
             sorted[off[u] + rk[u]] = make_float4(ps[0], ps[1], ps[2], __int_as_float(pack_ranges(w, ps, R)));
+            if (sorted_clr) {
+                const long long i = i0 + u * stride;
+                sorted_clr[off[u] + rk[u]] = __ldg(reinterpret_cast<const uint32_t*>(clr.base + i * (long long)clr.stride + clr.off));
+            }
         }
     }
 }
@@ -992,7 +996,8 @@ __global__ void __launch_bounds__(kGatherThreads, 10) k_gather(const int4* __res
 
 template <bool kFill>
 __device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant qz,
-                            const uint32_t* scmap, uint32_t* cnt, const uint32_t* off, float* out3) {
+                            const uint32_t* scmap, uint32_t* cnt, const uint32_t* off, float* out3, ClrSrc clr = {},
+                            uint32_t* out_clr = nullptr) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
         float w[3];
         if (!load_valid(p, i, trans, w[0], w[1], w[2])) continue;
@@ -1016,6 +1021,9 @@ __device__ void list_points(const TreeView& t, const LeafGrid& lg, PointSrc p, f
                         o[0] = ps[0];
                         o[1] = ps[1];
                         o[2] = ps[2];
+                        if (out_clr)
+                            out_clr[off[idx] + k] =
+                                __ldg(reinterpret_cast<const uint32_t*>(clr.base + i * (long long)clr.stride + clr.off));
                     }
                 }
     }
@@ -1025,8 +1033,8 @@ __global__ void k_list_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, 
     list_points<false>(t, lg, p, trans, R, qz, scmap, cnt, nullptr, nullptr);
 }
 __global__ void k_list_fill(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz, const uint32_t* scmap,
-                            const uint32_t* off, uint32_t* cursor, float* out3) {
-    list_points<true>(t, lg, p, trans, R, qz, scmap, cursor, off, out3);
+                            const uint32_t* off, uint32_t* cursor, float* out3, ClrSrc clr, uint32_t* out_clr) {
+    list_points<true>(t, lg, p, trans, R, qz, scmap, cursor, off, out3, clr, out_clr);
 }
 
 // reference-shaped gather over materialized lists: one block per linked leaf,
@@ -1054,6 +1062,134 @@ __global__ void k_gather_lists(TreeView t, const int* __restrict__ linked, const
     }
     __syncthreads();
     write_tile<T>(gp, tile, interior + (size_t)slot * 4096, false);
+}
+
+// ---- colour averages (GatherDensity / GatherLevelSet with a colour channel) ----
+//
+// The reference (PT.cuh:717-731, 757-771) gives every voxel of a subcell
+//   CLR2CHAR((accum ? CHAR2CLR(old) : (0,0,0,1)) + sum_j CHAR2CLR(c_j)) / (n + accum))
+// over the n entries of the subcell's list, adding the FP32 terms c/255 in the
+// arbitrary order of its atomically filled list.  Here the sum is exact: the bytes
+// are added as integers (with the old colour's bytes, or 255 for the alpha of the
+// non-accumulating start), divided by 255 once, then the reference's remaining
+// FP32 steps follow.  CLR2CHAR's uchar(x) conversion truncates and saturates
+// (NaN -> 0), as the GPU's float-to-integer conversion does.
+
+__device__ __forceinline__ uint32_t clr_byte(float x) {
+    if (!(x == x) || x <= 0.0f) return 0u;
+    if (x >= 255.0f) return 255u;
+    return (uint32_t)x;
+}
+__device__ __forceinline__ uint32_t clr_average(const uint32_t sum[4], uint32_t n, uint32_t old, int accum) {
+    uint32_t out = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t t = sum[k] + (accum ? ((old >> (8 * k)) & 0xFFu) : (k == 3 ? 255u : 0u));
+        float c = __fdiv_rn(__uint2float_rn(t), 255.0f);
+        c = __fdiv_rn(c, __uint2float_rn(n + (accum ? 1u : 0u)));
+        out |= clr_byte(__fmul_rn(c, 255.0f)) << (8 * k);
+    }
+    return out;
+}
+
+// One block of 128 threads per linked brick; warp w takes subcells w, w+4, ...  For
+// its subcell S the warp visits the home bins H = S + o, o in [olo, ohi]^3 (every
+// offset at which a member can be homed), a lane per offset to resolve the bin
+// ranges, then the lanes stride over each bin's points and keep those whose
+// membership masks include S.  Integer sums, so the result is deterministic.
+__global__ void __launch_bounds__(128) k_gather_colour(const int4* __restrict__ gtab, const uint32_t* __restrict__ bin_off,
+                                                       const float4* __restrict__ pts, const uint32_t* __restrict__ pclr,
+                                                       int olo, int ohi, int accum, uint32_t* __restrict__ out) {
+    __shared__ int nrank[27];
+    const int4* rec = gtab + (size_t)blockIdx.x * 32;
+    const int4 head = __ldg(rec + 27);
+    const int slot = head.w;
+    if (slot < 0) return;
+    if (threadIdx.x < 27) nrank[threadIdx.x] = __ldg(rec + threadIdx.x).x;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sx0 = head.x >> 2, sy0 = head.y >> 2, sz0 = head.z >> 2;
+    const int span = ohi - olo + 1, noff = span * span * span;
+    uint32_t* dst = out + (size_t)slot * 4096;
+    for (int sc = warp; sc < 64; sc += 4) {
+        const int lx = sc & 3, ly = (sc >> 2) & 3, lz = sc >> 4;
+        const int Sx = sx0 + lx, Sy = sy0 + ly, Sz = sz0 + lz;
+        uint32_t sum[4] = {0u, 0u, 0u, 0u}, n = 0;
+        for (int g0 = 0; g0 < noff; g0 += 32) {
+            const int e = g0 + lane;
+            uint32_t beg = 0, cnt = 0;
+            int need = 0;
+            if (e < noff) {
+                const int ox = olo + e % span, oy = olo + (e / span) % span, oz = olo + e / (span * span);
+                const int hx = Sx + ox, hy = Sy + oy, hz = Sz + oz;
+                if (hx >= 0 && hy >= 0 && hz >= 0) {
+                    const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
+                    const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
+                    if (r >= 0) {
+                        const unsigned bin = (unsigned)r * 64u + (unsigned)(((hz & 3) << 4) | ((hy & 3) << 2) | (hx & 3));
+                        beg = __ldg(bin_off + bin);
+                        cnt = __ldg(bin_off + bin + 1) - beg;
+                        need = member_bits(ox, oy, oz);
+                    }
+                }
+            }
+            unsigned nonempty = __ballot_sync(0xFFFFFFFFu, cnt > 0);
+            while (nonempty) {
+                const int l = __ffs(nonempty) - 1;
+                nonempty &= nonempty - 1;
+                const uint32_t b = __shfl_sync(0xFFFFFFFFu, beg, l);
+                const uint32_t c = __shfl_sync(0xFFFFFFFFu, cnt, l);
+                const int nd = __shfl_sync(0xFFFFFFFFu, need, l);
+                for (uint32_t j = lane; j < c; j += 32) {
+                    const int m = __float_as_int(__ldg(&pts[b + j].w));
+                    if ((m & nd) == nd) {
+                        const uint32_t v = __ldg(pclr + b + j);
+                        sum[0] += v & 0xFFu;
+                        sum[1] += (v >> 8) & 0xFFu;
+                        sum[2] += (v >> 16) & 0xFFu;
+                        sum[3] += v >> 24;
+                        n++;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) sum[k] = __reduce_add_sync(0xFFFFFFFFu, sum[k]);
+        n = __reduce_add_sync(0xFFFFFFFFu, n);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int v = lane + 32 * h;
+            const int x = 4 * lx + (v & 3), y = 4 * ly + ((v >> 2) & 3), z = 4 * lz + (v >> 4);
+            uint32_t* o = dst + (z << 8) + (y << 4) + x;
+            *o = clr_average(sum, n, accum ? *o : 0u, accum);
+        }
+    }
+}
+
+// over materialized lists (the fallback form): one block per linked leaf, a thread
+// per voxel, each summing its subcell's list
+__global__ void k_gather_colour_lists(TreeView t, const int* __restrict__ linked, const uint32_t* __restrict__ off,
+                                      const uint32_t* __restrict__ clr, int ax, int ay, int accum,
+                                      uint32_t* __restrict__ out) {
+    const int leaf = linked[blockIdx.x];
+    const Node nd = t.nodes[0][leaf];
+    const int slot = slot_of_value(nd.value, ax, ay);
+    if (slot < 0) return;
+    uint32_t* dst = out + (size_t)slot * 4096;
+    for (int v = threadIdx.x; v < 4096; v += blockDim.x) {
+        const int x = v & 15, y = (v >> 4) & 15, z = v >> 8;
+        const int s = ((z >> 2) << 4) | ((y >> 2) << 2) | (x >> 2);
+        const unsigned idx = blockIdx.x * 64u + (unsigned)s;
+        uint32_t sum[4] = {0u, 0u, 0u, 0u};
+        for (uint32_t j = off[idx]; j < off[idx + 1]; j++) {
+            const uint32_t c = __ldg(clr + j);
+            sum[0] += c & 0xFFu;
+            sum[1] += (c >> 8) & 0xFFu;
+            sum[2] += (c >> 16) & 0xFFu;
+            sum[3] += c >> 24;
+        }
+        dst[v] = clr_average(sum, off[idx + 1] - off[idx], accum ? dst[v] : 0u, accum);
+    }
 }
 
 // ---- legacy InsertPoints + ScatterDensity (brick binning and a splat) ----
@@ -1192,9 +1328,20 @@ void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 
                                                     totals);
 }
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
-                        const uint32_t* bin_off, float4* sorted, cudaStream_t s) {
+                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted);
+    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr,
+                                                     clr.base ? sorted_clr : nullptr);
+}
+void launch_gather_colour(const int4* gtab, long long nbricks, const uint32_t* bin_off, const float4* pts,
+                          const uint32_t* pclr, int olo, int ohi, int accum, uint32_t* out, cudaStream_t s) {
+    if (nbricks <= 0) return;
+    k_gather_colour<<<(unsigned)nbricks, 128, 0, s>>>(gtab, bin_off, pts, pclr, olo, ohi, accum, out);
+}
+void launch_gather_colour_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
+                                const uint32_t* clr, int ax, int ay, int accum, uint32_t* out, cudaStream_t s) {
+    if (nbricks <= 0) return;
+    k_gather_colour_lists<<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, clr, ax, ay, accum, out);
 }
 void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,
                        int ax, int ay, long long n, int* bad, cudaStream_t s) {
@@ -1222,9 +1369,11 @@ void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3
     k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, cnt);
 }
 void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
-                      const uint32_t* scmap, const uint32_t* off, uint32_t* cursor, float* out3, cudaStream_t s) {
+                      const uint32_t* scmap, const uint32_t* off, uint32_t* cursor, float* out3, ClrSrc clr,
+                      uint32_t* out_clr, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, off, cursor, out3);
+    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, off, cursor, out3, clr,
+                                                   clr.base ? out_clr : nullptr);
 }
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s) {

@@ -471,13 +471,32 @@ __global__ void k_count_flags(const Node* nodes, long long n, unsigned long long
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
 }
 
-// ComputeBounds (VG.cpp:1792-1816): min corner / max corner of flagged leaves
-__global__ void k_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !leaves[i].flags) return;
-    for (int a = 0; a < 3; a++) {
-        atomicMin(out6 + a, leaves[i].pos[a]);
-        atomicMax(out6 + 3 + a, leaves[i].pos[a] + (1 << lgrange0));
+// ComputeBounds (VG.cpp:1792-1816): both corners start at the position of leaf 0 of
+// the pool (flagged or not); every flagged leaf widens them by [pos, pos + range0).
+// One block; out6 = {min xyz, max xyz}, written whole (no initialisation needed).
+__global__ void __launch_bounds__(1024) k_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6) {
+    __shared__ int red[6][32];
+    int v[6];
+    for (int a = 0; a < 3; a++) v[a] = v[3 + a] = leaves[0].pos[a];
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const Node& nd = leaves[i];
+        if (!nd.flags) continue;
+        for (int a = 0; a < 3; a++) {
+            v[a] = min(v[a], nd.pos[a]);
+            v[3 + a] = max(v[3 + a], nd.pos[a] + (1 << lgrange0));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 6; k++) {
+        const int r = k < 3 ? __reduce_min_sync(0xFFFFFFFFu, v[k]) : __reduce_max_sync(0xFFFFFFFFu, v[k]);
+        if (lane == 0) red[k][warp] = r;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x, nw = (blockDim.x + 31) >> 5;
+        int r = red[k][0];
+        for (int w = 1; w < nw; w++) r = k < 3 ? min(r, red[k][w]) : max(r, red[k][w]);
+        out6[k] = r;
     }
 }
 
@@ -565,7 +584,7 @@ void launch_count_flags(const Node* nodes, long long n, unsigned long long* out,
 }
 void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s) {
     if (n <= 0) return;
-    k_leaf_bounds<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, lgrange0, out6);
+    k_leaf_bounds<<<1, 1024, 0, s>>>(leaves, n, lgrange0, out6);
 }
 
 }  // namespace gbvdb

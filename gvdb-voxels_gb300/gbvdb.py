@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(PKG, "libgbvdb.so")
 OK, INVALID_ARG, OUT_OF_MEMORY, CUDA_ERROR, DEPTH_UNSUPPORTED, CAPACITY, TIMEOUT, NOT_SUPPORTED, NOOP = range(9)
 STATUS_NAMES = ["OK", "INVALID_ARG", "OUT_OF_MEMORY", "CUDA_ERROR", "DEPTH_UNSUPPORTED", "CAPACITY", "TIMEOUT",
                 "NOT_SUPPORTED", "NOOP"]
-T_UCHAR, T_FLOAT, T_HALF, T_BFLOAT16 = 0, 3, 100, 101
+T_UCHAR, T_UCHAR4, T_FLOAT, T_HALF, T_BFLOAT16 = 0, 2, 3, 100, 101
 
 NODE_DTYPE = np.dtype([
     ("lev", "u1"), ("flags", "u1"), ("prio", "u1"), ("pad", "u1"),
@@ -25,6 +25,7 @@ NODE_DTYPE = np.dtype([
     ("parent", "<u8"), ("childlist", "<u8"), ("mask", "<u8"),
 ])
 AMAP_DTYPE = np.dtype([("pos", "<i4", 3), ("leaf", "<i4")])
+VDB_INFO_BYTES = 1232  # sizeof(gbvdb_vdb_info), the reference's VDBInfo layout
 
 # every symbol declared in include/gbvdb.h
 EXPORTS = [
@@ -39,7 +40,8 @@ EXPORTS = [
     "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
-    "gbvdb_export_point_leaves", "gbvdb_checksum_device",
+    "gbvdb_export_point_leaves", "gbvdb_checksum_device", "gbvdb_fill_channel4", "gbvdb_clear_channel",
+    "gbvdb_get_vol_bounds", "gbvdb_get_device_bytes", "gbvdb_get_vdb_info",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -106,6 +108,11 @@ def load(path=LIB_PATH):
     L.gbvdb_gather_levelset.argtypes = [vp, i32, i64, f32, fp, i64, i32, i32, i32]
     L.gbvdb_update_apron.argtypes = [vp, i32, f32]
     L.gbvdb_fill_channel.argtypes = [vp, i32, f32]
+    L.gbvdb_fill_channel4.argtypes = [vp, i32, fp]
+    L.gbvdb_clear_channel.argtypes = [vp, i32]
+    L.gbvdb_get_vol_bounds.argtypes = [vp, fp]
+    L.gbvdb_get_device_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_get_vdb_info.argtypes = [vp, vp, i64]
     L.gbvdb_get_depth.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gbvdb_get_node_counts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_get_point_bounds.argtypes = [vp, fp]
@@ -226,11 +233,17 @@ class Grid:
     def add_channel(self, chan=0, dtype=T_FLOAT, apron=1, axiscnt=(0, 0, 0)):
         self._check(self.L.gbvdb_add_channel(self._h, chan, dtype, apron, *axiscnt), "add_channel")
 
-    def set_points(self, points, n=None):
+    def set_points(self, points, n=None, colours=None):
+        """colours: None or a CUDA uint32/int32 tensor, one RGBA8 value per point (R in the low byte)"""
         ptr, cnt, stride = _dev_ptr(points)
-        self._points = points  # keep the buffer alive
+        cptr, cstride = None, 0
+        if colours is not None:
+            if not colours.is_cuda or colours.dtype.itemsize != 4 or colours.dim() != 1 or colours.shape[0] < cnt:
+                raise ValueError("colours must be a CUDA tensor of one 4-byte value per point")
+            cptr, cstride = ctypes.c_void_p(colours.data_ptr()), colours.stride(0) * 4
+        self._points = (points, colours)  # keep the buffers alive
         self._check(self.L.gbvdb_set_points(self._h, ctypes.c_void_p(ptr), cnt if n is None else n, 0, stride,
-                                            None, 0, 0, None, 0, 0), "set_points")
+                                            None, 0, 0, cptr, 0, cstride), "set_points")
         return cnt
 
     # -- topology ------------------------------------------------------------
@@ -281,7 +294,33 @@ class Grid:
         return self._check(self.L.gbvdb_update_apron(self._h, chan, boundval), "update_apron")
 
     def fill_channel(self, chan, value):
+        """FillChannel: a float, or a 4-vector (x, y, z, w) as the reference's Vector4DF"""
+        if hasattr(value, "__len__"):
+            v = (ctypes.c_float * 4)(*[float(x) for x in value])
+            return self._check(self.L.gbvdb_fill_channel4(self._h, chan, v), "fill_channel")
         return self._check(self.L.gbvdb_fill_channel(self._h, chan, value), "fill_channel")
+
+    def clear_channel(self, chan):
+        """ClearChannel: every voxel of the channel to 0"""
+        return self._check(self.L.gbvdb_clear_channel(self._h, chan), "clear_channel")
+
+    def vol_bounds(self):
+        """getVolMin / getVolMax after FinishTopology(.., bounds): (min xyz, max xyz), or None"""
+        out = (ctypes.c_float * 6)()
+        if self._check(self.L.gbvdb_get_vol_bounds(self._h, out), "get_vol_bounds") == NOOP:
+            return None
+        return np.array(out[:], dtype=np.float32)
+
+    def vdb_info(self):
+        """the VDBInfo-layout view (include/gbvdb_device.cuh) as raw bytes"""
+        buf = ctypes.create_string_buffer(VDB_INFO_BYTES)
+        self._check(self.L.gbvdb_get_vdb_info(self._h, buf, VDB_INFO_BYTES), "get_vdb_info")
+        return buf.raw
+
+    def device_bytes(self):
+        out = ctypes.c_int64()
+        self._check(self.L.gbvdb_get_device_bytes(self._h, ctypes.byref(out)), "get_device_bytes")
+        return int(out.value)
 
     # -- state / export ------------------------------------------------------
     def depth(self):
@@ -326,10 +365,11 @@ class Grid:
 
     def atlas_bricks(self, chan=0):
         """Padded bricks of the assigned slots, shape (used, 18, 18, 18) [slot, z, y, x].
-        float32 channels return float32; half returns float16; bfloat16 returns raw uint16."""
+        float32 channels return float32; half returns float16; bfloat16 returns raw uint16; RGBA8
+        colour channels return uint32 (R in the low byte)."""
         info = self.atlas_info(chan)
         used = info["used"]
-        dt = {T_FLOAT: np.float32, T_HALF: np.float16, T_BFLOAT16: np.uint16}[info["dtype"]]
+        dt = {T_FLOAT: np.float32, T_HALF: np.float16, T_BFLOAT16: np.uint16, T_UCHAR4: np.uint32}[info["dtype"]]
         out = np.zeros(used * 5832, dtype=dt)
         if used:
             self._check(self.L.gbvdb_export_atlas_bricks(self._h, chan, out.ctypes.data, out.nbytes),

@@ -54,6 +54,7 @@ typedef enum {
 
 /* channel element types: the reference's T_* codes (gvdb_types.h) plus two storage extensions */
 #define GBVDB_T_UCHAR 0
+#define GBVDB_T_UCHAR4 2    /* RGBA8 colour channel (gathered colour averages) */
 #define GBVDB_T_FLOAT 3
 #define GBVDB_T_HALF 100    /* extension: FP16 storage, FP32 accumulation */
 #define GBVDB_T_BFLOAT16 101 /* extension: BF16 storage, FP32 accumulation */
@@ -79,7 +80,10 @@ GBVDB_API gbvdb_status gbvdb_set_channel_default(gbvdb_grid g, int ax, int ay, i
 GBVDB_API gbvdb_status gbvdb_add_channel(gbvdb_grid g, int chan, int dtype, int apron,
                                          int ax, int ay, int az);
 /* SetPoints / SetDataGPU (gvdb_volume_gvdb.cpp:4900-4908, 4872-4880): position i is the
- * float3 at pos + i*stride + off.  vel and clr may be NULL. */
+ * float3 at pos + i*stride + off.  vel and clr may be NULL; clr (device memory) holds one
+ * RGBA8 colour per point as the uint32 at clr + i*clr_stride + clr_off (R in the low byte,
+ * cuda_gvdb_particles.cuh:236): InsertPointsSubcell then carries colours into its lists
+ * and the gathers average them into their chanClr channel. */
 GBVDB_API gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* dev_pos, int64_t n, int off, int stride,
                                         const void* dev_vel, int vel_off, int vel_stride,
                                         const void* dev_clr, int clr_off, int clr_stride);
@@ -102,11 +106,18 @@ GBVDB_API gbvdb_status gbvdb_update_atlas(gbvdb_grid g);
  * *out_len receives the total subcell list length pSCPntsLength. */
 GBVDB_API gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int subcell_size, int64_t n, float radius,
                                                    const float trans[3], int64_t* out_len);
-/* GatherDensity (gvdb_volume_gvdb.cpp:5318-5344): v = max(accum ? old : 0, max_j(radius - |p_j - v|)) */
+/* GatherDensity (gvdb_volume_gvdb.cpp:5318-5344): v = max(accum ? old : 0, max_j(radius - |p_j - v|)).
+ * When the last insert carried point colours, clr_chan must be a GBVDB_T_UCHAR4 channel: every
+ * voxel of a subcell gets the mean of the subcell's member colours, started from its old
+ * colour with accum (else from (0, 0, 0, 255)) and divided by (members + accum)
+ * (cuda_gvdb_particles.cuh:717-731).  The member bytes are summed exactly as integers and
+ * divided by 255 once (the reference adds FP32 terms c/255 in the arbitrary order of its
+ * lists), so a byte may differ from the reference's by one. */
 GBVDB_API gbvdb_status gbvdb_gather_density(gbvdb_grid g, int subcell_size, int64_t n, float radius,
                                             const float trans[3], int64_t sc_len, int chan, int clr_chan,
                                             int accum);
-/* GatherLevelSet (gvdb_volume_gvdb.cpp:5348-5373): v = min(accum ? old : 3, min_j(|p_j - v| - radius)) */
+/* GatherLevelSet (gvdb_volume_gvdb.cpp:5348-5373): v = min(accum ? old : 3, min_j(|p_j - v| - radius));
+ * colours as GatherDensity (cuda_gvdb_particles.cuh:757-771) */
 GBVDB_API gbvdb_status gbvdb_gather_levelset(gbvdb_grid g, int subcell_size, int64_t n, float radius,
                                              const float trans[3], int64_t sc_len, int chan, int clr_chan,
                                              int accum);
@@ -137,8 +148,14 @@ GBVDB_API gbvdb_status gbvdb_export_point_leaves(gbvdb_grid g, int32_t* pnode, i
                                                  int64_t cap_offsets, float* points, int64_t cap_points);
 /* UpdateApron(chan, boundval) (gvdb_volume_gvdb.cpp:4418-4457, cuda_gvdb_operators.cuh:72-131) */
 GBVDB_API gbvdb_status gbvdb_update_apron(gbvdb_grid g, int chan, float boundval);
-/* ClearChannel / FillChannel (gvdb_volume_gvdb.cpp:2456-2485) for the assigned slots */
+/* FillChannel(chan, Vector4DF) (gvdb_volume_gvdb.cpp:2456-2470): every voxel of every slot of
+ * the atlas, interior and apron; float channels take value[0], T_UCHAR4 channels
+ * CLR2INT(value[0], value[1], value[2], 1) (cuda_gvdb_operators.cuh:20, 368-373) */
+GBVDB_API gbvdb_status gbvdb_fill_channel4(gbvdb_grid g, int chan, const float value[4]);
+/* FillChannel with (value, 0, 0, 0) */
 GBVDB_API gbvdb_status gbvdb_fill_channel(gbvdb_grid g, int chan, float value);
+/* ClearChannel (gvdb_volume_gvdb.cpp:1596-1603): every voxel of the channel's atlas to 0 */
+GBVDB_API gbvdb_status gbvdb_clear_channel(gbvdb_grid g, int chan);
 
 /* --- state and export (for parity checks, VBX and consumers) -------------- */
 /* depth of the last build, traversal top level (VG.cpp:3957-3968) */
@@ -147,6 +164,11 @@ GBVDB_API gbvdb_status gbvdb_get_depth(gbvdb_grid g, int* depth, int* top_lev);
 GBVDB_API gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used);
 /* getBoundMin/Max (gvdb_volume_gvdb.h:563-564): 6 floats */
 GBVDB_API gbvdb_status gbvdb_get_point_bounds(gbvdb_grid g, float* out6);
+/* getVolMin/getVolMax (gvdb_volume_base.h:57-59): the bounds ComputeBounds set at the last
+ * FinishTopology(.., compute_bounds = 1) (gvdb_volume_gvdb.cpp:1792-1816): both corners start
+ * at leaf 0 of the pool, each flagged leaf widens them by [pos, pos + brick range).
+ * 6 floats {min xyz, max xyz}; GBVDB_NOOP before any such call. */
+GBVDB_API gbvdb_status gbvdb_get_vol_bounds(gbvdb_grid g, float* out6);
 /* node pool of one level as 64-byte records (host buffer, `cap` records) */
 GBVDB_API gbvdb_status gbvdb_export_nodes(gbvdb_grid g, int lev, void* host_out, int64_t cap);
 /* child-list pool of one level (res^3 u64 per node) */
@@ -202,8 +224,19 @@ GBVDB_API gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev
  * more assigned atlas slots are rejected with GBVDB_CAPACITY.  The first call on
  * a device looks up that array's device address (cudaGetSymbolAddress); make
  * that first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (different streams or grids without ordering) race. */
+ * that overlap on the GPU (different streams or grids without ordering) race.
+ * The looked-up address is kept for the life of the process: resetting a device
+ * (cudaDeviceReset) while the library is loaded is not supported. */
 GBVDB_API gbvdb_status gbvdb_checksum_noalloc(gbvdb_grid g, int chan, double* dev_out);
+/* The grid as the reference's VDBInfo (cuda_gvdb_nodes.cuh:42-67, uploaded by PrepareVDB,
+ * gvdb_volume_gvdb.cpp:3946-3989) for user kernels: struct gbvdb_vdb_info of
+ * include/gbvdb_device.cuh (same layout; per channel the interior and apron-record base
+ * addresses in place of the texture / surface objects, read and written with
+ * gbvdb_atlas_read / gbvdb_atlas_write at the reference's atlas coordinates).  Written to
+ * host memory (bytes >= sizeof(gbvdb_vdb_info)); valid until the next call that changes
+ * the topology or the atlas.  From this call on every UpdateApron copies all apron voxels,
+ * as after gbvdb_get_atlas_device. */
+GBVDB_API gbvdb_status gbvdb_get_vdb_info(gbvdb_grid g, void* host_out, int64_t bytes);
 /* device pointers of the atlas storage (interior bricks, apron records) for consumers.
  * A caller holding these pointers may write the interior at any time, so from this
  * call on every UpdateApron of the grid copies the interiors as they are (the
@@ -230,6 +263,8 @@ GBVDB_API gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap);
 /* out4 = {kernel launches issued so far, host readbacks so far, last subcell-list length,
  * linked leaves of the last insert} */
 GBVDB_API gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4);
+/* device bytes held by the grid (pools, atlas, scratch; no counterpart in the reference) */
+GBVDB_API gbvdb_status gbvdb_get_device_bytes(gbvdb_grid g, int64_t* out);
 
 /* --- served form (no counterpart in the reference) -------------------------
  * A request loop over voxelize-and-gather jobs: worker threads, each with its

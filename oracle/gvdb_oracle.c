@@ -97,6 +97,7 @@ typedef struct OGrid {
     int64_t* sc_cnt;
     int64_t* sc_off;
     float* sc_pts;            /* 3 floats per entry, in subcell order */
+    uint32_t* sc_clr;         /* RGBA8 per entry when the insert carried colours, else NULL */
     int64_t sc_len;
     size_t sc_nleaf;          /* leaf count when the lists were built */
     int nthreads;
@@ -433,7 +434,7 @@ void og_destroy(OGrid* g) {
     if (!g) return;
     for (int l = 0; l < OG_MAXLEV; l++) { free(g->nodes[l]); free(g->clist[l]); }
     for (int c = 0; c < OG_MAXCHAN; c++) free(g->chan[c].data);
-    free(g->amap); free(g->sc_map); free(g->sc_cnt); free(g->sc_off); free(g->sc_pts);
+    free(g->amap); free(g->sc_map); free(g->sc_cnt); free(g->sc_off); free(g->sc_pts); free(g->sc_clr);
     free(g);
 }
 
@@ -722,19 +723,29 @@ static inline float quant16(float w, float mn, float rg) {
 }
 
 static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off, float R,
-                          const float trans[3], int64_t* out_len, int fp16);
+                          const float trans[3], int64_t* out_len, int fp16, const char* clr, int clr_stride,
+                          int clr_off);
 
 int og_insert_points_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off,
                              float R, const float trans[3], int64_t* out_len) {
-    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 0);
+    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 0, NULL, 0, 0);
+}
+/* InsertPointsSubcell with a point colour buffer (SetPoints' third DataPtr): each list
+ * entry also carries the point's colour, the uint at clr + i*clr_stride + clr_off
+ * (gvdbInsertSubcell, PT.cuh:236, 269) */
+int og_insert_points_subcell_clr(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off,
+                                 float R, const float trans[3], const void* clr, int clr_stride, int clr_off,
+                                 int64_t* out_len) {
+    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 0, (const char*)clr, clr_stride, clr_off);
 }
 int og_insert_points_subcell_fp16(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off,
                                   float R, const float trans[3], int64_t* out_len) {
-    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 1);
+    return insert_subcell(g, sc, posv, n, stride, off, R, trans, out_len, 1, NULL, 0, 0);
 }
 
 static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int stride, int off, float R,
-                          const float trans[3], int64_t* out_len, int fp16) {
+                          const float trans[3], int64_t* out_len, int fp16, const char* clr, int clr_stride,
+                          int clr_off) {
     const char* pos = (const char*)posv;
     const float prange[3] = {g->posmax[0] - g->posmin[0], g->posmax[1] - g->posmin[1], g->posmax[2] - g->posmin[2]};
     if (g->nused[0] == 0) return OG_NOOP;
@@ -752,7 +763,8 @@ static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int str
     }
     g->sc_nbricks = nl;
     size_t nsc = nl * (size_t)scpb;
-    free(g->sc_cnt); free(g->sc_off); free(g->sc_pts);
+    free(g->sc_cnt); free(g->sc_off); free(g->sc_pts); free(g->sc_clr);
+    g->sc_clr = NULL;
     g->sc_cnt = (int64_t*)calloc(nsc + 1, sizeof(int64_t));
     g->sc_off = (int64_t*)calloc(nsc + 1, sizeof(int64_t));
     int D = g->last_depth;
@@ -764,6 +776,7 @@ static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int str
             g->sc_off[nsc] = acc;
             g->sc_len = acc;
             g->sc_pts = (float*)malloc((size_t)(acc > 0 ? acc : 1) * 3 * sizeof(float));
+            if (clr) g->sc_clr = (uint32_t*)malloc((size_t)(acc > 0 ? acc : 1) * sizeof(uint32_t));
         }
         for (int64_t i = 0; i < n; i++) {
             float p[3];
@@ -791,6 +804,7 @@ static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int str
                             int64_t at = g->sc_off[idx] + g->sc_cnt[idx]++;
                             for (int a = 0; a < 3; a++)
                                 g->sc_pts[at * 3 + a] = fp16 ? quant16(w[a], g->posmin[a], prange[a]) : w[a];
+                            if (clr) memcpy(&g->sc_clr[at], clr + (size_t)i * clr_stride + clr_off, 4);
                         }
                     }
         }
@@ -803,6 +817,76 @@ static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int str
 /* gvdbGatherDensity / gvdbGatherLevelSet (PT.cuh:696-773) in FP64.
  * mode 0 = density: v = max(accum ? old : 0, max_j(rho - |p_j - v|))
  * mode 1 = level set: v = min(accum ? old : 3, min_j(|p_j - v| - rho)) */
+/* RGBA8 byte of an averaged colour component: the reference's uchar(c * 255.0f)
+ * (CLR2CHAR, PT.cuh:16) as the GPU converts it: truncation toward zero, values
+ * beyond [0, 255] clamped, NaN to 0 (PTX cvt.rzi to an integer type saturates) */
+static uint32_t clr_byte(float c255) {
+    if (!(c255 == c255)) return 0u;
+    if (c255 <= 0.0f) return 0u;
+    if (c255 >= 255.0f) return 255u;
+    return (uint32_t)c255;
+}
+
+/* The colour of one voxel (gvdbGatherDensity / gvdbGatherLevelSet, PT.cuh:717-731,
+ * 757-771): clr = accum ? CHAR2CLR(old) : (0, 0, 0, 1), plus CHAR2CLR of every list
+ * entry of the voxel's subcell, divided by (list length + accum), CLR2CHAR.  Here the
+ * sum is formed exactly, in integer byte units (the reference adds the FP32 terms
+ * c/255 in list order, which is arbitrary), then divided by 255 once; the remaining
+ * FP32 operations are the reference's: c / (n + accum), c * 255, truncation. */
+static uint32_t clr_average(const uint64_t sum[4], int64_t cnt, uint32_t old, int accum) {
+    uint32_t out = 0;
+    for (int k = 0; k < 4; k++) {
+        uint64_t t = sum[k] + (accum ? ((old >> (8 * k)) & 0xFFu) : (k == 3 ? 255u : 0u));
+        float c = (float)t / 255.0f;
+        c = c / (float)(cnt + (accum ? 1 : 0));
+        out |= clr_byte(c * 255.0f) << (8 * k);
+    }
+    return out;
+}
+
+int og_gather(OGrid* g, int mode, float rho, int chan, int accum);
+/* the gather with the colour channel clr_chan (T_UCHAR4; -1 = none): colours are
+ * averaged when the last insert carried point colours (VG.cpp:5063, PT.cuh:728) */
+int og_gather_clr(OGrid* g, int mode, float rho, int chan, int clr_chan, int accum) {
+    int rc = og_gather(g, mode, rho, chan, accum);
+    if (rc != OG_OK || clr_chan < 0 || !g->sc_clr) return rc;
+    if (clr_chan >= OG_MAXCHAN || !g->chan[clr_chan].used || g->chan[clr_chan].dtype != 2) return OG_INVALID_ARG;
+    int sc = g->sc_size;
+    int scres = og_res(g, 0) / sc;
+    int scpb = scres * scres * scres;
+    size_t nleaf = g->ncnt[0];
+    double* atl = g->chan[clr_chan].data;
+#ifdef _OPENMP
+    int nt = g->nthreads > 0 ? g->nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt)
+#endif
+    for (int64_t i = 0; i < (int64_t)nleaf; i++) {
+        const ONode* nd = &g->nodes[0][i];
+        if (nd->parent == UNDEF64) continue;
+        int64_t slot = leaf_slot(g, nd);
+        if (slot < 0) continue;
+        double* brick = atl + (size_t)slot * 5832;
+        for (int s = 0; s < scpb; s++) {
+            size_t idx = (size_t)g->sc_map[i] * scpb + s;
+            int sx = s % scres, sy = (s / scres) % scres, sz = s / (scres * scres);
+            int64_t beg = g->sc_len ? g->sc_off[idx] : 0, cnt = g->sc_len ? g->sc_off[idx + 1] - g->sc_off[idx] : 0;
+            uint64_t sum[4] = {0, 0, 0, 0};
+            for (int64_t j = 0; j < cnt; j++) {
+                uint32_t c = g->sc_clr[beg + j];
+                for (int k = 0; k < 4; k++) sum[k] += (c >> (8 * k)) & 0xFFu;
+            }
+            for (int tz = 0; tz < sc; tz++)
+                for (int ty = 0; ty < sc; ty++)
+                    for (int tx = 0; tx < sc; tx++) {
+                        int lx = sx * sc + tx, ly = sy * sc + ty, lz = sz * sc + tz;
+                        double* cell = brick + ((size_t)(lz + 1) * 18 + (ly + 1)) * 18 + (lx + 1);
+                        *cell = (double)clr_average(sum, cnt, (uint32_t)*cell, accum);
+                    }
+        }
+    }
+    return OG_OK;
+}
+
 int og_gather(OGrid* g, int mode, float rho, int chan, int accum) {
     if (chan < 0 || chan >= OG_MAXCHAN || !g->chan[chan].used) return OG_INVALID_ARG;
     if (g->nused[0] == 0) return OG_NOOP;
@@ -854,6 +938,9 @@ int og_gather(OGrid* g, int mode, float rho, int chan, int accum) {
 int og_update_apron(OGrid* g, int chan, float boundval) {
     if (chan < 0 || chan >= OG_MAXCHAN || !g->chan[chan].used) return OG_INVALID_ARG;
     double* atl = g->chan[chan].data;
+    /* T_UCHAR4: make_uchar4(boundval, ...) (OP.cuh:140-143) */
+    const uint32_t b8 = clr_byte(boundval);
+    const double bv = g->chan[chan].dtype == 2 ? (double)(b8 | (b8 << 8) | (b8 << 16) | (b8 << 24)) : (double)boundval;
     int used = g->atlas_last;
 #ifdef _OPENMP
     int nt = g->nthreads > 0 ? g->nthreads : omp_get_max_threads();
@@ -868,7 +955,7 @@ int og_update_apron(OGrid* g, int chan, float boundval) {
                 for (int x = 0; x < 18; x++) {
                     if (x > 0 && x < 17 && y > 0 && y < 17 && z > 0 && z < 17) continue;
                     int32_t w[3] = {bp[0] + x - 1, bp[1] + y - 1, bp[2] + z - 1};
-                    double v = (double)boundval;
+                    double v = bv;
                     int64_t nl = get_leaf_at_voxel(g, w);
                     if (nl >= 0) {
                         const ONode* nn = &g->nodes[0][nl];
@@ -882,6 +969,49 @@ int og_update_apron(OGrid* g, int chan, float boundval) {
                 }
     }
     return OG_OK;
+}
+
+/* FillChannel(chan, v) (VG.cpp:2456-2470) over every slot of the current atlas,
+ * interior and apron: FP channels get v[0] (FUNC_FILL_F), T_UCHAR4 channels
+ * CLR2INT(v0, v1, v2, 1) (FUNC_FILL_C4, OP.cuh:368-373; CLR2INT OP.cuh:20).  The
+ * reference's fill kernel leaves the atlas's first voxel plane on each axis (an
+ * apron plane) unwritten; here every voxel is written. */
+void og_fill_channel(OGrid* g, int chan, const float v[4]) {
+    if (chan < 0 || chan >= OG_MAXCHAN || !g->chan[chan].used) return;
+    OChan* ch = &g->chan[chan];
+    double val = (double)v[0];
+    if (ch->dtype == 2) {
+        uint32_t c = ((uint32_t)(1.0f * 255.0f) << 24) | ((uint32_t)(v[2] * 255.0f) << 16) |
+                     ((uint32_t)(v[1] * 255.0f) << 8) | (uint32_t)(v[0] * 255.0f);
+        val = (double)c;
+    }
+    size_t n = ch->cap_slots * 5832;
+    for (size_t i = 0; i < n; i++) ch->data[i] = val;
+}
+/* ClearChannel (VG.cpp:1596-1603): every voxel of the atlas to 0 */
+void og_clear_channel(OGrid* g, int chan) {
+    if (chan < 0 || chan >= OG_MAXCHAN || !g->chan[chan].used) return;
+    memset(g->chan[chan].data, 0, g->chan[chan].cap_slots * 5832 * sizeof(double));
+}
+
+/* ComputeBounds (VG.cpp:1792-1816): both corners start at the position of leaf 0
+ * of the pool (flagged or not); every flagged leaf then widens them by its box
+ * [pos, pos + range0).  out6 = {min xyz, max xyz}; returns 0 on an empty pool. */
+int og_compute_bounds(const OGrid* g, float out6[6]) {
+    if (g->ncnt[0] == 0) return 0;
+    const int64_t rg = og_range(g, 0);
+    float mn[3], mx[3];
+    for (int a = 0; a < 3; a++) mn[a] = mx[a] = (float)g->nodes[0][0].pos[a];
+    for (size_t i = 0; i < g->ncnt[0]; i++) {
+        const ONode* nd = &g->nodes[0][i];
+        if (!nd->flags) continue;
+        for (int a = 0; a < 3; a++) {
+            if ((float)nd->pos[a] < mn[a]) mn[a] = (float)nd->pos[a];
+            if ((float)(nd->pos[a] + rg) > mx[a]) mx[a] = (float)(nd->pos[a] + rg);
+        }
+    }
+    for (int a = 0; a < 3; a++) { out6[a] = mn[a]; out6[3 + a] = mx[a]; }
+    return 1;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -65,6 +65,13 @@ def lib():
         L.og_insert_points_subcell_fp16.argtypes = [vp, i32, vp, i64, i32, i32, f32, fp3,
                                                     ctypes.POINTER(ctypes.c_int64)]
         L.og_gather.argtypes = [vp, i32, f32, i32, i32]
+        L.og_gather_clr.argtypes = [vp, i32, f32, i32, i32, i32]
+        L.og_insert_points_subcell_clr.argtypes = [vp, i32, vp, i64, i32, i32, f32, fp3, vp, i32, i32,
+                                                   ctypes.POINTER(ctypes.c_int64)]
+        L.og_fill_channel.argtypes = [vp, i32, fp3]
+        L.og_clear_channel.argtypes = [vp, i32]
+        L.og_compute_bounds.restype = i32
+        L.og_compute_bounds.argtypes = [vp, fp3]
         L.og_update_apron.argtypes = [vp, i32, f32]
         for name in ("og_depth", "og_top_lev", "og_childlist_len"):
             getattr(L, name).restype = i32
@@ -193,11 +200,18 @@ class OracleGrid:
     def update_atlas(self):
         return lib().og_update_atlas(self._h)
 
-    def insert_points_subcell(self, points, radius, subcell=4, trans=(0, 0, 0)):
+    def insert_points_subcell(self, points, radius, subcell=4, trans=(0, 0, 0), colours=None):
+        """colours: None or one uint32 RGBA8 (R in the low byte) per point"""
         p, n, stride = self._pts(points)
         out = ctypes.c_int64(-1)
-        rc = lib().og_insert_points_subcell(self._h, subcell, p.ctypes.data, n, stride, 0,
-                                            float(radius), _f3(trans), ctypes.byref(out))
+        if colours is None:
+            rc = lib().og_insert_points_subcell(self._h, subcell, p.ctypes.data, n, stride, 0,
+                                                float(radius), _f3(trans), ctypes.byref(out))
+        else:
+            c = np.ascontiguousarray(colours, dtype=np.uint32)
+            assert c.shape[0] >= n
+            rc = lib().og_insert_points_subcell_clr(self._h, subcell, p.ctypes.data, n, stride, 0, float(radius),
+                                                    _f3(trans), c.ctypes.data, 4, 0, ctypes.byref(out))
         return rc, int(out.value)
 
     def insert_points_subcell_fp16(self, points, radius, subcell=4, trans=(0, 0, 0)):
@@ -208,11 +222,27 @@ class OracleGrid:
                                                  float(radius), _f3(trans), ctypes.byref(out))
         return rc, int(out.value)
 
-    def gather_density(self, radius, chan=0, accum=False):
-        return lib().og_gather(self._h, 0, float(radius), chan, 1 if accum else 0)
+    def gather_density(self, radius, chan=0, accum=False, clr_chan=-1):
+        return lib().og_gather_clr(self._h, 0, float(radius), chan, clr_chan, 1 if accum else 0)
 
-    def gather_levelset(self, radius, chan=0, accum=False):
-        return lib().og_gather(self._h, 1, float(radius), chan, 1 if accum else 0)
+    def gather_levelset(self, radius, chan=0, accum=False, clr_chan=-1):
+        return lib().og_gather_clr(self._h, 1, float(radius), chan, clr_chan, 1 if accum else 0)
+
+    def fill_channel(self, chan, value):
+        """FillChannel: a float, or a 4-vector (x, y, z, w) as the reference's Vector4DF"""
+        v = list(value) if hasattr(value, "__len__") else [float(value), 0.0, 0.0, 0.0]
+        a = (ctypes.c_float * 4)(*[float(x) for x in v])
+        lib().og_fill_channel(self._h, chan, a)
+
+    def clear_channel(self, chan):
+        lib().og_clear_channel(self._h, chan)
+
+    def compute_bounds(self):
+        """ComputeBounds restated: (min xyz, max xyz) as floats, or None for an empty pool"""
+        out = (ctypes.c_float * 6)()
+        if not lib().og_compute_bounds(self._h, out):
+            return None
+        return np.array(out[:], dtype=np.float32)
 
     def update_apron(self, chan=0, boundval=0.0):
         return lib().og_update_apron(self._h, chan, float(boundval))
@@ -257,7 +287,8 @@ class OracleGrid:
         return _copy(lib().og_atlas_map(self._h), AMAP_DTYPE, ax * ay * az)
 
     def atlas_bricks(self, chan=0, slots=None):
-        """FP64 padded bricks, shape (slots, 18, 18, 18) indexed [slot, z, y, x]."""
+        """FP64 padded bricks, shape (slots, 18, 18, 18) indexed [slot, z, y, x] (a T_UCHAR4
+        channel holds each RGBA8 voxel as the value of its uint32)."""
         ax, ay, az, used = self.atlas_dims()
         n = used if slots is None else slots
         return _copy(lib().og_atlas_data(self._h, chan), np.float64, n * 5832).reshape(n, 18, 18, 18)

@@ -104,11 +104,14 @@ struct Harness {
     // points
     CUdeviceptr pts = 0;
     int npts = 0;
-    // atlas (channel 0, T_FLOAT)
+    // atlas: channel 0 T_FLOAT, channel 1 T_UCHAR4 (colour, created on request)
     int ax = 16, ay = 16, az = 1;
     int atlas_last = 0;
-    CUarray arr = nullptr;
-    CUsurfObject surf = 0;
+    CUarray arr = nullptr, carr = nullptr;
+    CUsurfObject surf = 0, csurf = 0;
+    bool colour_chan = false;
+    CUdeviceptr clr = 0;  // point colours (uint per point), 0 = none
+    CUdeviceptr sc_clr = 0;
     CUdeviceptr amap = 0;
     size_t amap_cnt = 0;
     std::vector<int32_t> amap_cpu;
@@ -123,6 +126,30 @@ struct Harness {
     CUdeviceptr bbx = 0, bby = 0, bbz = 0, bbox = 0;
     size_t bb_cap = 0;
     CUevent ev0 = nullptr, ev1 = nullptr;
+    // kernel timing: an event pair around every kernel launch and Thrust call
+    bool timing = false;
+    std::vector<CUevent> tev;
+    size_t ntev = 0;
+    void tmark() {
+        if (!timing) return;
+        if (ntev == tev.size()) {
+            CUevent e;
+            ck(cuEventCreate(&e, 0), "event");
+            tev.push_back(e);
+        }
+        ck(cuEventRecord(tev[ntev++], 0), "event");
+    }
+    float kernel_ms() {  // sum over the recorded pairs
+        if (!ntev) return 0.0f;
+        ck(cuEventSynchronize(tev[ntev - 1]), "event");
+        float tot = 0.0f;
+        for (size_t i = 0; i + 1 < ntev; i += 2) {
+            float ms = 0.0f;
+            ck(cuEventElapsedTime(&ms, tev[i], tev[i + 1]), "event");
+            tot += ms;
+        }
+        return tot;
+    }
 
     CUfunction fn(const char* name) {
         CUfunction f;
@@ -137,7 +164,10 @@ struct Harness {
         }
     }
     void launch(const char* name, unsigned gx, unsigned gy, unsigned gz, unsigned bx, unsigned by, unsigned bz, void** args) {
-        ck(cuLaunchKernel(fn(name), gx, gy, gz, bx, by, bz, 0, nullptr, args, nullptr), name);
+        CUfunction f = fn(name);
+        tmark();
+        ck(cuLaunchKernel(f, gx, gy, gz, bx, by, bz, 0, nullptr, args, nullptr), name);
+        tmark();
     }
     void realloc_dev(CUdeviceptr& p, size_t& cap, size_t need) {
         if (need <= cap && p) return;
@@ -241,6 +271,7 @@ struct Harness {
             info.atlas_res[0] = ax * 18; info.atlas_res[1] = ay * 18; info.atlas_res[2] = az * 18;
             info.brick_res = 18;
             info.volOut[0] = surf;
+            info.volOut[1] = csurf;
         }
         ck(cuMemcpyHtoD(cuinfo, &info, sizeof(info)), "prepare");
     }
@@ -282,8 +313,12 @@ struct Harness {
         float out[6];
         for (int i = 0; i < 3; i++) {
             thrust::device_ptr<float> b = thrust::device_pointer_cast((float*)ax3[i]);
-            out[i] = *thrust::min_element(b, b + npts);
-            out[3 + i] = *thrust::max_element(b, b + npts);
+            tmark();
+            auto mn = thrust::min_element(b, b + npts);
+            auto mx = thrust::max_element(b, b + npts);
+            tmark();
+            out[i] = *mn;
+            out[3 + i] = *mx;
         }
         for (int a = 0; a < 3; a++) {
             posmin[a] = out[a] - 1; posmax[a] = out[3 + a] + 2;
@@ -318,7 +353,9 @@ struct Harness {
         aux(sorted, (size_t)count * 8);
         ck(cuMemcpyDtoD(sorted, keys, (size_t)count * 8), "sort copy");
         thrust::device_ptr<uint64_t> b = thrust::device_pointer_cast((uint64_t*)sorted);
+        tmark();
         thrust::sort(b, b + count, thrust::less<uint64_t>());
+        tmark();
         aux(marker, (size_t)count * 4);
         aux(presum, (size_t)count * 4);
         aux(cnt, 4);
@@ -460,6 +497,17 @@ struct Harness {
         return ex;
     }
 
+    int accumulate_topology(float radius, float3 orig, int min_depth) {  // VG.cpp:1158-1178
+        bounding_box(orig);
+        int root[3];
+        int D = determine_depth(root);
+        if (D < min_depth) D = min_depth;
+        if (D == 0 || D > 5) return 4;
+        if (rebuild) return rebuild_topology(radius, orig);
+        box_pass(radius, orig, D, true, true);
+        return 0;
+    }
+
     int rebuild_topology(float radius, float3 orig) {  // VG.cpp:1181-1218
         bounding_box(orig);
         int root[3];
@@ -478,20 +526,36 @@ struct Harness {
     }
 
     // ---- atlas (AL.cpp:311-456, 622-715; VG.cpp:2630-2704)
-    void make_atlas(int new_az, bool preserve) {
+    // One CUarray per channel; a grown array is cleared and the old one copied in
+    // (AllocateTextureGPU, AL.cpp:389-456).  A fresh array is cleared as well.
+    void make_array(CUarray& a, CUsurfObject& so, bool colour, int new_az, bool preserve) {
         CUDA_ARRAY3D_DESCRIPTOR d{};
-        d.Format = CU_AD_FORMAT_FLOAT;
-        d.NumChannels = 1;
+        d.Format = colour ? CU_AD_FORMAT_UNSIGNED_INT8 : CU_AD_FORMAT_FLOAT;
+        d.NumChannels = colour ? 4 : 1;
         d.Width = (size_t)ax * 18;
         d.Height = (size_t)ay * 18;
         d.Depth = (size_t)new_az * 18;
         d.Flags = CUDA_ARRAY3D_SURFACE_LDST;
         CUarray na;
         ck(cuArray3DCreate(&na, &d), "atlas");
-        if (preserve && arr) {
+        {
+            std::vector<char> zero((size_t)ax * 18 * 4 * ay * 18 * new_az * 18, 0);
+            CUDA_MEMCPY3D cp{};
+            cp.srcMemoryType = CU_MEMORYTYPE_HOST;
+            cp.srcHost = zero.data();
+            cp.srcPitch = (size_t)ax * 18 * 4;
+            cp.srcHeight = (size_t)ay * 18;
+            cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+            cp.dstArray = na;
+            cp.WidthInBytes = (size_t)ax * 18 * 4;
+            cp.Height = (size_t)ay * 18;
+            cp.Depth = (size_t)new_az * 18;
+            ck(cuMemcpy3D(&cp), "atlas clear");
+        }
+        if (preserve && a) {
             CUDA_MEMCPY3D cp{};
             cp.srcMemoryType = CU_MEMORYTYPE_ARRAY;
-            cp.srcArray = arr;
+            cp.srcArray = a;
             cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
             cp.dstArray = na;
             cp.WidthInBytes = (size_t)ax * 18 * 4;
@@ -499,14 +563,35 @@ struct Harness {
             cp.Depth = (size_t)az * 18;
             ck(cuMemcpy3D(&cp), "atlas copy");
         }
-        if (surf) cuSurfObjectDestroy(surf);
-        if (arr) cuArrayDestroy(arr);
-        arr = na;
+        if (so) cuSurfObjectDestroy(so);
+        if (a) cuArrayDestroy(a);
+        a = na;
         CUDA_RESOURCE_DESC rd{};
         rd.resType = CU_RESOURCE_TYPE_ARRAY;
-        rd.res.array.hArray = arr;
-        ck(cuSurfObjectCreate(&surf, &rd), "surf");
+        rd.res.array.hArray = a;
+        ck(cuSurfObjectCreate(&so, &rd), "surf");
+    }
+    void make_atlas(int new_az, bool preserve) {
+        make_array(arr, surf, false, new_az, preserve);
+        if (colour_chan) make_array(carr, csurf, true, new_az, preserve);
         az = new_az;
+    }
+    // FillChannel(chan, v) as the whole atlas array (the reference's FUNC_FILL_F leaves the
+    // array's first voxel plane of each axis, an apron plane, unwritten)
+    void fill(int chan, float v) {
+        size_t W = (size_t)ax * 18, H = (size_t)ay * 18, Dz = (size_t)az * 18;
+        std::vector<float> vals(W * H * Dz, v);
+        CUDA_MEMCPY3D cp{};
+        cp.srcMemoryType = CU_MEMORYTYPE_HOST;
+        cp.srcHost = vals.data();
+        cp.srcPitch = W * 4;
+        cp.srcHeight = H;
+        cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+        cp.dstArray = chan == 0 ? arr : carr;
+        cp.WidthInBytes = W * 4;
+        cp.Height = H;
+        cp.Depth = Dz;
+        ck(cuMemcpy3D(&cp), "fill");
     }
     void update_atlas() {
         size_t total = pool[0][0].lastEle, used = pool[0][0].usedNum;
@@ -570,8 +655,11 @@ struct Harness {
         ck(cuMemsetD8(sc_cnt, 0, (size_t)nsc * 4), "cnt");
         aux(sc_pnts, (size_t)sc_len * 12);
         CUdeviceptr z = 0;
+        int cstride = 4;
+        if (clr) aux(sc_clr, (size_t)sc_len * 4);  // VG.cpp:5063
         void* d[23] = {&cuinfo, &sc, &scpb, &npts, &sc_cnt, &sc_off, &sc_map, &rng, &trans, &scdim, &radius,
-                       &pts, &off, &stride, &sc_pnts, &z, &off, &stride, &z, &z, &off, &stride, &z};
+                       &pts, &off, &stride, &sc_pnts, &z, &off, &stride, &z, clr ? &clr : &z, &off, &cstride,
+                       clr ? &sc_clr : &z};
         launch("gvdbInsertSubcell", npts / 512 + 1, 1, 1, 512, 1, 1, d);
         aux(sc_pos, (size_t)nsc * 12);
         aux(sc_nid, (size_t)nsc * 4);
@@ -586,31 +674,32 @@ struct Harness {
         prepare(false);
         int nsc = 64 * num_brick;
         CUdeviceptr z = 0;
-        int chan = 0, clr = 1;
-        void* a[14] = {&cuinfo, &npts, &nsc, &radius, &sc_nid, &sc_cnt, &sc_off, &sc_pos, &sc_pnts, &z, &z, &chan, &clr,
-                       &accum};
+        int chan = 0, cchan = 1;
+        CUdeviceptr cl = (clr && colour_chan) ? sc_clr : 0;
+        void* a[14] = {&cuinfo, &npts, &nsc, &radius, &sc_nid, &sc_cnt, &sc_off, &sc_pos, &sc_pnts, &z, &cl, &chan,
+                       &cchan, &accum};
         launch(mode == 0 ? "gvdbGatherDensity" : "gvdbGatherLevelSet", nsc, 1, 1, 4, 4, 4, a);
         return 0;
     }
 
-    int update_apron(float boundval) {  // VG.cpp:4418-4457
+    int update_apron(int c, float boundval) {  // VG.cpp:4418-4457
         prepare(false);
         int bricks = (int)pool[0][0].lastEle;
         if (bricks == 0) return 8;
-        unsigned char chan = 0;
+        unsigned char chan = (unsigned char)c;
         int brickres = 18, brickwid = 16;
         void* a[6] = {&cuinfo, &chan, &bricks, &brickres, &brickwid, &boundval};
-        launch("gvdbUpdateApronF", bricks, (18 + 7) / 8, (18 + 7) / 8, 6, 8, 8, a);
+        launch(c == 0 ? "gvdbUpdateApronF" : "gvdbUpdateApronC4", bricks, (18 + 7) / 8, (18 + 7) / 8, 6, 8, 8, a);
         return 0;
     }
 
     // padded bricks of slots [0, used) from the CUarray, [slot][z][y][x]
-    void read_bricks(float* out) {
+    void read_bricks(int chan, float* out) {  // 4-byte voxels (FP32 or RGBA8)
         size_t W = (size_t)ax * 18, H = (size_t)ay * 18, Dz = (size_t)az * 18;
         std::vector<float> all(W * H * Dz);
         CUDA_MEMCPY3D cp{};
         cp.srcMemoryType = CU_MEMORYTYPE_ARRAY;
-        cp.srcArray = arr;
+        cp.srcArray = chan == 0 ? arr : carr;
         cp.dstMemoryType = CU_MEMORYTYPE_HOST;
         cp.dstHost = all.data();
         cp.dstPitch = W * 4;
@@ -691,8 +780,65 @@ int rh_gather(void* hp, int mode, float radius, int accum) {
     Harness* h = (Harness*)hp;
     RH_TRY(h, return h->gather(mode, radius, accum != 0));
 }
-int rh_update_apron(void* hp, float boundval) { Harness* h = (Harness*)hp; RH_TRY(h, return h->update_apron(boundval)); }
+int rh_update_apron(void* hp, int chan, float boundval) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, return h->update_apron(chan, boundval));
+}
+int rh_accumulate_topology(void* hp, float radius, const float* orig, int min_depth) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, return h->accumulate_topology(radius, make_float3(orig[0], orig[1], orig[2]), min_depth));
+}
+// AddChannel(1, T_UCHAR4): a colour channel with the atlas layout of channel 0
+int rh_add_colour_channel(void* hp) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, {
+        h->colour_chan = true;
+        h->make_array(h->carr, h->csurf, true, h->az, false);
+        return 0;
+    });
+}
+// point colours (RGBA8 as one uint per point; n must match the last rh_set_points), NULL clears
+int rh_set_colors(void* hp, const uint32_t* host_rgba, int n) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, {
+        if (h->clr) cuMemFree(h->clr);
+        h->clr = 0;
+        if (host_rgba) {
+            h->ck(cuMemAlloc(&h->clr, (size_t)std::max(n, 1) * 4), "clr");
+            if (n) h->ck(cuMemcpyHtoD(h->clr, host_rgba, (size_t)n * 4), "clr");
+        }
+        return 0;
+    });
+}
+int rh_fill(void* hp, int chan, float v) { Harness* h = (Harness*)hp; RH_TRY(h, h->fill(chan, v); return 0); }
+// per-kernel timing: on = 1 starts a new record; rh_kernel_ms returns the summed device
+// time of the kernels and Thrust calls launched since
+int rh_timing(void* hp, int on) {
+    Harness* h = (Harness*)hp;
+    h->timing = on != 0;
+    h->ntev = 0;
+    return 0;
+}
+float rh_kernel_ms(void* hp) {
+    Harness* h = (Harness*)hp;
+    try {
+        return h->kernel_ms();
+    } catch (const std::string& e) {
+        h->err = e;
+        return -1.0f;
+    }
+}
 int rh_sync(void* hp) { Harness* h = (Harness*)hp; RH_TRY(h, h->ck(cuCtxSynchronize(), "sync"); return 0); }
+// CUDA events on the NULL stream, which every launch and copy of the harness uses
+int rh_event_begin(void* hp) { Harness* h = (Harness*)hp; RH_TRY(h, h->ck(cuEventRecord(h->ev0, 0), "ev"); return 0); }
+float rh_event_end_ms(void* hp) {
+    Harness* h = (Harness*)hp;
+    float ms = -1.0f;
+    if (cuEventRecord(h->ev1, 0) != CUDA_SUCCESS || cuEventSynchronize(h->ev1) != CUDA_SUCCESS ||
+        cuEventElapsedTime(&ms, h->ev0, h->ev1) != CUDA_SUCCESS)
+        return -1.0f;
+    return ms;
+}
 
 long long rh_node_count(void* hp, int lev) { return (long long)((Harness*)hp)->pool[0][lev].lastEle; }
 long long rh_used_count(void* hp, int lev) { return (long long)((Harness*)hp)->pool[0][lev].usedNum; }
@@ -713,7 +859,10 @@ void rh_atlas_map(void* hp, int* out) {
     Harness* h = (Harness*)hp;
     memcpy(out, h->amap_cpu.data(), h->amap_cpu.size() * 4);
 }
-int rh_atlas_bricks(void* hp, float* out) { Harness* h = (Harness*)hp; RH_TRY(h, h->read_bricks(out); return 0); }
+int rh_atlas_bricks(void* hp, int chan, float* out) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, h->read_bricks(chan, out); return 0);
+}
 // subcell lists: counts/offsets of the first `nsub` subcells and the list points
 int rh_subcells(void* hp, int* cnt_out, int* off_out, float* pts_out) {
     Harness* h = (Harness*)hp;

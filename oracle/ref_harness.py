@@ -20,14 +20,26 @@ class RefGrid:
         L.rh_create.restype = vp
         L.rh_create.argtypes = [ctypes.c_char_p, i32, ctypes.POINTER(ctypes.c_int)]
         for n in ("rh_set_points", "rh_rebuild_topology", "rh_update_atlas", "rh_insert_subcell", "rh_gather",
-                  "rh_update_apron", "rh_sync", "rh_top_lev", "rh_atlas_bricks", "rh_subcells", "rh_subcell_num"):
+                  "rh_update_apron", "rh_sync", "rh_top_lev", "rh_atlas_bricks", "rh_subcells", "rh_subcell_num",
+                  "rh_accumulate_topology", "rh_add_colour_channel", "rh_set_colors", "rh_fill", "rh_event_begin"):
             getattr(L, n).restype = i32
+        L.rh_accumulate_topology.argtypes = [vp, f32, fp, i32]
+        L.rh_add_colour_channel.argtypes = [vp]
+        L.rh_set_colors.argtypes = [vp, vp, i32]
+        L.rh_fill.argtypes = [vp, i32, f32]
+        L.rh_event_begin.argtypes = [vp]
+        L.rh_event_end_ms.restype = f32
+        L.rh_event_end_ms.argtypes = [vp]
+        L.rh_timing.restype = i32
+        L.rh_timing.argtypes = [vp, i32]
+        L.rh_kernel_ms.restype = f32
+        L.rh_kernel_ms.argtypes = [vp]
         L.rh_set_points.argtypes = [vp, fp, i32]
         L.rh_rebuild_topology.argtypes = [vp, f32, fp]
         L.rh_update_atlas.argtypes = [vp]
         L.rh_insert_subcell.argtypes = [vp, f32, fp, ctypes.POINTER(ctypes.c_int)]
         L.rh_gather.argtypes = [vp, i32, f32, i32]
-        L.rh_update_apron.argtypes = [vp, f32]
+        L.rh_update_apron.argtypes = [vp, i32, f32]
         L.rh_sync.argtypes = [vp]
         L.rh_node_count.restype = ctypes.c_longlong
         L.rh_node_count.argtypes = [vp, i32]
@@ -38,7 +50,7 @@ class RefGrid:
         L.rh_childlist.argtypes = [vp, i32, vp]
         L.rh_atlas_dims.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
         L.rh_atlas_map.argtypes = [vp, vp]
-        L.rh_atlas_bricks.argtypes = [vp, vp]
+        L.rh_atlas_bricks.argtypes = [vp, i32, vp]
         L.rh_subcells.argtypes = [vp, vp, vp, vp]
         L.rh_subcell_num.argtypes = [vp]
         L.rh_error.restype = ctypes.c_char_p
@@ -63,6 +75,39 @@ class RefGrid:
         self._keep = p
         self._ok(self.L.rh_set_points(self.h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), p.shape[0]), "set")
 
+    def set_colors(self, rgba):
+        """point colours, one uint32 (RGBA8, R in the low byte) per point; None: no colours"""
+        if rgba is None:
+            self._ok(self.L.rh_set_colors(self.h, None, 0), "colors")
+            return
+        c = np.ascontiguousarray(rgba, dtype=np.uint32)
+        self._keep_clr = c
+        self._ok(self.L.rh_set_colors(self.h, c.ctypes.data, c.shape[0]), "colors")
+
+    def add_colour_channel(self):
+        self._ok(self.L.rh_add_colour_channel(self.h), "colour channel")
+
+    def fill(self, chan, value):
+        self._ok(self.L.rh_fill(self.h, chan, float(value)), "fill")
+
+    def accumulate_topology(self, radius, orig=(0, 0, 0), min_depth=1):
+        o = (ctypes.c_float * 3)(*orig)
+        return self._ok(self.L.rh_accumulate_topology(self.h, radius, o, int(min_depth)), "accumulate")
+
+    def event_begin(self):
+        self._ok(self.L.rh_event_begin(self.h), "event")
+
+    def event_end_ms(self):
+        return float(self.L.rh_event_end_ms(self.h))
+
+    def timing(self, on=True):
+        """start (or stop) recording an event pair around every kernel / Thrust call"""
+        self.L.rh_timing(self.h, 1 if on else 0)
+
+    def kernel_ms(self):
+        """summed device time of the kernels and Thrust calls since timing(True)"""
+        return float(self.L.rh_kernel_ms(self.h))
+
     def rebuild_topology(self, radius, orig=(0, 0, 0)):
         o = (ctypes.c_float * 3)(*orig)
         return self._ok(self.L.rh_rebuild_topology(self.h, radius, o), "rebuild")
@@ -77,14 +122,14 @@ class RefGrid:
         self.len = n.value
         return rc, n.value
 
-    def gather_density(self, radius):
-        return self._ok(self.L.rh_gather(self.h, 0, radius, 0), "gather")
+    def gather_density(self, radius, accum=False):
+        return self._ok(self.L.rh_gather(self.h, 0, radius, 1 if accum else 0), "gather")
 
-    def gather_levelset(self, radius):
-        return self._ok(self.L.rh_gather(self.h, 1, radius, 0), "gather")
+    def gather_levelset(self, radius, accum=False):
+        return self._ok(self.L.rh_gather(self.h, 1, radius, 1 if accum else 0), "gather")
 
-    def update_apron(self, boundval):
-        return self._ok(self.L.rh_update_apron(self.h, boundval), "apron")
+    def update_apron(self, boundval, chan=0):
+        return self._ok(self.L.rh_update_apron(self.h, chan, boundval), "apron")
 
     def sync(self):
         self._ok(self.L.rh_sync(self.h), "sync")
@@ -125,11 +170,12 @@ class RefGrid:
         self.L.rh_atlas_map(self.h, out.ctypes.data)
         return out
 
-    def atlas_bricks(self):
+    def atlas_bricks(self, chan=0):
+        """padded bricks of the assigned slots, [slot, z, y, x]: FP32 (chan 0) or RGBA8 as uint32 (chan 1)"""
         used = self.atlas_dims()[3]
-        out = np.zeros(used * 5832, dtype=np.float32)
+        out = np.zeros(used * 5832, dtype=np.float32 if chan == 0 else np.uint32)
         if used:
-            self._ok(self.L.rh_atlas_bricks(self.h, out.ctypes.data), "bricks")
+            self._ok(self.L.rh_atlas_bricks(self.h, chan, out.ctypes.data), "bricks")
         return out.reshape(used, 18, 18, 18)
 
     def subcells(self):

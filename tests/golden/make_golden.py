@@ -5,7 +5,15 @@ compiled from the reference's kernels/cuda_gvdb_module.cu) are driven by
 oracle/ref_harness.cu, a restatement of VolumeGVDB's host code for the path,
 on small seeded inputs.  Each fixture stores the inputs and the reference's
 outputs: node pools, child lists, atlas map, subcell counts and per-subcell
-membership hashes, per-slot sums of the gathered channel and a few full bricks.
+membership hashes and every padded brick of the gathered channel (and of the
+colour channel where the case has one).
+
+Cases cover the call sequences of the reference's samples: RebuildTopology
+frames (full, then incremental), GatherDensity and GatherLevelSet, the
+accumulating gathers after FillChannel with AccumulateTopology
+(gPointFusion's sequence), GatherDensity with accumulation and point colours
+into a T_UCHAR4 channel on a fixed topology (gSprayDeposit's), and
+GatherLevelSet with colours (gFluidSurface's with m_use_color).
 
     python tests/golden/make_golden.py [out_dir]      (default: tests/golden)
 
@@ -40,7 +48,41 @@ def cases():
     pts = datasets.shell(2000, seed=102, rmin=30.0, rmax=40.0)
     out.append(dict(name="shell_levelset_r4", log2dims=(3, 3, 3, 4), radius=4.0, R=4.0, rho=2.0, mode="levelset",
                     boundval=3.0, frames=[pts]))
+    # AccumulateTopology + accumulating GatherLevelSet after FillChannel(0, 3)
+    pos, vel = datasets.fluid(n=5000, seed=103, box=(16, 24, 16), domain=32)
+    pos = pos + np.array([100.0, 60.0, 30.0], dtype=np.float32)
+    frames = [(pos + 1.5 * (k + 1) * vel).astype(np.float32) for k in range(3)]
+    out.append(dict(name="accum_levelset", log2dims=(3, 3, 3, 4), radius=2.0, R=2.0, rho=1.0, mode="levelset",
+                    boundval=3.0, frames=frames, topology="accumulate", fill=3.0, accum=True))
+    # fixed topology from a shell, then three batches of coloured points gathered with
+    # accumulation (density) into channel 0 and colours into channel 1
+    rng = np.random.default_rng(104)
+    base = datasets.shell(3000, seed=104, center=(200.0, 200.0, 200.0), rmin=40.0, rmax=50.0)
+    frames, colours = [base], [None]
+    for k in range(3):
+        sub = base[rng.choice(base.shape[0], 700, replace=False)]
+        sub = (sub + rng.normal(0.0, 0.7, size=sub.shape)).astype(np.float32)
+        frames.append(sub)
+        colours.append(_colours(rng, sub.shape[0]))
+    out.append(dict(name="accum_density_colour", log2dims=(3, 3, 3, 4), radius=1.0, R=1.0, rho=1.0, mode="density",
+                    boundval=0.0, frames=frames, colours=colours, topology="fixed", accum=True))
+    # GatherLevelSet with colours, full then incremental frame, on a depth-1 tree (root at
+    # level 1, [0, 128)^3; every box position stays inside it)
+    pos, vel = datasets.fluid(n=4000, seed=105, box=(16, 16, 16), domain=32)
+    pos = pos + np.array([24.0, 30.0, 20.0], dtype=np.float32)
+    frames = [(pos + 0.5 * (k + 1) * vel).astype(np.float32) for k in range(3)]
+    colours = [_colours(rng, f.shape[0]) for f in frames]
+    out.append(dict(name="colour_levelset", log2dims=(3, 3, 3, 4), radius=4.0, R=4.0, rho=2.0, mode="levelset",
+                    boundval=3.0, frames=frames, colours=colours))
     return out
+
+
+def _colours(rng, n):
+    """RGBA8 per point as uint32 (R in the low byte); a third opaque, a third with
+    random alpha, a third all-random"""
+    c = rng.integers(0, 256, size=(n, 4), dtype=np.uint32)
+    c[: n // 3, 3] = 255
+    return (c[:, 0] | (c[:, 1] << 8) | (c[:, 2] << 16) | (c[:, 3] << 24)).astype(np.uint32)
 
 
 def membership_hash(off, cnt, pts):
@@ -55,7 +97,7 @@ def membership_hash(off, cnt, pts):
     return h
 
 
-def snapshot(prefix, g, store):
+def snapshot(prefix, g, store, colour=False):
     store[prefix + "top_lev"] = g.top_lev
     store[prefix + "used"] = g.used_count(0)
     for lev in range(g.levs):
@@ -70,13 +112,9 @@ def snapshot(prefix, g, store):
     store[prefix + "sc_cnt"] = cnt
     store[prefix + "sc_hash"] = membership_hash(off, cnt, pts)
     store[prefix + "len"] = g.len
-    b = g.atlas_bricks().astype(np.float64)
-    inner = b[:, 1:17, 1:17, 1:17].reshape(b.shape[0], -1)
-    m = np.ones((18, 18, 18), bool)
-    m[1:17, 1:17, 1:17] = False
-    store[prefix + "slot_sum"] = inner.sum(axis=1)
-    store[prefix + "apron_sum"] = b[:, m].sum(axis=1)
-    store[prefix + "bricks"] = b[:4].astype(np.float32)
+    store[prefix + "bricks"] = g.atlas_bricks(0)
+    if colour:
+        store[prefix + "colour"] = g.atlas_bricks(1)
 
 
 def main(out_dir):
@@ -85,21 +123,40 @@ def main(out_dir):
     os.makedirs(out_dir, exist_ok=True)
     for c in cases():
         g = ref_harness.RefGrid(c["log2dims"])
+        topo = c.get("topology", "rebuild")
+        accum = bool(c.get("accum", False))
+        colours = c.get("colours")
         store = {"log2dims": np.array(c["log2dims"]), "radius": c["radius"], "R": c["R"], "rho": c["rho"],
-                 "mode": c["mode"], "boundval": c["boundval"], "nframes": len(c["frames"])}
+                 "mode": c["mode"], "boundval": c["boundval"], "nframes": len(c["frames"]), "topology": topo,
+                 "accum": accum, "colour": colours is not None}
+        if colours is not None:
+            g.add_colour_channel()
+        if c.get("fill") is not None:
+            store["fill"] = c["fill"]
+            g.fill(0, c["fill"])
         for k, pts in enumerate(c["frames"]):
             store["f%d_points" % k] = pts
+            clr = colours[k] if colours is not None else None
+            if clr is not None:
+                store["f%d_colours" % k] = clr
             g.set_points(pts)
-            g.rebuild_topology(c["radius"])
-            g.update_atlas()
+            g.set_colors(clr)
+            if topo == "accumulate":
+                g.accumulate_topology(c["radius"])
+            elif topo == "rebuild" or k == 0:
+                g.rebuild_topology(c["radius"])
+            if topo != "fixed" or k == 0:
+                g.update_atlas()
             g.insert_points_subcell(c["R"])
             if c["mode"] == "density":
-                g.gather_density(c["rho"])
+                g.gather_density(c["rho"], accum)
             else:
-                g.gather_levelset(c["rho"])
-            g.update_apron(c["boundval"])
+                g.gather_levelset(c["rho"], accum)
+            g.update_apron(c["boundval"], 0)
+            if colours is not None:
+                g.update_apron(0.0, 1)
             g.sync()
-            snapshot("f%d_" % k, g, store)
+            snapshot("f%d_" % k, g, store, colours is not None)
         path = os.path.join(out_dir, c["name"] + ".npz")
         np.savez_compressed(path, **store)
         print(path, os.path.getsize(path))

@@ -4,9 +4,15 @@ kernels/cuda_gvdb_module.cu, run under a restatement of its host code).
 
 Pinned bit-exactly: node pools (lev, flags, pos, value, parent, childlist),
 child lists, top level, used leaf count, atlas dimensions and map, subcell list
-lengths and per-subcell membership hashes.  Gathered values: per-slot sums of
-the interior and apron voxels and four full bricks within 1e-5 relative /
-1e-6 absolute per voxel (the reference computes sqrtf under --use_fast_math).
+lengths and per-subcell membership hashes.  Gathered values: every voxel of
+every padded brick (interior and apron) within 1e-5 relative / 1e-6 absolute
+(the reference computes sqrtf under --use_fast_math).  Colours (T_UCHAR4): every
+byte within 1 of the reference's, which adds its FP32 terms c/255 in the
+arbitrary order of its atomically filled lists.
+
+Call sequences: RebuildTopology frames (full, then incremental);
+AccumulateTopology with accumulating gathers after FillChannel; a fixed
+topology with accumulating, coloured density gathers; coloured level sets.
 """
 import glob
 import os
@@ -25,17 +31,36 @@ def run_oracle(fx):
     g = oracle.OracleGrid(tuple(int(v) for v in fx["log2dims"]))
     g.add_channel(0)
     mode = str(fx["mode"])
+    topo = str(fx["topology"]) if "topology" in fx.files else "rebuild"
+    accum = bool(fx["accum"]) if "accum" in fx.files else False
+    colour = bool(fx["colour"]) if "colour" in fx.files else False
+    if colour:
+        g.add_channel(1, dtype=2)
+    if "fill" in fx.files:
+        g.fill_channel(0, float(fx["fill"]))
     for k in range(int(fx["nframes"])):
         pts = fx["f%d_points" % k]
-        assert g.rebuild_topology(pts, float(fx["radius"])) == 0
-        g.update_atlas()
-        rc, ln = g.insert_points_subcell(pts, float(fx["R"]))
+        clr = fx["f%d_colours" % k] if ("f%d_colours" % k) in fx.files else None
+        if topo == "accumulate":
+            assert g.accumulate_topology(pts, float(fx["radius"])) == 0
+        elif topo == "rebuild" or k == 0:
+            assert g.rebuild_topology(pts, float(fx["radius"])) == 0
+        if topo != "fixed" or k == 0:
+            g.update_atlas()
+        rc, ln = g.insert_points_subcell(pts, float(fx["R"]), colours=clr)
+        cc = 1 if colour else -1
         if mode == "density":
-            g.gather_density(float(fx["rho"]))
+            g.gather_density(float(fx["rho"]), accum=accum, clr_chan=cc)
         else:
-            g.gather_levelset(float(fx["rho"]))
+            g.gather_levelset(float(fx["rho"]), accum=accum, clr_chan=cc)
         g.update_apron(0, float(fx["boundval"]))
+        if colour:
+            g.update_apron(1, 0.0)
         yield k, g, ln
+
+
+def rgba_bytes(u32):
+    return np.asarray(u32, dtype=np.uint32).view(np.uint8).astype(np.int16)
 
 
 @pytest.mark.skipif(not FIXTURES, reason="no golden fixtures")
@@ -61,14 +86,13 @@ def test_oracle_matches_reference_kernels(path):
         assert np.array_equal(cnt, ref_cnt[:len(cnt)]) and not ref_cnt[len(cnt):].any()
         h = membership_hash(off[:-1], cnt, pts)
         assert np.array_equal(h, fx[p + "sc_hash"][:len(h)])
-        b = g.atlas_bricks(0)
-        inner = b[:, 1:17, 1:17, 1:17].reshape(b.shape[0], -1)
-        m = np.ones((18, 18, 18), bool)
-        m[1:17, 1:17, 1:17] = False
-        lim = 1e-6 * 4096 + 1e-5 * np.abs(inner).sum(axis=1)
-        assert np.all(np.abs(inner.sum(axis=1) - fx[p + "slot_sum"]) <= lim), k
-        alim = 1e-6 * 1736 + 1e-5 * np.abs(b[:, m]).sum(axis=1)
-        assert np.all(np.abs(b[:, m].sum(axis=1) - fx[p + "apron_sum"]) <= alim), k
         ref_b = fx[p + "bricks"].astype(np.float64)
-        mine = b[:ref_b.shape[0]]
-        assert np.all(np.abs(mine - ref_b) <= 1e-6 + 1e-5 * np.abs(ref_b)), k
+        mine = g.atlas_bricks(0)
+        assert mine.shape == ref_b.shape, k
+        err = np.abs(mine - ref_b)
+        assert np.all(err <= 1e-6 + 1e-5 * np.abs(ref_b)), (k, float(err.max()))
+        if (p + "colour") in fx.files:
+            ref_c = rgba_bytes(fx[p + "colour"])
+            mine_c = rgba_bytes(g.atlas_bricks(1).astype(np.uint32))
+            d = np.abs(mine_c - ref_c)
+            assert d.max() <= 1, (k, int(d.max()), int((d > 0).sum()))
