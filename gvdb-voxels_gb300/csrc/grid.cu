@@ -16,7 +16,10 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
 #include "gbvdb.h"
+#include "host_topology.h"
 #include "kernels.h"
 
 using namespace gbvdb;
@@ -138,6 +141,11 @@ struct gbvdb_grid_s {
     // scratch
     DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     unsigned char* pinned = nullptr;
+
+    // ActivateSpace / RebuildTopologyCPU: host copies of the pools (fetched from the
+    // device at the first activation) that the next call reading the topology commits
+    std::unique_ptr<HostTopology> host;
+    bool host_dirty = false;
 
     // legacy InsertPoints: leaf and rank per point, points grouped by leaf
     DevBuf pnode, pndx, gcnt, goff, psort;
@@ -325,6 +333,84 @@ struct gbvdb_grid_s {
             cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
             stage_ms.push_back(ms);
         }
+    }
+
+    // ------------------------------------------- host topology (ActivateSpace)
+    // PoolFetchAll: host copies of the device pools for ActivateSpace to extend
+    void host_begin() {
+        if (host) return;
+        if (!configured) throw StatusError{GBVDB_INVALID_ARG, "Configure was not called"};
+        refresh_nused0();
+        sync();
+        host.reset(new HostTopology());
+        host->configure(levs, log2dim, range);
+        for (int l = 0; l < levs; l++) {
+            host->nodes[l].resize((size_t)ncnt[l]);
+            if (ncnt[l])
+                check(cudaMemcpy(host->nodes[l].data(), nodes[l].p, (size_t)ncnt[l] * sizeof(Node), cudaMemcpyDeviceToHost),
+                      "fetch nodes");
+            host->used[l] = (size_t)nused[l];
+            size_t lists = 0;
+            for (const Node& n : host->nodes[l])
+                if (n.childlist != kUndefL) lists = std::max(lists, (size_t)(n.childlist >> 16) + 1);
+            host->lists_used[l] = lists;
+            host->clist[l].resize(lists * (size_t)cl_len(l));
+            if (!host->clist[l].empty())
+                check(cudaMemcpy(host->clist[l].data(), clist[l].p, host->clist[l].size() * 8, cudaMemcpyDeviceToHost),
+                      "fetch child lists");
+        }
+        host->root = (root_lev >= 0 && ncnt[root_lev] > 0) ? elem(0, root_lev, 0) : HostTopology::kNone;
+    }
+
+    // PoolCommitAll of the host pools: they replace the device pools
+    void host_commit() {
+        if (!host_dirty) return;
+        host_dirty = false;
+        std::unique_ptr<HostTopology> h = std::move(host);
+        layout_changed();
+        const long long nl = (long long)h->nodes[0].size();
+        for (int l = 0; l < levs; l++) {
+            const long long n = (long long)h->nodes[l].size();
+            grow(nodes[l], (size_t)std::max(n, 1ll) * sizeof(Node));
+            if (l >= 1) grow(clist[l], (size_t)std::max(n, 1ll) * (size_t)cl_len(l) * 8);
+            if (n) check(cudaMemcpyAsync(nodes[l].p, h->nodes[l].data(), (size_t)n * sizeof(Node), cudaMemcpyHostToDevice,
+                                         stream), "commit nodes");
+            if (!h->clist[l].empty())
+                check(cudaMemcpyAsync(clist[l].p, h->clist[l].data(), h->clist[l].size() * 8, cudaMemcpyHostToDevice,
+                                      stream), "commit child lists");
+            if (l >= 1 && (long long)h->lists_used[l] < n)  // lists not taken yet read as empty
+                check(cudaMemsetAsync(ptr<unsigned long long>(clist[l]) + h->clist[l].size(), 0xFF,
+                                      ((size_t)n * (size_t)cl_len(l) - h->clist[l].size()) * 8, stream),
+                      "commit child lists");
+            ncnt[l] = n;
+            nused[l] = (long long)h->used[l];
+        }
+        sync();  // the host copies are released below
+        nused0_stale = false;
+        root_lev = -1;
+        if (h->root != HostTopology::kNone) {
+            root_lev = (int)((h->root >> 8) & 0xFF);
+            const Node& r = h->nodes[root_lev][(size_t)(h->root >> 16)];
+            for (int a = 0; a < 3; a++) root_pos[a] = r.pos[a];
+        }
+        last_depth = std::max(root_lev, 0);
+        // the dense leaf lookup covers every leaf's brick
+        lgdom_init = false;
+        for (long long i = 0; i < nl; i++) {
+            const Node& n = h->nodes[0][(size_t)i];
+            for (int a = 0; a < 3; a++) {
+                const int c = n.pos[a] >> lgrange[0];
+                lgdom_lo[a] = lgdom_init ? std::min(lgdom_lo[a], c) : c;
+                lgdom_hi[a] = lgdom_init ? std::max(lgdom_hi[a], c) : c;
+            }
+            lgdom_init = true;
+        }
+        build_leaf_grid();
+        nbr_count = -1;
+        ins_n = -1;
+        sc_valid = false;
+        lists_valid = false;
+        rebuild_topo = 1;  // a later RebuildTopology starts from an empty grid
     }
 
     // ------------------------------------------------------------ topology
@@ -1378,11 +1464,15 @@ struct gbvdb_grid_s {
 
 // ------------------------------------------------------------------ C ABI
 
-#define GBVDB_GUARD(g)                                    \
+#define GBVDB_GUARD_NOCOMMIT(g)                           \
     if (!(g)) return GBVDB_INVALID_ARG;                   \
     std::lock_guard<std::mutex> _lk((g)->mu);             \
     try {                                                 \
         cudaSetDevice((g)->device);
+// every other entry point first commits pending host activations (ActivateSpace)
+#define GBVDB_GUARD(g)                                    \
+    GBVDB_GUARD_NOCOMMIT(g)                               \
+        (g)->host_commit();
 #define GBVDB_END(g)                                      \
     }                                                     \
     catch (const StatusError& e) {                        \
@@ -1589,6 +1679,37 @@ gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off,
     g->pts.stride = stride;
     g->vel = vel;
     g->clr = ClrSrc{reinterpret_cast<const char*>(clr), clr ? clr_stride : 4, clr ? clr_off : 0};
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_activate_space(gbvdb_grid g, const float pos[3], uint64_t* out_node) {
+    GBVDB_GUARD_NOCOMMIT(g)
+    if (!pos) return GBVDB_INVALID_ARG;
+    g->host_begin();
+    const int32_t v[3] = {(int32_t)pos[0], (int32_t)pos[1], (int32_t)pos[2]};  // Vector3DI(Vector3DF) truncates
+    const uint64_t id = g->host->activate_space(v);
+    g->host_dirty = true;
+    if (out_node) *out_node = id;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_rebuild_topology_cpu(gbvdb_grid g, int64_t n, const float orig[3], const void* host_pos,
+                                        int stride) {
+    GBVDB_GUARD_NOCOMMIT(g)
+    if (n < 0 || (n > 0 && !host_pos) || (stride != 0 && stride < 12)) return GBVDB_INVALID_ARG;
+    if (stride == 0) stride = 12;
+    g->host_begin();
+    const float o[3] = {orig ? orig[0] : 0.0f, orig ? orig[1] : 0.0f, orig ? orig[2] : 0.0f};
+    const char* base = static_cast<const char*>(host_pos);
+    for (int64_t i = 0; i < n; i++) {
+        float p[3];
+        memcpy(p, base + i * (int64_t)stride, 12);
+        const int32_t v[3] = {(int32_t)(p[0] + o[0]), (int32_t)(p[1] + o[1]), (int32_t)(p[2] + o[2])};
+        g->host->activate_space(v);
+    }
+    g->host_dirty = true;
     return GBVDB_OK;
     GBVDB_END(g)
 }

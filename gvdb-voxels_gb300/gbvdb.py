@@ -41,7 +41,8 @@ EXPORTS = [
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
     "gbvdb_export_point_leaves", "gbvdb_checksum_device", "gbvdb_fill_channel4", "gbvdb_clear_channel",
-    "gbvdb_get_vol_bounds", "gbvdb_get_device_bytes", "gbvdb_get_vdb_info",
+    "gbvdb_get_vol_bounds", "gbvdb_get_device_bytes", "gbvdb_get_vdb_info", "gbvdb_activate_space",
+    "gbvdb_rebuild_topology_cpu",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -113,6 +114,8 @@ def load(path=LIB_PATH):
     L.gbvdb_get_vol_bounds.argtypes = [vp, fp]
     L.gbvdb_get_device_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_get_vdb_info.argtypes = [vp, vp, i64]
+    L.gbvdb_activate_space.argtypes = [vp, fp, ctypes.POINTER(ctypes.c_uint64)]
+    L.gbvdb_rebuild_topology_cpu.argtypes = [vp, i64, fp, vp, i32]
     L.gbvdb_get_depth.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gbvdb_get_node_counts.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_get_point_bounds.argtypes = [vp, fp]
@@ -253,6 +256,18 @@ class Grid:
     def accumulate_topology(self, n, radius, orig=(0, 0, 0), min_depth=1):
         return self._check(self.L.gbvdb_accumulate_topology(self._h, n, radius, _f3(orig), min_depth),
                            "accumulate_topology")
+
+    def activate_space(self, pos):
+        """ActivateSpace (host path): the existing leaf's Elem id, or 0xFFFFFFFF for a new leaf"""
+        out = ctypes.c_uint64(0)
+        self._check(self.L.gbvdb_activate_space(self._h, _f3(pos), ctypes.byref(out)), "activate_space")
+        return int(out.value)
+
+    def rebuild_topology_cpu(self, points, orig=(0, 0, 0)):
+        """RebuildTopologyCPU of host float32 (N, 3) positions"""
+        p = np.ascontiguousarray(points[:, :3], dtype=np.float32)
+        self._check(self.L.gbvdb_rebuild_topology_cpu(self._h, p.shape[0], _f3(orig), p.ctypes.data, 12),
+                    "rebuild_topology_cpu")
 
     def request_full_rebuild(self, tf=True):
         self._check(self.L.gbvdb_request_full_rebuild(self._h, 1 if tf else 0), "request_full_rebuild")

@@ -100,6 +100,18 @@ GBVDB_API gbvdb_status gbvdb_request_full_rebuild(gbvdb_grid g, int tf);
 GBVDB_API gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bounds);
 /* UpdateAtlas (gvdb_volume_gvdb.cpp:2630-2704) */
 GBVDB_API gbvdb_status gbvdb_update_atlas(gbvdb_grid g);
+/* ActivateSpace(Vector3DF pos) (gvdb_volume_gvdb.cpp:2766-2774, 2795-2855): the host topology
+ * path.  Activates the leaf holding the truncated position, creating the nodes above it and
+ * growing the root upwards (Reparent) as the reference does, on host copies of the pools
+ * (fetched from the device at the first activation).  *out_node (may be NULL) receives the
+ * leaf's Elem reference when it existed, else 0xFFFFFFFF (ID_UNDEFL).  Every other entry
+ * point first commits pending activations to the device pools (PoolCommitAll); a later
+ * RebuildTopology then starts from an empty grid. */
+GBVDB_API gbvdb_status gbvdb_activate_space(gbvdb_grid g, const float pos[3], uint64_t* out_node);
+/* RebuildTopologyCPU(num_pnts, orig, pos) (gvdb_volume_gvdb.cpp:1220-1227): ActivateSpace of
+ * pos[i] + orig for n HOST float3 positions, element i at host_pos + i*stride (0 = 12) */
+GBVDB_API gbvdb_status gbvdb_rebuild_topology_cpu(gbvdb_grid g, int64_t n, const float orig[3],
+                                                  const void* host_pos, int stride);
 
 /* --- points to voxels ---------------------------------------------------- */
 /* InsertPointsSubcell(subcell_size, num_pnts, radius, trans, &len) (gvdb_volume_gvdb.cpp:4971-5092);

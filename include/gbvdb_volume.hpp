@@ -30,6 +30,13 @@ struct Vector3DI {
     Vector3DI() : x(0), y(0), z(0) {}
     Vector3DI(int a, int b, int c) : x(a), y(b), z(c) {}
 };
+struct Vector4DF {
+    float x, y, z, w;
+    Vector4DF() : x(0), y(0), z(0), w(0) {}
+    Vector4DF(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
+};
+typedef int64_t slong;
+#define ID_UNDEFL 0xFFFFFFFF
 
 // the fields of the reference's DataPtr (gvdb_allocator.h:35-55) that SetPoints reads
 struct DataPtr {
@@ -40,7 +47,8 @@ struct DataPtr {
 };
 
 // channel types and filter constants of gvdb_types.h
-enum { T_UCHAR = GBVDB_T_UCHAR, T_FLOAT = GBVDB_T_FLOAT, T_HALF = GBVDB_T_HALF, T_BFLOAT16 = GBVDB_T_BFLOAT16 };
+enum { T_UCHAR = GBVDB_T_UCHAR, T_UCHAR4 = GBVDB_T_UCHAR4, T_FLOAT = GBVDB_T_FLOAT, T_HALF = GBVDB_T_HALF,
+       T_BFLOAT16 = GBVDB_T_BFLOAT16 };
 enum { F_NEAREST = 0, F_LINEAR = 1, F_MIDPOINT = 2 };
 enum { FUNC_SMOOTH = GBVDB_FUNC_SMOOTH };
 enum { F_CLAMP = 0, F_BORDER = 1, F_WRAP = 2 };
@@ -102,6 +110,18 @@ class VolumeGVDB {
         chk(gbvdb_finish_topology(g_, pCommitPool ? 1 : 0, pComputeBounds ? 1 : 0), "FinishTopology");
     }
     void UpdateAtlas() { chk(gbvdb_update_atlas(g_), "UpdateAtlas"); }
+    // the host topology path (VG.cpp:1220-1227, 2766-2774): ActivateSpace returns the existing
+    // leaf's id, or ID_UNDEFL for a new leaf; the next call that reads the topology commits
+    slong ActivateSpace(Vector3DF pos) {
+        float p[3] = {pos.x, pos.y, pos.z};
+        uint64_t id = ID_UNDEFL;
+        if (chk(gbvdb_activate_space(g_, p, &id), "ActivateSpace") != GBVDB_OK) return (slong)ID_UNDEFL;
+        return (slong)id;
+    }
+    void RebuildTopologyCPU(int pNumPnts, Vector3DF pOrig, Vector3DF* pPos) {
+        float o[3] = {pOrig.x, pOrig.y, pOrig.z};
+        chk(gbvdb_rebuild_topology_cpu(g_, pNumPnts, o, pPos, (int)sizeof(Vector3DF)), "RebuildTopologyCPU");
+    }
 
     // points to voxels (VG.cpp:4971-5092, 5318-5373)
     void InsertPointsSubcell(int subcell_size, int num_pnts, float pRadius, Vector3DF trans, int& pSCPntsLength) {
@@ -154,7 +174,12 @@ class VolumeGVDB {
         (void)changeCtx;
         chk(gbvdb_update_apron(g_, chan, boundval), "UpdateApron");
     }
+    void FillChannel(uchar chan, Vector4DF val) {
+        float v[4] = {val.x, val.y, val.z, val.w};
+        chk(gbvdb_fill_channel4(g_, chan, v), "FillChannel");
+    }
     void FillChannel(uchar chan, float value) { chk(gbvdb_fill_channel(g_, chan, value), "FillChannel"); }
+    void ClearChannel(uchar chan) { chk(gbvdb_clear_channel(g_, chan), "ClearChannel"); }
 
     // UpdateNeighbors / UpdateApronFaces / Compute(FUNC_SMOOTH) (VG.cpp:2527-2556, 4461-4496, 4532-4558)
     void UpdateNeighbors() { chk(gbvdb_update_neighbors(g_), "UpdateNeighbors"); }
@@ -189,6 +214,18 @@ class VolumeGVDB {
     Vector3DF getBoundMax() {
         float b[6] = {0, 0, 0, 0, 0, 0};
         gbvdb_get_point_bounds(g_, b);
+        return Vector3DF(b[3], b[4], b[5]);
+    }
+
+    // getVolMin / getVolMax (gvdb_volume_base.h:57-59): bounds of the last FinishTopology
+    Vector3DF getVolMin() {
+        float b[6] = {0, 0, 0, 0, 0, 0};
+        gbvdb_get_vol_bounds(g_, b);
+        return Vector3DF(b[0], b[1], b[2]);
+    }
+    Vector3DF getVolMax() {
+        float b[6] = {0, 0, 0, 0, 0, 0};
+        gbvdb_get_vol_bounds(g_, b);
         return Vector3DF(b[3], b[4], b[5]);
     }
 
