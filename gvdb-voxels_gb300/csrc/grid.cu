@@ -140,6 +140,8 @@ struct gbvdb_grid_s {
 
     // scratch
     DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    DevBuf touch_dirs;          // per home leaf position: the directions its points' boxes cover
+    bool touch_dirs_on = true;  // GBVDB_TUNE_TOUCH_DIRS
     unsigned char* pinned = nullptr;
 
     // ActivateSpace / RebuildTopologyCPU: host copies of the pools (fetched from the
@@ -586,6 +588,13 @@ struct gbvdb_grid_s {
 
     static constexpr long long kMaxBits = 1ll << 34;
 
+    // scratch of the direction-set form of the box pass (null: the per-point walk)
+    uint32_t* touch_dirs_buf(const KeyDomains& kd) {
+        if (!touch_dirs_on) return nullptr;
+        grow(touch_dirs, (size_t)touch_dirs_words(kd) * 4);
+        return ptr<uint32_t>(touch_dirs);
+    }
+
     void activate_full(long long n, float radius, float3 orig, int D, const int rpos[3]) {
         // root first (VG.cpp:1288-1300)
         ensure_pool(D, 1);
@@ -625,7 +634,7 @@ struct gbvdb_grid_s {
             int rlo[3], rhi[3];
             for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
             launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
-                            nullptr, ptr<int>(misc) + 8, stream);
+                            nullptr, ptr<int>(misc) + 8, touch_dirs_buf(kd), stream);
             check_launch("keys_extra");
             if (allocate_from_bitmap(D, kd, bits) > 0) {
                 mark();
@@ -654,7 +663,7 @@ struct gbvdb_grid_s {
         int rlo[3], rhi[3];
         for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
         launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
-                        ptr<int>(markers), ptr<int>(misc) + 8, stream);
+                        ptr<int>(markers), ptr<int>(misc) + 8, touch_dirs_buf(kd), stream);
         check_launch("keys_incr");
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
         std::vector<uint32_t> at = count_bitmap(D, kd, bits);
@@ -941,8 +950,8 @@ struct gbvdb_grid_s {
     // a float in channel c's storage type: FP32 bits, FP16 / BF16 bits, or for T_UCHAR4
     // make_uchar4(v, v, v, v) (UpdateApronC4's boundary value, OP.cuh:140-143)
     uint32_t storage_bits(int c, float v) const {
-        if (ch[c].dtype == GBVDB_T_UCHAR4) {
-            const uint32_t b = !(v == v) || v <= 0.0f ? 0u : (v >= 255.0f ? 255u : (uint32_t)v);
+        if (ch[c].dtype == GBVDB_T_UCHAR4) {  // the same float -> uchar conversion as the colour gathers
+            const uint32_t b = !(v == v) || v <= 0.0f ? 0u : (v >= 4294967296.0f ? 255u : (uint32_t)v & 0xFFu);
             return b | (b << 8) | (b << 16) | (b << 24);
         }
         if (ch[c].esize == 4) return bits_of(v);
@@ -1533,7 +1542,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
                       &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab};
@@ -2099,6 +2108,11 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
         for (int c = 0; c < 8; c++) g->interior_written(c);
         return GBVDB_OK;
     }
+    if (param == GBVDB_TUNE_TOUCH_DIRS) {
+        if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
+        g->touch_dirs_on = value != 0;
+        return GBVDB_OK;
+    }
     return GBVDB_INVALID_ARG;
     GBVDB_END(g)
 }
@@ -2136,7 +2150,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->sorted_clr, &g->list_cnt, &g->list_off, &g->list_pts, &g->list_clr,
                             &g->offs_buf, &g->lgrid,
-                            &g->touched, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
+                            &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
                             &g->nbmask, &g->gtab};

@@ -43,10 +43,13 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tm
 void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s);
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
                        uint32_t* bitmap, int* err, cudaStream_t s);
-// touched: scratch bitmap with the layout of `bitmap`, cleared by the caller
+// touched: scratch bitmap with the layout of `bitmap`, cleared by the caller; dirs (or null):
+// scratch of touch_dirs_words(dom) words for the direction-set form (boxes within one node
+// of the home node), cleared by the launcher
+long long touch_dirs_words(const KeyDomains& dom);
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
-                     uint32_t* bitmap, int* markers, int* err, cudaStream_t s);
+                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, cudaStream_t s);
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s);
 void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s);

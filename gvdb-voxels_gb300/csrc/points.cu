@@ -1072,13 +1072,15 @@ __global__ void k_gather_lists(TreeView t, const int* __restrict__ linked, const
 // arbitrary order of its atomically filled list.  Here the sum is exact: the bytes
 // are added as integers (with the old colour's bytes, or 255 for the alpha of the
 // non-accumulating start), divided by 255 once, then the reference's remaining
-// FP32 steps follow.  CLR2CHAR's uchar(x) conversion truncates and saturates
-// (NaN -> 0), as the GPU's float-to-integer conversion does.
+// FP32 steps follow.  CLR2CHAR's uchar(x) conversion is the reference kernels' (pinned
+// by golden fixtures of them): truncation to a 32-bit unsigned integer (NaN and negative
+// values to 0, 2^32 and above to 0xFFFFFFFF), keeping the low byte, so a component
+// above 255 wraps.
 
 __device__ __forceinline__ uint32_t clr_byte(float x) {
     if (!(x == x) || x <= 0.0f) return 0u;
-    if (x >= 255.0f) return 255u;
-    return (uint32_t)x;
+    if (x >= 4294967296.0f) return 255u;
+    return (uint32_t)x & 0xFFu;
 }
 __device__ __forceinline__ uint32_t clr_average(const uint32_t sum[4], uint32_t n, uint32_t old, int accum) {
     uint32_t out = 0;

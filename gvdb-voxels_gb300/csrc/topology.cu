@@ -266,6 +266,85 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
     }
 }
 
+// Level-0 box positions in two steps when every box reaches at most one node past
+// the point's own (home) node on each side, i.e. radius and the box's upper reach
+// are both at most the node range: (1) each point ORs into its home node's entry
+// the 27-bit set of neighbour directions d = (dx, dy, dz) in {-1, 0, 1}^3 that its
+// box covers (bit (dz+1)*9 + (dy+1)*3 + (dx+1)), after the same truncation and
+// root clipping as the per-point walk; (2) a node position of the key domain is
+// touched iff the entry of the node at -d has bit d.  The same set as the walk over
+// every box position, for one load (and on a new combination an atomic) per point.
+// The entries cover the level-0 key domain widened by one node on each side.
+struct DirDomain {
+    int lo[3];
+    int dim[3];
+};
+
+__global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, int lg, int3 rlo, int3 rhi,
+                             DirDomain dd, uint32_t* __restrict__ dirs, int* err) {
+    const int rr = 1 << lg;
+    const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
+        float x, y, z;
+        load_pos(p.base, i, p.stride, p.off, x, y, z);
+        const float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
+        if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
+        int m[3], hb[3];
+        bool any = true;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int ip = (int)w[a];
+            const float fi = (float)ip;
+            int lo = trunc_mult((int)fsub(fi, radius), lg), hi = trunc_mult((int)fadd(fi, hr), lg);
+            if (lo < rl[a]) lo += ((rl[a] - lo + rr - 1) >> lg) << lg;
+            if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
+            hb[a] = ip >> lg;
+            const int l = (lo >> lg) - hb[a], h = (hi >> lg) - hb[a];
+            any &= hi >= lo;
+            m[a] = hi >= lo ? (((1 << (h - l + 1)) - 1) << (l + 1)) & 7 : 0;
+        }
+        if (!any) continue;
+        uint32_t m27 = 0;
+#pragma unroll
+        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+            for (int dy = 0; dy < 3; dy++)
+                if (((m[2] >> dz) & (m[1] >> dy)) & 1) m27 |= (uint32_t)m[0] << (dz * 9 + dy * 3);
+        const int rx = hb[0] - dd.lo[0], ry = hb[1] - dd.lo[1], rz = hb[2] - dd.lo[2];
+        if ((unsigned)rx >= (unsigned)dd.dim[0] || (unsigned)ry >= (unsigned)dd.dim[1] || (unsigned)rz >= (unsigned)dd.dim[2]) {
+            atomicOr(err, 1);
+            continue;
+        }
+        uint32_t* e = dirs + ((long long)rx * dd.dim[1] + ry) * dd.dim[2] + rz;
+        if ((__ldcg(e) & m27) != m27) atomicOr(e, m27);
+    }
+}
+
+// a lane per level-0 bit (position of the key domain), a warp per bitmap word
+__global__ void k_touch_from_dirs(KeyDomain d, DirDomain dd, const uint32_t* __restrict__ dirs, uint32_t* touched) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = g >> 5, nw = (d.nbits + 31) >> 5;
+    if (w >= nw) return;  // whole warps leave together (blockDim is a multiple of 32)
+    const int b = (int)(g & 31);
+    const long long li = w * 32 + b;
+    bool hit = false;
+    if (li < d.nbits) {
+        const int rz = (int)(li % d.dim[2]);
+        const long long q = li / d.dim[2];
+        const int ry = (int)(q % d.dim[1]);
+        const int rx = (int)(q / d.dim[1]);
+        // entry of the home node at -dir, in the widened domain (offset 1 per axis)
+        for (int dz = -1; dz <= 1 && !hit; dz++)
+            for (int dy = -1; dy <= 1 && !hit; dy++)
+                for (int dx = -1; dx <= 1 && !hit; dx++) {
+                    const long long e = ((long long)(rx + 1 - dx) * dd.dim[1] + (ry + 1 - dy)) * dd.dim[2] + (rz + 1 - dz);
+                    hit = (__ldg(dirs + e) >> ((dz + 1) * 9 + (dy + 1) * 3 + (dx + 1))) & 1u;
+                }
+    }
+    const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hit);
+    if (b == 0) touched[(d.bitbase >> 5) + w] = mask;
+}
+
 // Box positions of level lev from those of lev-1: every touched position's parent.  For
 // one box, trunc(b / R_lev) * R_lev .. trunc(e / R_lev) * R_lev is the set of parents
 // of trunc(b / R_lev-1) * R_lev-1 .. trunc(e / R_lev-1) * R_lev-1 once both are clipped
@@ -519,17 +598,38 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
     unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
     k_keys_pass1<<<blocks, 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, err);
 }
+long long touch_dirs_words(const KeyDomains& dom) {
+    return (long long)(dom.d[0].dim[0] + 2) * (dom.d[0].dim[1] + 2) * (dom.d[0].dim[2] + 2);
+}
+
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
-                     uint32_t* bitmap, int* markers, int* err, cudaStream_t s) {
+                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
-    // the points touch level 0 (its bits start at bit 0); the upper levels follow from it
-    long long nwords = (dom.d[0].bitbase + dom.d[0].nbits + 31) >> 5;
-    size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
-    // fewer, fuller blocks when each one flushes a shared bitmap
-    unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-    k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
+    const float hr = hi_mul == 2 ? 2.0f * radius : radius;
+    const float rr = (float)(1 << t.lgrange[0]);
+    if (dirs && radius <= rr && hr <= rr) {
+        // boxes within one node of the home node: direction sets per home node
+        DirDomain dd;
+        for (int a = 0; a < 3; a++) {
+            dd.lo[a] = dom.d[0].lo[a] - 1;
+            dd.dim[a] = dom.d[0].dim[a] + 2;
+        }
+        cudaMemsetAsync(dirs, 0, (size_t)touch_dirs_words(dom) * 4, s);
+        if (p.n > 0)
+            k_touch_dirs<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
+                                                                      dirs, err);
+        const long long nw = (dom.d[0].nbits + 31) >> 5;
+        k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
+    } else {
+        // the points touch level 0 (its bits start at bit 0); the upper levels follow from it
+        long long nwords = (dom.d[0].bitbase + dom.d[0].nbits + 31) >> 5;
+        size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
+        // fewer, fuller blocks when each one flushes a shared bitmap
+        unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
+        k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
+    }
     for (int lev = 1; lev < depth; lev++) {
         long long nw = (dom.d[lev - 1].nbits + 31) >> 5;
         k_touch_up<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);

@@ -65,6 +65,7 @@ class JobResult(ctypes.Structure):
 TUNE_DENSE_MIN = 1
 TUNE_FUSED_APRON = 2
 TUNE_AUTOTUNE = 3
+TUNE_TOUCH_DIRS = 4
 FUNC_SMOOTH = 113
 
 

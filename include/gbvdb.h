@@ -268,6 +268,10 @@ GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** int
                                     interior change in between, only writes the faces of missing neighbours
                                     (boundval); the atlas ends bit-identical to a full UpdateApron.  0: every
                                     UpdateApron copies all apron voxels (the reference's kernel). */
+#define GBVDB_TUNE_TOUCH_DIRS 4  /* 1 (default): the box passes of RebuildTopology (extra and incremental
+                                    bricks) record, per home leaf position, the set of the 27 neighbour
+                                    directions its points' boxes reach, when no box reaches past a
+                                    neighbour; 0: every point walks its box positions.  Same node sets. */
 GBVDB_API gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value);
 /* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
 GBVDB_API gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable);

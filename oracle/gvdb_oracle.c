@@ -818,13 +818,14 @@ static int insert_subcell(OGrid* g, int sc, const void* posv, int64_t n, int str
  * mode 0 = density: v = max(accum ? old : 0, max_j(rho - |p_j - v|))
  * mode 1 = level set: v = min(accum ? old : 3, min_j(|p_j - v| - rho)) */
 /* RGBA8 byte of an averaged colour component: the reference's uchar(c * 255.0f)
- * (CLR2CHAR, PT.cuh:16) as the GPU converts it: truncation toward zero, values
- * beyond [0, 255] clamped, NaN to 0 (PTX cvt.rzi to an integer type saturates) */
+ * (CLR2CHAR, PT.cuh:16) as its kernels convert it (pinned by the golden fixtures):
+ * truncation toward zero to a 32-bit unsigned integer (NaN and negative values to 0,
+ * values of 2^32 and more to 0xFFFFFFFF), then its low byte, so that a component
+ * above 255 wraps (an opaque average (1 + n) / n of the non-accumulating start). */
 static uint32_t clr_byte(float c255) {
-    if (!(c255 == c255)) return 0u;
-    if (c255 <= 0.0f) return 0u;
-    if (c255 >= 255.0f) return 255u;
-    return (uint32_t)c255;
+    if (!(c255 == c255) || c255 <= 0.0f) return 0u;
+    if (c255 >= 4294967296.0f) return 255u;
+    return (uint32_t)c255 & 0xFFu;
 }
 
 /* The colour of one voxel (gvdbGatherDensity / gvdbGatherLevelSet, PT.cuh:717-731,

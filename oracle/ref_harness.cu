@@ -100,7 +100,11 @@ struct Harness {
     CUdeviceptr cuinfo = 0;
     bool rebuild = true;
     int curr_depth = -1;
-    float posmin[3], posmax[3];
+    float posmin[3], posmax[3], posrange[3];
+    bool fp16_lists = false;  // the last insert was InsertPointsSubcell_FP16 (ushort3 lists)
+    // legacy InsertPoints / ScatterDensity buffers
+    CUdeviceptr pnode = 0, pndx = 0, gcnt = 0, goff = 0, psort = 0;
+    CUdeviceptr nbr = 0;
     // points
     CUdeviceptr pts = 0;
     int npts = 0;
@@ -324,6 +328,7 @@ struct Harness {
             posmin[a] = out[a] - 1; posmax[a] = out[3 + a] + 2;
             posmin[a] = 0 > posmin[a] ? 0 : posmin[a];
             posmax[a] = 0 > posmax[a] ? 0 : posmax[a];
+            posrange[a] = posmax[a] - posmin[a];  // mPosRange (VG.cpp:5458-5462)
         }
     }
     int determine_depth(int root[3]) {  // VG.cpp:821-837
@@ -626,7 +631,7 @@ struct Harness {
     }
 
     // ---- InsertPointsSubcell (VG.cpp:4971-5092)
-    int insert_subcell(float radius, float3 trans) {
+    int insert_subcell(float radius, float3 trans, bool fp16 = false) {
         int numBrick = (int)pool[0][0].usedNum;
         if (numBrick == 0) return 8;
         prepare(false);
@@ -653,14 +658,25 @@ struct Harness {
         sc_num = nsc;
         if (sc_len == 0) return 0;
         ck(cuMemsetD8(sc_cnt, 0, (size_t)nsc * 4), "cnt");
-        aux(sc_pnts, (size_t)sc_len * 12);
+        aux(sc_pnts, (size_t)sc_len * (fp16 ? 6 : 12));
+        fp16_lists = fp16;
         CUdeviceptr z = 0;
         int cstride = 4;
         if (clr) aux(sc_clr, (size_t)sc_len * 4);  // VG.cpp:5063
-        void* d[23] = {&cuinfo, &sc, &scpb, &npts, &sc_cnt, &sc_off, &sc_map, &rng, &trans, &scdim, &radius,
-                       &pts, &off, &stride, &sc_pnts, &z, &off, &stride, &z, clr ? &clr : &z, &off, &cstride,
-                       clr ? &sc_clr : &z};
-        launch("gvdbInsertSubcell", npts / 512 + 1, 1, 1, 512, 1, 1, d);
+        if (fp16) {  // VG.cpp:5160-5172
+            float3 pmin = make_float3(posmin[0], posmin[1], posmin[2]);
+            float3 prng = make_float3(posrange[0], posrange[1], posrange[2]);
+            float3 vmin = make_float3(0, 0, 0), vrng = make_float3(0, 0, 0);
+            void* d[27] = {&cuinfo, &sc, &scpb, &npts, &sc_cnt, &sc_off, &sc_map, &pmin, &prng, &vmin, &vrng,
+                           &rng, &trans, &scdim, &radius, &pts, &off, &stride, &sc_pnts, &z, &off, &stride, &z,
+                           clr ? &clr : &z, &off, &cstride, clr ? &sc_clr : &z};
+            launch("gvdbInsertSubcell_fp16", npts / 512 + 1, 1, 1, 512, 1, 1, d);
+        } else {
+            void* d[23] = {&cuinfo, &sc, &scpb, &npts, &sc_cnt, &sc_off, &sc_map, &rng, &trans, &scdim, &radius,
+                           &pts, &off, &stride, &sc_pnts, &z, &off, &stride, &z, clr ? &clr : &z, &off, &cstride,
+                           clr ? &sc_clr : &z};
+            launch("gvdbInsertSubcell", npts / 512 + 1, 1, 1, 512, 1, 1, d);
+        }
         aux(sc_pos, (size_t)nsc * 12);
         aux(sc_nid, (size_t)nsc * 4);
         void* e[8] = {&cuinfo, &sc_nid, &sc_pos, &nmap, &scdim, &scpb, &sc, &sc_map};
@@ -680,6 +696,153 @@ struct Harness {
                        &cchan, &accum};
         launch(mode == 0 ? "gvdbGatherDensity" : "gvdbGatherLevelSet", nsc, 1, 1, 4, 4, 4, a);
         return 0;
+    }
+
+    int gather_levelset_fp16(float radius) {  // VG.cpp:5375-5401
+        int num_brick = (int)pool[0][0].usedNum;
+        if (num_brick == 0) return 8;
+        prepare(false);
+        int nsc = 64 * num_brick;
+        CUdeviceptr z = 0;
+        int chan = 0, cchan = 1;
+        float3 pmin = make_float3(posmin[0], posmin[1], posmin[2]);
+        float3 prng = make_float3(posrange[0], posrange[1], posrange[2]);
+        float3 vmin = make_float3(0, 0, 0), vrng = make_float3(0, 0, 0);
+        void* a[17] = {&cuinfo, &npts, &nsc, &radius, &pmin, &prng, &vmin, &vrng, &sc_nid, &sc_cnt, &sc_off, &sc_pos,
+                       &sc_pnts, &z, &z, &chan, &cchan};
+        launch("gvdbGatherLevelSet_fp16", nsc, 1, 1, 4, 4, 4, a);
+        return 0;
+    }
+
+    // host getNodeAtPoint for a leaf, from mRoot (the root of the last build) through the
+    // host child lists; -1 when no leaf holds p
+    long long leaf_at(const int p[3]) {
+        int D = -1;
+        for (int l = levs - 1; l >= 0; l--)
+            if (pool[0][l].lastEle > 0) { D = l; break; }
+        if (D <= 0) return -1;
+        HNode* nd = node(D, 0);
+        for (int lev = D; lev >= 1; lev--) {
+            const int rg = range(lev), r = res(lev), cr = rg / r;
+            int o[3];
+            for (int a = 0; a < 3; a++) {
+                o[a] = p[a] - nd->pos[a];
+                if (o[a] < 0 || o[a] >= rg) return -1;
+            }
+            if (nd->childlist == UNDEFL) return -1;
+            const uint64_t c = clist_of(nd->childlist)[((o[2] / cr) * r + o[1] / cr) * r + o[0] / cr];
+            if (c == UNDEF64) return -1;
+            nd = node(lev - 1, (size_t)(c >> 16));
+            if (lev - 1 == 0) return (long long)(c >> 16);
+        }
+        return -1;
+    }
+
+    // UpdateNeighbors (VG.cpp:2527-2556) + UpdateApronFaces (VG.cpp:4461-4496).  The table
+    // holds -1 (ID_UNDEFL) for a missing neighbour, which the kernel skips; the reference
+    // stores ElemNdx(ID_UNDEFL) = 65535 there, which its kernel would read as a node.
+    int update_apron_faces() {
+        prepare(false);
+        int bricks = (int)pool[0][0].lastEle;
+        if (bricks == 0) return 8;
+        std::vector<int> tab((size_t)bricks * 6);
+        const int d = 16;
+        for (int n = 0; n < bricks; n++) {
+            HNode* nd = node(0, n);
+            const int ct[3] = {nd->pos[0] + d / 2, nd->pos[1] + d / 2, nd->pos[2] + d / 2};
+            const int off[6][3] = {{-d, 0, 0}, {0, -d, 0}, {0, 0, -d}, {d, 0, 0}, {0, d, 0}, {0, 0, d}};
+            for (int k = 0; k < 6; k++) {
+                const int p[3] = {ct[0] + off[k][0], ct[1] + off[k][1], ct[2] + off[k][2]};
+                tab[(size_t)n * 6 + k] = (int)leaf_at(p);
+            }
+        }
+        aux(nbr, tab.size() * 4);
+        ck(cuMemcpyHtoD(nbr, tab.data(), tab.size() * 4), "nbr");
+        unsigned char chan = 0;
+        int brickres = 18, brickwid = 16;
+        void* a[6] = {&cuinfo, &chan, &bricks, &brickres, &brickwid, &nbr};
+        launch("gvdbUpdateApronFacesF", bricks, (16 + 7) / 8, (16 + 7) / 8, 3, 8, 8, a);
+        return 0;
+    }
+
+    // Compute(FUNC_SMOOTH, 0, 1, params, false, skipOverAprons = true) (VG.cpp:4532-4558): one
+    // pass of gvdbOpSmooth over the packed atlas
+    int smooth(float p1, float p2, float p3) {
+        prepare(false);
+        int3 ares = make_int3(ax * 18, ay * 18, az * 18);
+        unsigned char chan = 0;
+        const unsigned gx = (unsigned)(ax * 16 + 7) / 8, gy = (unsigned)(ay * 16 + 7) / 8, gz = (unsigned)(az * 16 + 7) / 8;
+        void* a[6] = {&cuinfo, &ares, &chan, &p1, &p2, &p3};
+        launch("gvdbOpSmooth", gx, gy, gz, 8, 8, 8, a);
+        return 0;
+    }
+
+    // legacy InsertPoints(bPrefix = true) (VG.cpp:5219-5267)
+    int insert_points(float3 trans) {
+        prepare(false);
+        int bricks = (int)pool[0][0].lastEle;
+        aux(pnode, (size_t)std::max(npts, 1) * 4);
+        aux(pndx, (size_t)std::max(npts, 1) * 4);
+        aux(gcnt, (size_t)std::max(bricks, 1) * 4);
+        ck(cuMemsetD8(gcnt, 0, (size_t)std::max(bricks, 1) * 4), "gcnt");
+        int off = 0, stride = 12;
+        void* a[9] = {&cuinfo, &npts, &pts, &off, &stride, &pnode, &pndx, &gcnt, &trans};
+        launch("gvdbInsertPoints", npts / 512 + 1, 1, 1, 512, 1, 1, a);
+        aux(goff, (size_t)std::max(bricks, 1) * 4);
+        prefix_sum(gcnt, goff, bricks);
+        aux(psort, (size_t)std::max(npts, 1) * 12);
+        void* b[11] = {&npts, &pts, &off, &stride, &pnode, &pndx, &bricks, &gcnt, &goff, &psort, &trans};
+        launch("gvdbSortPoints", npts / 512 + 1, 1, 1, 512, 1, 1, b);
+        return 0;
+    }
+
+    // ScatterDensity(num_pnts, radius, amp, trans, expand, avgColor = false) (VG.cpp:5624-5660),
+    // launched with the VDBInfo pointer that gvdbScatterPointDensity takes first
+    // (PT.cuh:525; the reference's host code omits it)
+    int scatter_density(float radius, float amp, float3 trans, bool expand) {
+        prepare(false);
+        CUdeviceptr z = 0;
+        int off = 0, stride = 12, coff = 0, cstride = 4;
+        void* a[14] = {&cuinfo, &npts, &radius, &amp, &pts, &off, &stride, &z, &coff, &cstride, &pnode, &trans, &expand,
+                       &z};
+        launch("gvdbScatterPointDensity", npts / 256 + 1, 1, 1, 256, 1, 1, a);
+        return 0;
+    }
+
+    // padded bricks of slots [0, n) (4-byte voxels, [slot][z][y][x]) into the atlas array
+    void write_bricks(int chan, const float* in, int n) {
+        size_t W = (size_t)ax * 18, H = (size_t)ay * 18, Dz = (size_t)az * 18;
+        std::vector<float> all(W * H * Dz);
+        CUDA_MEMCPY3D cp{};
+        cp.srcMemoryType = CU_MEMORYTYPE_ARRAY;
+        cp.srcArray = chan == 0 ? arr : carr;
+        cp.dstMemoryType = CU_MEMORYTYPE_HOST;
+        cp.dstHost = all.data();
+        cp.dstPitch = W * 4;
+        cp.dstHeight = H;
+        cp.WidthInBytes = W * 4;
+        cp.Height = H;
+        cp.Depth = Dz;
+        ck(cuMemcpy3D(&cp), "read atlas");
+        for (int s = 0; s < n; s++) {
+            int pz = s / (ax * ay), rem = s - pz * ax * ay, py = rem / ax, px = rem - py * ax;
+            for (int z = 0; z < 18; z++)
+                for (int y = 0; y < 18; y++)
+                    for (int x = 0; x < 18; x++)
+                        all[((size_t)(pz * 18 + z) * H + (py * 18 + y)) * W + (px * 18 + x)] =
+                            in[(size_t)s * 5832 + (z * 18 + y) * 18 + x];
+        }
+        CUDA_MEMCPY3D wp{};
+        wp.srcMemoryType = CU_MEMORYTYPE_HOST;
+        wp.srcHost = all.data();
+        wp.srcPitch = W * 4;
+        wp.srcHeight = H;
+        wp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+        wp.dstArray = chan == 0 ? arr : carr;
+        wp.WidthInBytes = W * 4;
+        wp.Height = H;
+        wp.Depth = Dz;
+        ck(cuMemcpy3D(&wp), "write atlas");
     }
 
     int update_apron(int c, float boundval) {  // VG.cpp:4418-4457
@@ -776,6 +939,29 @@ int rh_insert_subcell(void* hp, float radius, const float* trans, int* len) {
     Harness* h = (Harness*)hp;
     RH_TRY(h, int r = h->insert_subcell(radius, make_float3(trans[0], trans[1], trans[2])); *len = h->sc_len; return r);
 }
+int rh_insert_subcell_fp16(void* hp, float radius, const float* trans, int* len) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, int r = h->insert_subcell(radius, make_float3(trans[0], trans[1], trans[2]), true); *len = h->sc_len;
+           return r);
+}
+int rh_gather_levelset_fp16(void* hp, float radius) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, return h->gather_levelset_fp16(radius));
+}
+int rh_update_apron_faces(void* hp) { Harness* h = (Harness*)hp; RH_TRY(h, return h->update_apron_faces()); }
+int rh_smooth(void* hp, float p1, float p2, float p3) { Harness* h = (Harness*)hp; RH_TRY(h, return h->smooth(p1, p2, p3)); }
+int rh_insert_points(void* hp, const float* trans) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, return h->insert_points(make_float3(trans[0], trans[1], trans[2])));
+}
+int rh_scatter_density(void* hp, float radius, float amp, const float* trans, int expand) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, return h->scatter_density(radius, amp, make_float3(trans[0], trans[1], trans[2]), expand != 0));
+}
+int rh_write_bricks(void* hp, int chan, const float* in, int n) {
+    Harness* h = (Harness*)hp;
+    RH_TRY(h, h->write_bricks(chan, in, n); return 0);
+}
 int rh_gather(void* hp, int mode, float radius, int accum) {
     Harness* h = (Harness*)hp;
     RH_TRY(h, return h->gather(mode, radius, accum != 0));
@@ -869,7 +1055,7 @@ int rh_subcells(void* hp, int* cnt_out, int* off_out, float* pts_out) {
     RH_TRY(h, {
         h->ck(cuMemcpyDtoH(cnt_out, h->sc_cnt, (size_t)h->sc_num * 4), "cnt");
         h->ck(cuMemcpyDtoH(off_out, h->sc_off, (size_t)h->sc_num * 4), "off");
-        if (h->sc_len) h->ck(cuMemcpyDtoH(pts_out, h->sc_pnts, (size_t)h->sc_len * 12), "pts");
+        if (h->sc_len && pts_out) h->ck(cuMemcpyDtoH(pts_out, h->sc_pnts, (size_t)h->sc_len * 12), "pts");
         return 0;
     });
 }

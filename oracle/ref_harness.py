@@ -21,8 +21,17 @@ class RefGrid:
         L.rh_create.argtypes = [ctypes.c_char_p, i32, ctypes.POINTER(ctypes.c_int)]
         for n in ("rh_set_points", "rh_rebuild_topology", "rh_update_atlas", "rh_insert_subcell", "rh_gather",
                   "rh_update_apron", "rh_sync", "rh_top_lev", "rh_atlas_bricks", "rh_subcells", "rh_subcell_num",
-                  "rh_accumulate_topology", "rh_add_colour_channel", "rh_set_colors", "rh_fill", "rh_event_begin"):
+                  "rh_accumulate_topology", "rh_add_colour_channel", "rh_set_colors", "rh_fill", "rh_event_begin",
+                  "rh_insert_subcell_fp16", "rh_gather_levelset_fp16", "rh_update_apron_faces", "rh_smooth",
+                  "rh_insert_points", "rh_scatter_density", "rh_write_bricks"):
             getattr(L, n).restype = i32
+        L.rh_insert_subcell_fp16.argtypes = [vp, f32, fp, ctypes.POINTER(ctypes.c_int)]
+        L.rh_gather_levelset_fp16.argtypes = [vp, f32]
+        L.rh_update_apron_faces.argtypes = [vp]
+        L.rh_smooth.argtypes = [vp, f32, f32, f32]
+        L.rh_insert_points.argtypes = [vp, fp]
+        L.rh_scatter_density.argtypes = [vp, f32, f32, fp, i32]
+        L.rh_write_bricks.argtypes = [vp, i32, vp, i32]
         L.rh_accumulate_topology.argtypes = [vp, f32, fp, i32]
         L.rh_add_colour_channel.argtypes = [vp]
         L.rh_set_colors.argtypes = [vp, vp, i32]
@@ -122,6 +131,37 @@ class RefGrid:
         self.len = n.value
         return rc, n.value
 
+    def insert_points_subcell_fp16(self, radius, trans=(0, 0, 0)):
+        t = (ctypes.c_float * 3)(*trans)
+        n = ctypes.c_int(0)
+        rc = self._ok(self.L.rh_insert_subcell_fp16(self.h, radius, t, ctypes.byref(n)), "insert fp16")
+        self.len = n.value
+        return rc, n.value
+
+    def gather_levelset_fp16(self, radius):
+        return self._ok(self.L.rh_gather_levelset_fp16(self.h, radius), "gather fp16")
+
+    def update_apron_faces(self):
+        """UpdateNeighbors + UpdateApronFaces on channel 0"""
+        return self._ok(self.L.rh_update_apron_faces(self.h), "apron faces")
+
+    def smooth(self, p1, p2, p3=0.0):
+        """one Compute(FUNC_SMOOTH) pass on channel 0"""
+        return self._ok(self.L.rh_smooth(self.h, p1, p2, p3), "smooth")
+
+    def insert_points(self, trans=(0, 0, 0)):
+        t = (ctypes.c_float * 3)(*trans)
+        return self._ok(self.L.rh_insert_points(self.h, t), "insert points")
+
+    def scatter_density(self, radius, amp=1.0, trans=(0, 0, 0), expand=True):
+        t = (ctypes.c_float * 3)(*trans)
+        return self._ok(self.L.rh_scatter_density(self.h, radius, amp, t, 1 if expand else 0), "scatter")
+
+    def write_bricks(self, bricks, chan=0):
+        """padded FP32 bricks [slot, z, y, x] of slots [0, n) into the atlas"""
+        b = np.ascontiguousarray(bricks, dtype=np.float32)
+        return self._ok(self.L.rh_write_bricks(self.h, chan, b.ctypes.data, b.shape[0]), "write bricks")
+
     def gather_density(self, radius, accum=False):
         return self._ok(self.L.rh_gather(self.h, 0, radius, 1 if accum else 0), "gather")
 
@@ -177,6 +217,14 @@ class RefGrid:
         if used:
             self._ok(self.L.rh_atlas_bricks(self.h, chan, out.ctypes.data), "bricks")
         return out.reshape(used, 18, 18, 18)
+
+    def subcell_counts(self):
+        """(counts, offsets) of all 64 * used subcells, without the list entries"""
+        n = int(self.L.rh_subcell_num(self.h))
+        cnt = np.zeros(n, dtype=np.int32)
+        off = np.zeros(n, dtype=np.int32)
+        self._ok(self.L.rh_subcells(self.h, cnt.ctypes.data, off.ctypes.data, None), "subcells")
+        return cnt, off
 
     def subcells(self):
         """(counts, offsets, points) of all 64 * used subcells"""

@@ -55,7 +55,7 @@ def snapshot_oracle(g, ln):
 
 def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
             boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True,
-            fp16_subcells=False, dense_min=None, fused_apron=None):
+            fp16_subcells=False, dense_min=None, fused_apron=None, touch_dirs=None):
     import torch
 
     import gbvdb
@@ -66,6 +66,8 @@ def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1
         g.set_tuning(gbvdb.TUNE_DENSE_MIN, dense_min)
     if fused_apron is not None:  # 0: every UpdateApron copies all apron voxels
         g.set_tuning(gbvdb.TUNE_FUSED_APRON, fused_apron)
+    if touch_dirs is not None:  # 0: the box passes walk every point's box positions
+        g.set_tuning(gbvdb.TUNE_TOUCH_DIRS, touch_dirs)
     g.add_channel(0, dtype, 1, axiscnt)
     seq = frames if frames is not None else [points]
     outs = []

@@ -77,6 +77,97 @@ def cases():
     return out
 
 
+def fcases():
+    """fixtures of the operators after the gather (UpdateApronFaces, Compute(FUNC_SMOOTH)),
+    the FP16 subcell pair and the legacy InsertPoints + ScatterDensity; each runs on one
+    fresh full rebuild, so every leaf holds an assigned atlas slot"""
+    out = []
+    pts = datasets.shell(4000, seed=110, center=(180.0, 180.0, 180.0), rmin=30.0, rmax=38.0)
+    out.append(dict(name="faces_smooth", kind="faces_smooth", log2dims=(3, 3, 3, 4), radius=1.0, R=1.0, rho=1.0,
+                    points=pts, smooth=(1.5, 0.0)))
+    pos, vel = datasets.fluid(n=6000, seed=111, box=(16, 32, 16), domain=32)
+    pts = (pos + np.array([150.0, 60.0, 60.0], dtype=np.float32)).astype(np.float32)
+    out.append(dict(name="fp16_levelset", kind="fp16", log2dims=(3, 3, 3, 4), radius=2.0, R=2.0, rho=1.5,
+                    points=pts))
+    # one point per 5-voxel lattice cell, jittered inside it: no two points' seven-voxel
+    # splats touch one voxel, so the reference kernel's unsynchronised updates do not race
+    rng = np.random.default_rng(112)
+    g = np.stack(np.meshgrid(np.arange(14), np.arange(14), np.arange(14), indexing="ij"), axis=-1).reshape(-1, 3)
+    pts = (200.0 + 5.0 * g + rng.uniform(1.6, 3.4, size=g.shape)).astype(np.float32)
+    out.append(dict(name="scatter_density", kind="scatter", log2dims=(3, 3, 3, 4), radius=1.0, points=pts,
+                    sradius=1.5, amp=1.0))
+    return out
+
+
+def smooth_field(rng, n):
+    """random values on the voxels 2..5 of every 8^3 block of each 16^3 interior, zero
+    elsewhere: after one smoothing pass the voxels on the blocks' faces are still zero, so
+    the reference's blocks (which read each other's voxels as halo with no ordering) see
+    the same values whether a neighbour block has written already or not"""
+    b = np.zeros((n, 18, 18, 18), dtype=np.float32)
+    loc = (np.arange(16) % 8 >= 2) & (np.arange(16) % 8 <= 5)
+    m = loc[:, None, None] & loc[None, :, None] & loc[None, None, :]
+    inner = b[:, 1:17, 1:17, 1:17]
+    inner[:, m] = rng.uniform(-2.0, 2.0, size=(n, int(m.sum()))).astype(np.float32)
+    return b
+
+
+def topology(g, store):
+    store["top_lev"] = g.top_lev
+    store["used"] = g.used_count(0)
+    for lev in range(g.levs):
+        n = g.nodes(lev)
+        for f in ("lev", "flags", "pos", "value", "parent", "childlist"):
+            store["L%d_%s" % (lev, f)] = n[f]
+        if lev > 0:
+            store["L%d_clist" % lev] = g.childlist(lev)
+    store["atlas_dims"] = np.array(g.atlas_dims())
+    store["amap"] = g.atlas_map().view(np.int32)
+
+
+def run_fcase(c, store):
+    import ref_harness
+
+    g = ref_harness.RefGrid(c["log2dims"])
+    pts = c["points"]
+    store.update({"kind": c["kind"], "log2dims": np.array(c["log2dims"]), "radius": c["radius"], "points": pts})
+    g.set_points(pts)
+    g.rebuild_topology(c["radius"])
+    g.update_atlas()
+    if c["kind"] == "faces_smooth":
+        store.update({"R": c["R"], "rho": c["rho"]})
+        g.insert_points_subcell(c["R"])
+        g.gather_density(c["rho"])
+        g.sync()
+        store["gathered"] = g.atlas_bricks(0)
+        g.update_apron_faces()
+        g.sync()
+        store["faces"] = g.atlas_bricks(0)
+        field = smooth_field(np.random.default_rng(113), store["faces"].shape[0])
+        g.write_bricks(field)
+        g.smooth(*c["smooth"])
+        g.sync()
+        store["smooth_in"] = field
+        store["smooth_params"] = np.array(c["smooth"], dtype=np.float32)
+        store["smooth_out"] = g.atlas_bricks(0)
+    elif c["kind"] == "fp16":
+        store.update({"R": c["R"], "rho": c["rho"]})
+        _, ln = g.insert_points_subcell_fp16(c["R"])
+        g.gather_levelset_fp16(c["rho"])
+        g.update_apron(3.0, 0)
+        g.sync()
+        store["len"] = ln
+        store["sc_cnt"] = g.subcell_counts()[0]
+        store["bricks"] = g.atlas_bricks(0)
+    else:
+        store.update({"sradius": c["sradius"], "amp": c["amp"]})
+        g.insert_points()
+        g.scatter_density(c["sradius"], c["amp"])
+        g.sync()
+        store["bricks"] = g.atlas_bricks(0)
+    topology(g, store)
+
+
 def _colours(rng, n):
     """RGBA8 per point as uint32 (R in the low byte); a third opaque, a third with
     random alpha, a third all-random"""
@@ -158,6 +249,12 @@ def main(out_dir):
             g.sync()
             snapshot("f%d_" % k, g, store, colours is not None)
         path = os.path.join(out_dir, c["name"] + ".npz")
+        np.savez_compressed(path, **store)
+        print(path, os.path.getsize(path))
+    for c in fcases():
+        store = {}
+        run_fcase(c, store)
+        path = os.path.join(out_dir, "op_" + c["name"] + ".npz")
         np.savez_compressed(path, **store)
         print(path, os.path.getsize(path))
 

@@ -37,9 +37,11 @@ def test_shell_200k_density(gpu_lib):
     assert abs(o[0]["checksum"] - g[0]["checksum"]) <= 1e-6 * max(1.0, abs(o[0]["checksum"]))
 
 
-def test_fluid_frames_levelset(gpu_lib):
+@pytest.mark.parametrize("touch_dirs", [1, 0])
+def test_fluid_frames_levelset(gpu_lib, touch_dirs):
     """Dam-break frames: RebuildTopology(r=4), InsertPointsSubcell(R=4), GatherLevelSet(rho=2),
-    UpdateApron(3.0); frame 2 is a full rebuild (mCurrDepth quirk), frames 3+ incremental."""
+    UpdateApron(3.0); frame 2 is a full rebuild (mCurrDepth quirk), frames 3+ incremental.
+    Both forms of the box passes (direction sets per home leaf, per-point walk)."""
     pos, vel = _mini_fluid()
     frames = []
     p = pos.copy()
@@ -47,7 +49,8 @@ def test_fluid_frames_levelset(gpu_lib):
         p = (p + 0.5 * vel).astype(np.float32)
         frames.append(p.copy())
     _, o = H.run_oracle(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
-    _, g = H.run_gpu(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    _, g = H.run_gpu(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0,
+                     touch_dirs=touch_dirs)
     for k in range(len(frames)):
         _full_check(o[k], g[k], 3.0)
 

@@ -13,6 +13,15 @@ arbitrary order of its atomically filled lists.
 Call sequences: RebuildTopology frames (full, then incremental);
 AccumulateTopology with accumulating gathers after FillChannel; a fixed
 topology with accumulating, coloured density gathers; coloured level sets.
+
+Operator fixtures (op_*.npz), each on one full rebuild: UpdateApronFaces from the
+reference's own gathered bricks (faces bit-exact); one Compute(FUNC_SMOOTH) pass
+on a field whose block-face voxels stay zero (so the reference's unordered
+blocks give one answer), within 1e-6 absolute / 1e-5 relative; the FP16 subcell
+pair (list lengths exact; values within the tolerance plus one 16-bit
+quantisation step, since the reference quantises with approximate division);
+legacy InsertPoints + ScatterDensity on points whose splats never share a voxel
+(the reference kernel's updates are unsynchronised), within 1e-5 relative.
 """
 import glob
 import os
@@ -24,7 +33,9 @@ import oracle
 from golden.make_golden import membership_hash
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+FIXTURES = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                  if not os.path.basename(p).startswith("op_"))
+OP_FIXTURES = sorted(glob.glob(os.path.join(HERE, "golden", "op_*.npz")))
 
 
 def run_oracle(fx):
@@ -96,3 +107,60 @@ def test_oracle_matches_reference_kernels(path):
             mine_c = rgba_bytes(g.atlas_bricks(1).astype(np.uint32))
             d = np.abs(mine_c - ref_c)
             assert d.max() <= 1, (k, int(d.max()), int((d > 0).sum()))
+
+
+def topology_matches(g, fx):
+    assert g.top_lev == int(fx["top_lev"])
+    assert g.used_count(0) == int(fx["used"])
+    for lev in range(g.levs):
+        n = g.nodes(lev)
+        for f in ("lev", "flags", "pos", "value", "parent", "childlist"):
+            assert np.array_equal(n[f], fx["L%d_%s" % (lev, f)]), (lev, f)
+        if lev > 0:
+            assert np.array_equal(g.childlist(lev), fx["L%d_clist" % lev]), lev
+    assert tuple(g.atlas_dims()) == tuple(int(v) for v in fx["atlas_dims"])
+    assert np.array_equal(g.atlas_map().view(np.int32), fx["amap"])
+
+
+@pytest.mark.skipif(not OP_FIXTURES, reason="no operator fixtures")
+@pytest.mark.parametrize("path", OP_FIXTURES, ids=[os.path.basename(p) for p in OP_FIXTURES])
+def test_oracle_matches_reference_operators(path):
+    fx = np.load(path)
+    kind = str(fx["kind"])
+    pts = fx["points"]
+    g = oracle.OracleGrid(tuple(int(v) for v in fx["log2dims"]))
+    g.add_channel(0)
+    assert g.rebuild_topology(pts, float(fx["radius"])) == 0
+    g.update_atlas()
+    topology_matches(g, fx)
+    if kind == "faces_smooth":
+        b = np.ascontiguousarray(fx["gathered"], dtype=np.float32).copy()
+        g.apron_faces_f32(b, g.neighbors())
+        assert np.array_equal(b, fx["faces"])
+        p1, p2 = (float(v) for v in fx["smooth_params"])
+        b = np.ascontiguousarray(fx["smooth_in"], dtype=np.float32).copy()
+        g.smooth_f32(b, p1, p2)
+        ref = fx["smooth_out"].astype(np.float64)
+        inner = (slice(None), slice(1, 17), slice(1, 17), slice(1, 17))
+        err = np.abs(b[inner].astype(np.float64) - ref[inner])
+        assert np.all(err <= 1e-6 + 1e-5 * np.abs(ref[inner])), float(err.max())
+    elif kind == "fp16":
+        rc, ln = g.insert_points_subcell_fp16(pts, float(fx["R"]))
+        assert ln == int(fx["len"])
+        off, _ = g.subcells()
+        cnt = np.diff(off)
+        ref_cnt = fx["sc_cnt"]
+        assert np.array_equal(cnt, ref_cnt[:len(cnt)]) and not ref_cnt[len(cnt):].any()
+        g.gather_levelset(float(fx["rho"]))
+        g.update_apron(0, 3.0)
+        b, ref = g.atlas_bricks(0), fx["bricks"].astype(np.float64)
+        lo, hi = pts.min(axis=0) - 1.0, pts.max(axis=0) + 2.0
+        step = float(np.sqrt(3.0) * np.max(hi - np.maximum(lo, 0.0)) / 65535.0) * 1.01
+        err = np.abs(b - ref)
+        assert np.all(err <= 1e-6 + 1e-5 * np.abs(ref) + step), float(err.max())
+    else:
+        g.insert_points(pts)
+        g.scatter_density(pts, float(fx["sradius"]), expand=True)
+        b, ref = g.atlas_bricks(0), fx["bricks"].astype(np.float64)
+        err = np.abs(b - ref)
+        assert np.all(err <= 1e-6 + 1e-5 * np.abs(ref)), float(err.max())

@@ -5,8 +5,8 @@ or a serving loop working inside a fixed memory budget).
 Checked through the C ABI on two calls in a row that share its static scratch
 array: each result equals gbvdb_checksum's bit for bit (both run the same
 kernels in the same fixed order) and the oracle's FP64 sum within the parity
-tolerance; the grid's device byte total and torch's allocator are unchanged by
-the calls; a grid with more atlas slots than the static array holds is refused
+tolerance; the grid's device byte total is unchanged by the calls and torch's
+allocator holds no more than before them; a grid with more atlas slots than the static array holds is refused
 with GBVDB_CAPACITY.  This file sorts last so that a run stopping at the first
 failure has already run every other test."""
 import ctypes
@@ -73,7 +73,7 @@ def test_checksum_noalloc_matches_checksum_twice(gpu_lib):
         st, got = _noalloc(g, out)
         assert st == gbvdb.OK, g.L.gbvdb_last_error(g._h)
         assert g.device_bytes() == bytes_before
-        assert torch.cuda.memory_allocated() == torch_before
+        assert torch.cuda.memory_allocated() <= torch_before
         assert got == ref, (got, ref)
         exact = og.checksum(0)
         assert abs(got - exact) <= 1e-6 + 1e-5 * abs(exact), (got, exact)
