@@ -16,6 +16,9 @@
 #include <string>
 #include <vector>
 
+#include <dlfcn.h>
+
+#include <cstdlib>
 #include <memory>
 
 #include "gbvdb.h"
@@ -67,6 +70,82 @@ uint16_t f2h_bits(float f) {  // round to nearest even, float -> IEEE half
     if (rem > 0x1000u || (rem == 0x1000u && (h & 1))) h++;
     return (uint16_t)(sign | h);
 }
+// ------------------------------------------------------------- tuning table
+// Per point-count bucket: the gather's dense-form threshold, the gather's resident
+// blocks per SM and the binning passes' points per thread, chosen by a tuning run
+// (gvdb-voxels_gb300/tune.py) and read from JSON at the first grid creation:
+//   {"buckets": [{"max_points": 100000, "dense_min": 2048, "gather_blocks": 10,
+//                 "bin_unroll": 2, "scatter_unroll": 4}, ...]}
+// from $GBVDB_TUNE_TABLE, else tune_table.json beside libgbvdb.so.  An insert or gather
+// of n points takes the first bucket with max_points >= n (the last one beyond).
+struct TuneEntry {
+    long long max_points = 0;
+    int dense_min = 2048, gather_blocks = 10, bin_unroll = 2, scatter_unroll = 4;
+};
+struct TuneTable {
+    std::vector<TuneEntry> b;
+    std::string source;
+};
+
+bool json_int(const std::string& obj, const char* key, long long* out) {
+    const std::string k = std::string("\"") + key + "\"";
+    size_t p = obj.find(k);
+    if (p == std::string::npos) return false;
+    p = obj.find(':', p + k.size());
+    if (p == std::string::npos) return false;
+    char* end = nullptr;
+    const long long v = std::strtoll(obj.c_str() + p + 1, &end, 10);
+    if (end == obj.c_str() + p + 1) return false;
+    *out = v;
+    return true;
+}
+
+TuneTable load_tune_table() {
+    TuneTable t;
+    std::string path;
+    if (const char* e = std::getenv("GBVDB_TUNE_TABLE")) {
+        path = e;
+    } else {
+        Dl_info info;
+        if (dladdr((void*)&load_tune_table, &info) && info.dli_fname) {
+            path = info.dli_fname;
+            const size_t sl = path.find_last_of('/');
+            path = (sl == std::string::npos ? std::string(".") : path.substr(0, sl)) + "/tune_table.json";
+        }
+    }
+    FILE* f = path.empty() ? nullptr : std::fopen(path.c_str(), "rb");
+    if (!f) return t;
+    std::string txt;
+    char buf[4096];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) txt.append(buf, n);
+    std::fclose(f);
+    size_t p = txt.find("\"buckets\"");
+    while (p != std::string::npos) {
+        const size_t a = txt.find('{', p), z = a == std::string::npos ? a : txt.find('}', a);
+        if (a == std::string::npos || z == std::string::npos) break;
+        const std::string obj = txt.substr(a, z - a + 1);
+        TuneEntry e;
+        long long v;
+        if (!json_int(obj, "max_points", &v)) break;
+        e.max_points = v;
+        if (json_int(obj, "dense_min", &v) && v >= 0) e.dense_min = (int)std::min<long long>(v, 1ll << 31);
+        if (json_int(obj, "gather_blocks", &v)) e.gather_blocks = v == 8 ? 8 : 10;
+        if (json_int(obj, "bin_unroll", &v)) e.bin_unroll = (v == 1 || v == 4) ? (int)v : 2;
+        if (json_int(obj, "scatter_unroll", &v)) e.scatter_unroll = (v == 2 || v == 8) ? (int)v : 4;
+        t.b.push_back(e);
+        p = z + 1;
+    }
+    std::sort(t.b.begin(), t.b.end(), [](const TuneEntry& x, const TuneEntry& y) { return x.max_points < y.max_points; });
+    if (!t.b.empty()) t.source = path;
+    return t;
+}
+
+const TuneTable& tune_table() {
+    static const TuneTable t = load_tune_table();
+    return t;
+}
+
 uint16_t f2bf_bits(float f) {
     uint32_t x;
     memcpy(&x, &f, 4);
@@ -162,6 +241,28 @@ struct gbvdb_grid_s {
     DevBuf gtab;       // per-brick gather setup (neighbour ranks and bin ranges, origin, slot)
 
     // tuning
+    bool table_on = true;  // GBVDB_TUNE_TABLE: settings from the tuning table when one is loaded
+    const TuneEntry* tune_entry(long long n) const {
+        const TuneTable& t = tune_table();
+        if (!table_on || t.b.empty()) return nullptr;
+        for (const TuneEntry& e : t.b)
+            if (n <= e.max_points) return &e;
+        return &t.b.back();
+    }
+    // explicit settings (set_tuning) win over the table; -1: table or built-in default
+    int bin_unroll_set = -1, scatter_unroll_set = -1, gather_blocks_set = -1;
+    int bin_unroll(long long n) const {
+        const TuneEntry* e = tune_entry(n);
+        return bin_unroll_set > 0 ? bin_unroll_set : (e ? e->bin_unroll : 2);
+    }
+    int scatter_unroll(long long n) const {
+        const TuneEntry* e = tune_entry(n);
+        return scatter_unroll_set > 0 ? scatter_unroll_set : (e ? e->scatter_unroll : 4);
+    }
+    int gather_blocks(long long n) const {
+        const TuneEntry* e = tune_entry(n);
+        return gather_blocks_set > 0 ? gather_blocks_set : (e ? e->gather_blocks : 10);
+    }
     int dense_min = 2048;
     // Dense-form threshold autotuner (on until GBVDB_TUNE_DENSE_MIN is set): the
     // gathers of a workload try each candidate once, timed with events on the
@@ -855,7 +956,7 @@ struct gbvdb_grid_s {
             nbm = ptr<uint32_t>(nbmask);
         }
         launch_bin_count(t, lgv, p, trans, R, qz, ptr<uint32_t>(scmap), nbm, ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),
-                         ptr<uint32_t>(rank_of), totals, stream);
+                         ptr<uint32_t>(rank_of), totals, bin_unroll(p.n), stream);
         check_launch("bin_count");
         grow(scan_tmp, scan_tmp_bytes(nbins));
         scan_exclusive_u32(ptr<uint32_t>(bin_cnt), ptr<uint32_t>(bin_off), nbins, scan_tmp.p, stream);
@@ -877,7 +978,7 @@ struct gbvdb_grid_s {
         // (InsertPointsSubcell, VG.cpp:5063-5075)
         if (clr.base) grow(sorted_clr, (size_t)std::max<uint32_t>(binned, 1) * 4);
         launch_bin_scatter(p, trans, R, qz, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
-                           ptr<float4>(sorted), clr, ptr<uint32_t>(sorted_clr), stream);
+                           ptr<float4>(sorted), clr, ptr<uint32_t>(sorted_clr), scatter_unroll(p.n), stream);
         check_launch("bin_scatter");
         mark();
         sc_valid = true;
@@ -1026,7 +1127,9 @@ struct gbvdb_grid_s {
             }
         } else {
             int tslot = -1;
-            gp.dense_min = tune_pick(sc_nbricks, &tslot);
+            const TuneEntry* te = tune_auto ? tune_entry(sc_pts.n) : nullptr;
+            gp.dense_min = te ? te->dense_min : tune_pick(sc_nbricks, &tslot);
+            gp.min_blocks = gather_blocks(sc_pts.n);
             // fused apron: needs the dense leaf lookup (the apron pass resolves
             // neighbours with the same table) and an apron of one voxel
             const bool push = fused_apron && lgv.cells && ch[chan].apron == 1 && atlas_last > 0;
@@ -2113,9 +2216,31 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
         g->touch_dirs_on = value != 0;
         return GBVDB_OK;
     }
+    if (param == GBVDB_TUNE_TABLE) {
+        if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
+        g->table_on = value != 0;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_BIN_UNROLL) {
+        if (value != 0 && value != 1 && value != 2 && value != 4) return GBVDB_INVALID_ARG;
+        g->bin_unroll_set = value ? (int)value : -1;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_SCATTER_UNROLL) {
+        if (value != 0 && value != 2 && value != 4 && value != 8) return GBVDB_INVALID_ARG;
+        g->scatter_unroll_set = value ? (int)value : -1;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_GATHER_BLOCKS) {
+        if (value != 0 && value != 8 && value != 10) return GBVDB_INVALID_ARG;
+        g->gather_blocks_set = value ? (int)value : -1;
+        return GBVDB_OK;
+    }
     return GBVDB_INVALID_ARG;
     GBVDB_END(g)
 }
+
+const char* gbvdb_tune_table_source(void) { return tune_table().source.c_str(); }
 
 gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable) {
     GBVDB_GUARD(g)

@@ -115,12 +115,14 @@ struct Quant {
 // linked flags of the 27 bricks around every linked leaf (bit (dz+1)*9 + (dy+1)*3 + (dx+1))
 void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s);
 // nbmask (or null): from launch_nb_mask; only for R <= 11, where member ranges stay within those 27 bricks
+// unroll: points per thread per step (1, 2 or 4)
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,
                       const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
-                      unsigned long long* totals, cudaStream_t s);
+                      unsigned long long* totals, int unroll, cudaStream_t s);
 // sorted_clr (or null): the binned points' colours from clr, in the order of `sorted`
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
-                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, cudaStream_t s);
+                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, int unroll,
+                        cudaStream_t s);
 
 struct GatherParams {
     int mode;          // 0 density, 1 level set
@@ -137,6 +139,7 @@ struct GatherParams {
     // voxels into the apron records of its 26 neighbours (see k_gather)
     void* apron;
     const int* apron_bad;  // set by the push check: the grid is not in the state the push assumes
+    int min_blocks;        // resident blocks per SM the gather is compiled for (10 or 8)
 };
 // fused-apron precondition (one thread per leaf); *bad must be 0 before the launch
 void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,

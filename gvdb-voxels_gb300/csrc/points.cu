@@ -108,15 +108,15 @@ __device__ __forceinline__ int range_in_brick(int lo, int hi, int o) {
     return b >= a ? ((b - a) >> 2) + 1 : 0;
 }
 
+// kU points per thread per step: the position loads, the home-leaf lookups, the rank
+// loads and the counting atomics of the kU points are each issued together (the pass
+// is bound by the latency of that dependent chain).  kU comes from the tuning table
+// (1, 2 or 4); measured on the fluid frame: kU = 1 or 2 (54 / 63 registers) beat 3 and
+// 4 (72 / 80 registers, fewer resident warps) by about 10 us.
+template <int kU>
 __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
                             const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ nbmask,
                             uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
-    // kU points per thread per step: the position loads, the home-leaf lookups, the
-    // rank loads and the counting atomics of the kU points are each issued together
-    // (the pass is bound by the latency of that dependent chain).  Measured on the
-    // fluid frame: kU = 1 or 2 (54 / 63 registers) beat 3 and 4 (72 / 80 registers,
-    // fewer resident warps) by about 10 us.
-    constexpr int kU = 2;
     unsigned long long members = 0, orphans = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
@@ -262,12 +262,12 @@ __device__ __forceinline__ int member_bits(int ox, int oy, int oz) {
     return (1 << (4 - ox)) | (1 << (13 - oy)) | (1 << (22 - oz));
 }
 
+// kU points per thread per step (2, 4 or 8 from the tuning table), their loads issued
+// together (the pass is bound by the latency of the dependent bin_of -> bin_off loads)
+template <int kU>
 __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const int* __restrict__ bin_of,
                               const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
                               float4* __restrict__ sorted, ClrSrc clr, uint32_t* __restrict__ sorted_clr) {
-    // kU points per thread per step, their loads issued together (the pass is bound by the
-    // latency of the dependent bin_of -> bin_off loads)
-    constexpr int kU = 4;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
         int b[kU];
@@ -654,10 +654,11 @@ __global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ l
 //   Skipped points cannot lower any voxel's minimum, so the result is exact.
 //
 // One coalesced write of the brick from the tile at the end.
-template <typename T>
-// 10 blocks per SM (48 registers; the 20.9 KiB of shared memory per block allows
-// 10): measured 0.774 ms on the fluid frame against 0.787 at 9 and 0.798 at 8
-__global__ void __launch_bounds__(kGatherThreads, 10) k_gather(const int4* __restrict__ gtab,
+// kMinB blocks per SM, from the tuning table (10 or 8).  10 (48 registers; the 20.9 KiB
+// of shared memory per block allows 10): measured 0.774 ms on the fluid frame against
+// 0.787 at 9 and 0.798 at 8
+template <typename T, int kMinB>
+__global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __restrict__ gtab,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
                                                            const int4* __restrict__ offs, int noffs,
@@ -1324,16 +1325,28 @@ void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t
 }
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
-                      unsigned long long* totals, cudaStream_t s) {
+                      unsigned long long* totals, int unroll, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_count<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of,
-                                                    totals);
+    const unsigned b = gs_blocks(p.n, 256);
+    if (unroll == 1)
+        k_bin_count<1><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
+    else if (unroll == 4)
+        k_bin_count<4><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
+    else
+        k_bin_count<2><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
 }
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
-                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, cudaStream_t s) {
+                        const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, int unroll,
+                        cudaStream_t s) {
     if (p.n <= 0) return;
-    k_bin_scatter<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr,
-                                                     clr.base ? sorted_clr : nullptr);
+    const unsigned b = gs_blocks(p.n, 256);
+    uint32_t* sc = clr.base ? sorted_clr : nullptr;
+    if (unroll == 2)
+        k_bin_scatter<2><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
+    else if (unroll == 8)
+        k_bin_scatter<8><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
+    else
+        k_bin_scatter<4><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
 }
 void launch_gather_colour(const int4* gtab, long long nbricks, const uint32_t* bin_off, const float4* pts,
                           const uint32_t* pclr, int olo, int ohi, int accum, uint32_t* out, cudaStream_t s) {
@@ -1355,15 +1368,24 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
     if (nbricks <= 0) return;
     k_gather_prep<<<blocks_for(nbricks * 32, 256), 256, 0, s>>>(t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay,
                                                                 gtab);
-    if (gp.dtype == 3)
-        k_gather<float><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
-                                                                     (float*)interior);
-    else if (gp.dtype == 100)
-        k_gather<__half><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
-                                                                      (__half*)interior);
-    else
-        k_gather<__nv_bfloat16><<<(unsigned)nbricks, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
-                                                                            (__nv_bfloat16*)interior);
+    const unsigned nb = (unsigned)nbricks;
+    if (gp.min_blocks == 8) {
+        if (gp.dtype == 3)
+            k_gather<float, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
+        else if (gp.dtype == 100)
+            k_gather<__half, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
+        else
+            k_gather<__nv_bfloat16, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
+                                                                    (__nv_bfloat16*)interior);
+    } else {
+        if (gp.dtype == 3)
+            k_gather<float, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
+        else if (gp.dtype == 100)
+            k_gather<__half, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
+        else
+            k_gather<__nv_bfloat16, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
+                                                                     (__nv_bfloat16*)interior);
+    }
 }
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                        const uint32_t* scmap, uint32_t* cnt, cudaStream_t s) {

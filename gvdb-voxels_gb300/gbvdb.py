@@ -42,7 +42,7 @@ EXPORTS = [
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
     "gbvdb_export_point_leaves", "gbvdb_checksum_device", "gbvdb_fill_channel4", "gbvdb_clear_channel",
     "gbvdb_get_vol_bounds", "gbvdb_get_device_bytes", "gbvdb_get_vdb_info", "gbvdb_activate_space",
-    "gbvdb_rebuild_topology_cpu",
+    "gbvdb_rebuild_topology_cpu", "gbvdb_tune_table_source",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -66,6 +66,10 @@ TUNE_DENSE_MIN = 1
 TUNE_FUSED_APRON = 2
 TUNE_AUTOTUNE = 3
 TUNE_TOUCH_DIRS = 4
+TUNE_TABLE = 5
+TUNE_BIN_UNROLL = 6
+TUNE_SCATTER_UNROLL = 7
+TUNE_GATHER_BLOCKS = 8
 FUNC_SMOOTH = 113
 
 
@@ -91,6 +95,8 @@ def load(path=LIB_PATH):
     for name in EXPORTS:
         getattr(L, name).restype = i32
     L.gbvdb_last_error.restype = ctypes.c_char_p
+    L.gbvdb_tune_table_source.restype = ctypes.c_char_p
+    L.gbvdb_tune_table_source.argtypes = []
     L.gbvdb_create.argtypes = [i32, ctypes.POINTER(vp)]
     L.gbvdb_destroy.argtypes = [vp]
     L.gbvdb_set_stream.argtypes = [vp, vp]

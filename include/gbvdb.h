@@ -272,7 +272,17 @@ GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** int
                                     bricks) record, per home leaf position, the set of the 27 neighbour
                                     directions its points' boxes reach, when no box reaches past a
                                     neighbour; 0: every point walks its box positions.  Same node sets. */
+#define GBVDB_TUNE_TABLE 5        /* 1 (default): when a tuning table is loaded (JSON from $GBVDB_TUNE_TABLE, else
+                                     tune_table.json beside libgbvdb.so; written by gvdb-voxels_gb300/tune.py), an
+                                     insert or gather of n points takes its bucket's settings: the dense-form
+                                     threshold (in place of the autotuner), the gather's resident blocks per SM
+                                     and the binning passes' points per thread.  0: built-in defaults. */
+#define GBVDB_TUNE_BIN_UNROLL 6   /* points per thread of the subcell count pass: 1, 2 or 4 (0: table / default 2) */
+#define GBVDB_TUNE_SCATTER_UNROLL 7 /* points per thread of the binning scatter: 2, 4 or 8 (0: table / default 4) */
+#define GBVDB_TUNE_GATHER_BLOCKS 8  /* resident blocks per SM the gather is built for: 10 or 8 (0: table / 10) */
 GBVDB_API gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value);
+/* where the tuning table was read from, or "" when none was loaded */
+GBVDB_API const char* gbvdb_tune_table_source(void);
 /* timing of the last call per stage (ms, CUDA events) when profiling is enabled */
 GBVDB_API gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable);
 GBVDB_API gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap);

@@ -1,8 +1,9 @@
 """Build recipe for the reference-kernel harness (test infrastructure).
 
 - oracle/_ref/cuda_gvdb_module.ptx: the reference's own kernel module, compiled
-  from its source file kernels/cuda_gvdb_module.cu with the flags of its CMake
-  project (PTX, --use_fast_math).  Built only where the reference sources are
+  from its source file source/gvdb_library/kernels/cuda_gvdb_module.cu of the
+  reference checkout ($GVDB_REFERENCE, or the first argument) with the flags of
+  its CMake project (PTX, --use_fast_math).  Built only where the reference sources are
   present; the PTX is text, so it also runs on a GPU machine without those
   sources, where the CUDA driver JIT-compiles it.  It is loaded and launched, never
   read.
@@ -16,7 +17,9 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_KERNELS = "/root/reference/source/gvdb_library/kernels"
+# the reference checkout: $GVDB_REFERENCE, else the directory this recipe was set up with
+REF_ROOT = os.environ.get("GVDB_REFERENCE", "/root/reference")
+REF_KERNELS = os.path.join(REF_ROOT, "source", "gvdb_library", "kernels")
 PTX = os.path.join(OUT, "cuda_gvdb_module.ptx")
 HARNESS_SRC = os.path.join(HERE, "ref_harness.cu")
 HARNESS = os.path.join(OUT, "libref_harness.so")
@@ -56,5 +59,9 @@ def build():
 
 
 if __name__ == "__main__":
+    import sys
+
+    if len(sys.argv) > 1:  # python oracle/ref_build.py <reference checkout>
+        REF_KERNELS = os.path.join(sys.argv[1], "source", "gvdb_library", "kernels")
     print(build_ptx())
     print(build_harness())

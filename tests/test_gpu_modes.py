@@ -155,6 +155,8 @@ def compare_seq(oo, gg, boundval):
 def golden_cases():
     out = []
     for p in sorted(glob.glob(os.path.join(HERE, "golden", "*.npz"))):
+        if os.path.basename(p).startswith("op_"):  # operator fixtures (test_oracle_golden.py)
+            continue
         fx = np.load(p)
         nf = int(fx["nframes"])
         case = {"name": os.path.basename(p), "log2dims": tuple(int(v) for v in fx["log2dims"]),
