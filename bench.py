@@ -326,10 +326,12 @@ def serve_pools(nmax, seed):
     return pools
 
 
-def serve_requests(count, seed, pools, lo=1e4, hi=4e6, upd_frac=0.3, nres=8):
+def serve_requests(count, seed, pools, lo=1e4, hi=4e6, upd_frac=0.3, nres=8, nver=4):
     """The request stream: size log-uniform in [lo, hi], generator uniform, 30% incremental
     updates (5% of a resident grid's points moved by N(0, 2)), FP32 / FP16 storage
-    alternating.  Payloads are prepared up front in pinned host memory."""
+    alternating.  Payloads are prepared up front in pinned host memory; each resident
+    grid's updates cycle through `nver` prepared versions (version v+1 moves 5% of the
+    points of version v), so that 10,000 requests fit in a few GB of pinned memory."""
     import torch
 
     rng = np.random.default_rng(seed)
@@ -337,12 +339,14 @@ def serve_requests(count, seed, pools, lo=1e4, hi=4e6, upd_frac=0.3, nres=8):
     for i in range(count):
         if resident and rng.random() < upd_frac:
             rid = int(rng.choice(sorted(resident)))
-            k, prev = resident[rid]
-            q = prev.numpy().copy()
-            idx = rng.choice(q.shape[0], max(1, q.shape[0] // 20), replace=False)
-            q[idx] += rng.normal(0.0, 2.0, size=(idx.size, 3)).astype(np.float32)
-            pts = torch.from_numpy(q).pin_memory()
-            resident[rid] = (k, pts)
+            k, vers, nxt = resident[rid]
+            if len(vers) < nver:  # the next version: 5% of the last one's points moved
+                q = vers[-1].numpy().copy()
+                idx = rng.choice(q.shape[0], max(1, q.shape[0] // 20), replace=False)
+                q[idx] += rng.normal(0.0, 2.0, size=(idx.size, 3)).astype(np.float32)
+                vers.append(torch.from_numpy(q).pin_memory())
+            pts = vers[nxt % len(vers)]
+            resident[rid] = (k, vers, nxt + 1)
         else:
             k = int(rng.integers(len(SERVE_KINDS)))
             n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
@@ -350,7 +354,7 @@ def serve_requests(count, seed, pools, lo=1e4, hi=4e6, upd_frac=0.3, nres=8):
             rid = -1
             if len(resident) < nres and rng.random() < 0.25:
                 rid = len(resident)
-                resident[rid] = (k, pts)
+                resident[rid] = (k, [pts], 1)
         reqs.append({"kind": k, "points": pts, "resident_id": rid, "dtype": 3 if i % 2 == 0 else 100})
     return reqs
 
@@ -392,18 +396,23 @@ def bench_served(args):
     cap = 120 << 30
     out = {"requests": len(reqs), "workers": args.serve_workers, "cap_bytes": cap,
            "stream": "log-uniform [1e4, %.0e] points; shell / fluid / surface generators; 30%% incremental "
-                     "updates of resident grids (5%% of points moved by N(0,2)); FP32 / FP16 alternating; "
-                     "Poisson arrivals; host (pinned) points, H2D inside each job" % args.serve_max_points,
+                     "updates of resident grids (5%% of points moved by N(0,2); each resident grid cycles through 4 "
+                     "prepared versions); FP32 / FP16 alternating; Poisson arrivals; host (pinned) points, H2D "
+                     "inside each job; saturation = the whole stream, a paced rate = its first rate * %g s "
+                     "requests" % (args.serve_max_points, args.serve_seconds),
            "plain": "one worker: the per-frame calls of each request back to back on one stream",
            "points_total": float(sum(int(r["points"].shape[0]) for r in reqs)), "rates": []}
     # warm-up (library, allocator pools)
     serve_run(reqs[: min(20, len(reqs))], None, args.serve_workers, 0, cap)
     for rate in [None] + list(args.serve_rates):
-        srv = serve_run(reqs, rate, args.serve_workers, 5, cap)
-        pln = serve_run(reqs, rate, 1, 5, cap)
+        # saturation: the whole stream; a paced rate: the stream's first rate * serve_seconds
+        # requests (10,000 requests at 100 req/s would take 100 s per run)
+        sub = reqs if rate is None else reqs[: max(50, min(len(reqs), int(rate * args.serve_seconds)))]
+        srv = serve_run(sub, rate, args.serve_workers, 5, cap)
+        pln = serve_run(sub, rate, 1, 5, cap)
         same = srv.pop("checksums") == pln.pop("checksums")
-        out["rates"].append({"rate_req_s": rate if rate else "saturation", "served": srv, "plain": pln,
-                             "same_results": same})
+        out["rates"].append({"rate_req_s": rate if rate else "saturation", "requests": len(sub), "served": srv,
+                             "plain": pln, "same_results": same})
     sat = out["rates"][0]
     out["speedup_points_per_s_at_saturation"] = sat["served"]["points_per_s"] / sat["plain"]["points_per_s"]
     return out
@@ -756,8 +765,10 @@ def main():
                     help="particles per fluid frame (default: the workload's 4,194,304; smaller for profiling)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form stream")
     ap.add_argument("--no-surface", action="store_true", help="skip the 16.8M-point surface workload")
-    ap.add_argument("--serve-requests", type=int, default=300)
-    ap.add_argument("--batch-grids", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=10_000)
+    ap.add_argument("--serve-seconds", type=float, default=8.0,
+                    help="paced rates run the stream's first rate * serve_seconds requests")
+    ap.add_argument("--batch-grids", type=int, default=256)
     ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-max-points", type=float, default=4e6)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 500.0, 2000.0])

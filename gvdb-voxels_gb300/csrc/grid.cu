@@ -864,6 +864,7 @@ struct gbvdb_grid_s {
     gbvdb_status update_atlas() {  // UpdateAtlas (VG.cpp:2630-2704)
         layout_changed();
         if (!ch[0].used) throw StatusError{GBVDB_INVALID_ARG, "no atlas channel"};
+        stage_begin();
         long long total = ncnt[0];
         // the flagged-leaf count is F below; an earlier count is only used when it is current
         long long used = nused0_stale ? 0 : nused[0];
@@ -897,6 +898,8 @@ struct gbvdb_grid_s {
                                 stream);
         check_launch("assign_slots");
         atlas_last = (int)F;
+        mark();
+        stage_end();
         return GBVDB_OK;
     }
 

@@ -280,43 +280,70 @@ struct DirDomain {
     int dim[3];
 };
 
+// kU points per thread per step: their position loads, then their entry loads, are
+// issued together (the pass is bound by the latency of that two-load chain)
+template <int kU>
 __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, int lg, int3 rlo, int3 rhi,
                              DirDomain dd, uint32_t* __restrict__ dirs, int* err) {
     const int rr = 1 << lg;
     const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
-        float x, y, z;
-        load_pos(p.base, i, p.stride, p.off, x, y, z);
-        const float w[3] = {fadd(x, orig.x), fadd(y, orig.y), fadd(z, orig.z)};
-        if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
-        int m[3], hb[3];
-        bool any = true;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+        float w[kU][3];
+        bool ok[kU];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const int ip = (int)w[a];
-            const float fi = (float)ip;
-            int lo = trunc_mult((int)fsub(fi, radius), lg), hi = trunc_mult((int)fadd(fi, hr), lg);
-            if (lo < rl[a]) lo += ((rl[a] - lo + rr - 1) >> lg) << lg;
-            if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
-            hb[a] = ip >> lg;
-            const int l = (lo >> lg) - hb[a], h = (hi >> lg) - hb[a];
-            any &= hi >= lo;
-            m[a] = hi >= lo ? (((1 << (h - l + 1)) - 1) << (l + 1)) & 7 : 0;
+        for (int u = 0; u < kU; u++) {
+            const long long i = i0 + u * stride;
+            ok[u] = i < p.n;
+            if (ok[u]) {
+                load_pos(p.base, i, p.stride, p.off, w[u][0], w[u][1], w[u][2]);
+                w[u][0] = fadd(w[u][0], orig.x);
+                w[u][1] = fadd(w[u][1], orig.y);
+                w[u][2] = fadd(w[u][2], orig.z);
+            }
         }
-        if (!any) continue;
-        uint32_t m27 = 0;
+        uint32_t m27[kU];
+        long long ent[kU];
 #pragma unroll
-        for (int dz = 0; dz < 3; dz++)
+        for (int u = 0; u < kU; u++) {
+            m27[u] = 0;
+            ent[u] = -1;
+            if (!ok[u] || w[u][0] < 0 || w[u][1] < 0 || w[u][2] < 0) continue;
+            int m[3], hb[3];
+            bool any = true;
 #pragma unroll
-            for (int dy = 0; dy < 3; dy++)
-                if (((m[2] >> dz) & (m[1] >> dy)) & 1) m27 |= (uint32_t)m[0] << (dz * 9 + dy * 3);
-        const int rx = hb[0] - dd.lo[0], ry = hb[1] - dd.lo[1], rz = hb[2] - dd.lo[2];
-        if ((unsigned)rx >= (unsigned)dd.dim[0] || (unsigned)ry >= (unsigned)dd.dim[1] || (unsigned)rz >= (unsigned)dd.dim[2]) {
-            atomicOr(err, 1);
-            continue;
+            for (int a = 0; a < 3; a++) {
+                const int ip = (int)w[u][a];
+                const float fi = (float)ip;
+                int lo = trunc_mult((int)fsub(fi, radius), lg), hi = trunc_mult((int)fadd(fi, hr), lg);
+                if (lo < rl[a]) lo += ((rl[a] - lo + rr - 1) >> lg) << lg;
+                if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
+                hb[a] = ip >> lg;
+                const int l = (lo >> lg) - hb[a], h = (hi >> lg) - hb[a];
+                any &= hi >= lo;
+                m[a] = hi >= lo ? (((1 << (h - l + 1)) - 1) << (l + 1)) & 7 : 0;
+            }
+            if (!any) continue;
+#pragma unroll
+            for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+                for (int dy = 0; dy < 3; dy++)
+                    if (((m[2] >> dz) & (m[1] >> dy)) & 1) m27[u] |= (uint32_t)m[0] << (dz * 9 + dy * 3);
+            const int rx = hb[0] - dd.lo[0], ry = hb[1] - dd.lo[1], rz = hb[2] - dd.lo[2];
+            if ((unsigned)rx >= (unsigned)dd.dim[0] || (unsigned)ry >= (unsigned)dd.dim[1] ||
+                (unsigned)rz >= (unsigned)dd.dim[2]) {
+                atomicOr(err, 1);
+                m27[u] = 0;
+                continue;
+            }
+            ent[u] = ((long long)rx * dd.dim[1] + ry) * dd.dim[2] + rz;
         }
-        uint32_t* e = dirs + ((long long)rx * dd.dim[1] + ry) * dd.dim[2] + rz;
-        if ((__ldcg(e) & m27) != m27) atomicOr(e, m27);
+        uint32_t cur[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) cur[u] = ent[u] >= 0 ? __ldcg(dirs + ent[u]) : 0xFFFFFFFFu;
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+            if (ent[u] >= 0 && (cur[u] & m27[u]) != m27[u]) atomicOr(dirs + ent[u], m27[u]);
     }
 }
 
@@ -618,8 +645,8 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
         }
         cudaMemsetAsync(dirs, 0, (size_t)touch_dirs_words(dom) * 4, s);
         if (p.n > 0)
-            k_touch_dirs<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
-                                                                      dirs, err);
+            k_touch_dirs<4><<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi,
+                                                                         dd, dirs, err);
         const long long nw = (dom.d[0].nbits + 31) >> 5;
         k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
     } else {

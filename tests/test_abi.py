@@ -61,3 +61,28 @@ def test_create_without_device_fails_cleanly():
     h = ctypes.c_void_p()
     st = L.gbvdb_create(0, ctypes.byref(h))
     assert st == gbvdb.CUDA_ERROR and not h.value
+
+
+def test_tuning_table_is_read(tmp_path):
+    """the library reads the tuning table beside it (or $GBVDB_TUNE_TABLE) at first use"""
+    import json
+    import subprocess
+    import sys
+
+    table = os.path.join(ROOT, "gvdb-voxels_gb300", "tune_table.json")
+    assert os.path.exists(table)
+    d = json.load(open(table))
+    assert d["buckets"] and all({"max_points", "dense_min", "gather_blocks", "bin_unroll", "scatter_unroll"}
+                                <= set(b) for b in d["buckets"])
+    L = gbvdb.load()
+    assert L.gbvdb_tune_table_source().decode() == os.path.realpath(table) or \
+        os.path.samefile(L.gbvdb_tune_table_source().decode(), table)
+    # an explicit table through the environment (a fresh process: the table is read once)
+    alt = tmp_path / "t.json"
+    alt.write_text(json.dumps({"buckets": [{"max_points": 5, "dense_min": 1, "gather_blocks": 8,
+                                            "bin_unroll": 4, "scatter_unroll": 8}]}))
+    code = ("import sys; sys.path.insert(0, %r); import gbvdb; "
+            "print(gbvdb.load().gbvdb_tune_table_source().decode())" % os.path.join(ROOT, "gvdb-voxels_gb300"))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         env=dict(os.environ, GBVDB_TUNE_TABLE=str(alt))).stdout.strip()
+    assert out == str(alt)
