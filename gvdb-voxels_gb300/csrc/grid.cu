@@ -236,6 +236,19 @@ struct gbvdb_grid_s {
     DevBuf nbr_table;
     long long nbr_count = -1;
     DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
+    // Side stream of gbvdb_checksum_overlap: the checksum of a frame reads the channel
+    // interiors while the grid's stream goes on with the next frame's topology and
+    // binning; every entry point that writes or reallocates interiors or the atlas map
+    // (all but the topology, binning and accessor calls) first makes the grid's stream
+    // wait for it on the device (join_side).
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_start = nullptr, side_done = nullptr;
+    bool side_pending = false;
+    void join_side() {
+        if (!side_pending) return;
+        cudaStreamWaitEvent(stream, side_done, 0);
+        side_pending = false;
+    }
     DevBuf push_bad;   // fused apron: the push check's flag (one int)
     DevBuf nbmask;     // linked flags of the 27 bricks around each leaf (InsertPointsSubcell)
     DevBuf gtab;       // per-brick gather setup (neighbour ranks and bin ranges, origin, slot)
@@ -1584,10 +1597,16 @@ struct gbvdb_grid_s {
     std::lock_guard<std::mutex> _lk((g)->mu);             \
     try {                                                 \
         cudaSetDevice((g)->device);
-// every other entry point first commits pending host activations (ActivateSpace)
-#define GBVDB_GUARD(g)                                    \
+// topology, binning and accessor entry points commit pending host activations
+// (ActivateSpace) first
+#define GBVDB_GUARD_NOJOIN(g)                             \
     GBVDB_GUARD_NOCOMMIT(g)                               \
         (g)->host_commit();
+// every other entry point also orders the grid's stream after a pending overlapped
+// checksum (gbvdb_checksum_overlap)
+#define GBVDB_GUARD(g)                                    \
+    GBVDB_GUARD_NOJOIN(g)                                 \
+        (g)->join_side();
 #define GBVDB_END(g)                                      \
     }                                                     \
     catch (const StatusError& e) {                        \
@@ -1651,11 +1670,16 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
-                      &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab};
+                      &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab, &g->sorted_clr,
+                      &g->list_clr};
+    g->join_side();
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
     for (int c = 0; c < 8; c++) { g->release(g->ch[c].interior); g->release(g->ch[c].apron_buf); }
     cudaStreamSynchronize(g->stream);
+    if (g->side) cudaStreamDestroy(g->side);
+    if (g->side_start) cudaEventDestroy(g->side_start);
+    if (g->side_done) cudaEventDestroy(g->side_done);
     for (int i = 0; i < 64; i++) cudaEventDestroy(g->ev[i]);
     for (int i = 0; i < 2 * gbvdb_grid_s::kTuneN; i++) cudaEventDestroy(g->tune_ev[i]);
     cudaFreeHost(g->pinned);
@@ -1784,7 +1808,7 @@ gbvdb_status gbvdb_load_vbx(gbvdb_grid g, const char* path) {
 
 gbvdb_status gbvdb_set_points(gbvdb_grid g, const void* pos, int64_t n, int off, int stride, const void* vel,
                               int vel_off, int vel_stride, const void* clr, int clr_off, int clr_stride) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     (void)vel_off; (void)vel_stride;
     if ((!pos && n > 0) || n < 0 || stride < 12 || off < 0 || (off % 4) || (stride % 4)) return GBVDB_INVALID_ARG;
     if (clr && (clr_off < 0 || clr_stride < 4 || (clr_off % 4) || (clr_stride % 4))) return GBVDB_INVALID_ARG;
@@ -1830,7 +1854,7 @@ gbvdb_status gbvdb_rebuild_topology_cpu(gbvdb_grid g, int64_t n, const float ori
 }
 
 gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3]) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     g->nbr_count = -1;  // the neighbour table and point groups describe the previous topology
     g->ins_n = -1;
     return g->rebuild(n, radius, f3(orig), false, 0);
@@ -1838,7 +1862,7 @@ gbvdb_status gbvdb_rebuild_topology(gbvdb_grid g, int64_t n, float radius, const
 }
 
 gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, const float orig[3], int min_depth) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     g->nbr_count = -1;
     g->ins_n = -1;
     return g->rebuild(n, radius, f3(orig), true, min_depth);
@@ -1846,14 +1870,14 @@ gbvdb_status gbvdb_accumulate_topology(gbvdb_grid g, int64_t n, float radius, co
 }
 
 gbvdb_status gbvdb_request_full_rebuild(gbvdb_grid g, int tf) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     g->rebuild_topo = tf ? 1 : 0;
     return GBVDB_OK;
     GBVDB_END(g)
 }
 
 gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bounds) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     (void)commit_pool;  // pools live on the device only; nothing to commit
     if (compute_bounds && g->ncnt[0] > 0) {  // ComputeBounds (VG.cpp:1792-1816)
         g->grow(g->misc, 256);
@@ -1875,7 +1899,7 @@ gbvdb_status gbvdb_update_atlas(gbvdb_grid g) {
 
 gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
                                          int64_t* out_len) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     long long len = 0;
     gbvdb_status st = g->insert_subcell(sc, n, radius, f3(trans), &len);
     if (st == GBVDB_OK && out_len) *out_len = len;
@@ -1885,7 +1909,7 @@ gbvdb_status gbvdb_insert_points_subcell(gbvdb_grid g, int sc, int64_t n, float 
 
 gbvdb_status gbvdb_insert_points_subcell_fp16(gbvdb_grid g, int sc, int64_t n, float radius, const float trans[3],
                                               int64_t* out_len) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     long long len = 0;
     gbvdb_status st = g->insert_subcell(sc, n, radius, f3(trans), &len, true);
     if (st == GBVDB_OK && out_len) *out_len = len;
@@ -1964,7 +1988,7 @@ gbvdb_status gbvdb_clear_channel(gbvdb_grid g, int chan) {
 }
 
 gbvdb_status gbvdb_get_depth(gbvdb_grid g, int* depth, int* top_lev) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (depth) *depth = g->last_depth;
     if (top_lev) *top_lev = g->top_lev();
     return GBVDB_OK;
@@ -1972,7 +1996,7 @@ gbvdb_status gbvdb_get_depth(gbvdb_grid g, int* depth, int* top_lev) {
 }
 
 gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     for (int l = 0; l < kMaxLev; l++) {
         if (total) total[l] = g->ncnt[l];
         if (used) {
@@ -1985,7 +2009,7 @@ gbvdb_status gbvdb_get_node_counts(gbvdb_grid g, int64_t* total, int64_t* used) 
 }
 
 gbvdb_status gbvdb_get_vol_bounds(gbvdb_grid g, float* out6) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (!out6) return GBVDB_INVALID_ARG;
     if (!g->bounds_valid) return GBVDB_NOOP;
     for (int a = 0; a < 6; a++) out6[a] = (float)g->bounds[a];
@@ -1994,7 +2018,7 @@ gbvdb_status gbvdb_get_vol_bounds(gbvdb_grid g, float* out6) {
 }
 
 gbvdb_status gbvdb_get_point_bounds(gbvdb_grid g, float* out6) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (!out6) return GBVDB_INVALID_ARG;
     for (int a = 0; a < 3; a++) { out6[a] = g->posmin[a]; out6[3 + a] = g->posmax[a]; }
     return GBVDB_OK;
@@ -2002,7 +2026,7 @@ gbvdb_status gbvdb_get_point_bounds(gbvdb_grid g, float* out6) {
 }
 
 gbvdb_status gbvdb_export_nodes(gbvdb_grid g, int lev, void* host_out, int64_t cap) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (lev < 0 || lev >= kMaxLev || !host_out) return GBVDB_INVALID_ARG;
     if (cap < g->ncnt[lev]) return GBVDB_CAPACITY;
     if (g->ncnt[lev] == 0) return GBVDB_OK;
@@ -2014,7 +2038,7 @@ gbvdb_status gbvdb_export_nodes(gbvdb_grid g, int lev, void* host_out, int64_t c
 }
 
 gbvdb_status gbvdb_export_childlist(gbvdb_grid g, int lev, uint64_t* host_out, int64_t cap) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (lev < 1 || lev >= g->levs || !host_out) return GBVDB_INVALID_ARG;
     long long n = g->ncnt[lev] * g->cl_len(lev);
     if (cap < n) return GBVDB_CAPACITY;
@@ -2108,6 +2132,36 @@ gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out) {
     launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
                           g->ptr<double>(g->csum_part), dev_out, g->stream);
     g->check_launch("checksum");
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+// the checksum on the grid's side stream: ordered after the grid's work so far, while
+// the grid's stream goes on; the next entry point that writes interiors waits for it
+gbvdb_status gbvdb_checksum_overlap(gbvdb_grid g, int chan, double* dev_out, double* host_out) {
+    GBVDB_GUARD(g)  // joins a previous overlapped checksum (its partials are reused)
+    if (chan < 0 || chan >= 8 || !g->ch[chan].used || !dev_out) return GBVDB_INVALID_ARG;
+    if (g->ch[chan].dtype == GBVDB_T_UCHAR4) return GBVDB_NOT_SUPPORTED;
+    if (!g->side) {
+        g->check(cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking), "side stream");
+        g->check(cudaEventCreateWithFlags(&g->side_start, cudaEventDisableTiming), "side event");
+        g->check(cudaEventCreateWithFlags(&g->side_done, cudaEventDisableTiming), "side event");
+    }
+    g->grow(g->csum_part, (size_t)std::max(g->atlas_last, 1) * 8);
+    g->check(cudaEventRecord(g->side_start, g->stream), "side event");
+    g->check(cudaStreamWaitEvent(g->side, g->side_start, 0), "side wait");
+    launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
+                          g->ptr<double>(g->csum_part), dev_out, g->side);
+    g->check_launch("checksum");
+    if (host_out) g->check(cudaMemcpyAsync(host_out, dev_out, 8, cudaMemcpyDeviceToHost, g->side), "checksum copy");
+    g->check(cudaEventRecord(g->side_done, g->side), "side event");
+    g->side_pending = true;
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
+gbvdb_status gbvdb_join(gbvdb_grid g) {
+    GBVDB_GUARD(g)
     return GBVDB_OK;
     GBVDB_END(g)
 }
@@ -2246,14 +2300,14 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
 const char* gbvdb_tune_table_source(void) { return tune_table().source.c_str(); }
 
 gbvdb_status gbvdb_set_profile(gbvdb_grid g, int enable) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     g->profile = enable != 0;
     return GBVDB_OK;
     GBVDB_END(g)
 }
 
 gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (!out4) return GBVDB_INVALID_ARG;
     out4[0] = g->n_launch;
     out4[1] = g->n_readback;
@@ -2289,7 +2343,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
 }
 
 gbvdb_status gbvdb_get_stage_times(gbvdb_grid g, double* ms, int cap) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)
     if (!ms) return GBVDB_INVALID_ARG;
     int n = std::min<int>(cap, (int)g->stage_ms.size());
     for (int i = 0; i < n; i++) ms[i] = g->stage_ms[(size_t)i];

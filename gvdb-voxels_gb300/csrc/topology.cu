@@ -38,15 +38,31 @@ __global__ void k_bbox(PointSrc p, float3 orig, int* out6) {
         // packed float3 on a 16-byte boundary: four points per three 16-byte loads
         const float4* v = reinterpret_cast<const float4*>(p.base);
         const long long groups = p.n >> 2;
-        for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < groups;
-             gi += (long long)gridDim.x * blockDim.x) {
-            const float4 a = __ldg(v + 3 * gi), b = __ldg(v + 3 * gi + 1), c = __ldg(v + 3 * gi + 2);
-            const float e[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+        const long long gstride = (long long)gridDim.x * blockDim.x;
+        // two groups per thread per step: six 16-byte loads in flight
+        for (long long g0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; g0 < groups; g0 += 2 * gstride) {
+            float4 q[6];
 #pragma unroll
-            for (int k = 0; k < 12; k++) {
-                const float w = fadd(e[k], o[k % 3]);
-                mn[k % 3] = fminf(mn[k % 3], w);
-                mx[k % 3] = fmaxf(mx[k % 3], w);
+            for (int u = 0; u < 2; u++) {
+                const long long gi = g0 + u * gstride;
+                const bool in = gi < groups;
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    q[3 * u + k] = in ? __ldg(v + 3 * gi + k) : make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const bool in = g0 + u * gstride < groups;
+                const float e[12] = {q[3 * u].x,     q[3 * u].y,     q[3 * u].z,     q[3 * u].w,
+                                     q[3 * u + 1].x, q[3 * u + 1].y, q[3 * u + 1].z, q[3 * u + 1].w,
+                                     q[3 * u + 2].x, q[3 * u + 2].y, q[3 * u + 2].z, q[3 * u + 2].w};
+                if (!in) continue;
+#pragma unroll
+                for (int k = 0; k < 12; k++) {
+                    const float w = fadd(e[k], o[k % 3]);
+                    mn[k % 3] = fminf(mn[k % 3], w);
+                    mx[k % 3] = fmaxf(mx[k % 3], w);
+                }
             }
         }
         first = groups << 2;
@@ -376,25 +392,46 @@ __global__ void k_touch_from_dirs(KeyDomain d, DirDomain dd, const uint32_t* __r
 // one box, trunc(b / R_lev) * R_lev .. trunc(e / R_lev) * R_lev is the set of parents
 // of trunc(b / R_lev-1) * R_lev-1 .. trunc(e / R_lev-1) * R_lev-1 once both are clipped
 // to the root (coordinates >= 0, where truncation is floor and the ranges nest).
+// The parent level's bitmap is small (a parent covers 8^3 or more children), so many
+// children of one warp and block share its words: the bits are ORed per block in
+// shared memory when the parent bitmap fits (kTouchSmemWords), then one atomicOr per
+// non-zero word; a same-word atomic per child would serialise on a few L2 lines.
 __global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_t* touched, int* err) {
+    extern __shared__ uint32_t sbm[];
+    const long long pw0 = parent.bitbase >> 5, pnw = (parent.nbits + 31) >> 5;
+    const bool use_smem = pnw <= kTouchSmemWords;
+    if (use_smem) {
+        for (long long k = threadIdx.x; k < pnw; k += blockDim.x) sbm[k] = 0;
+        __syncthreads();
+    }
     // one thread per bit of the child level (a warp per bitmap word)
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long w = g >> 5, w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
-    if (w >= nw) return;
     const int b = (int)(g & 31);
-    if (!((touched[w0 + w] >> b) & 1u)) return;
-    const long long li = w * 32 + b;
-    const int rz = (int)(li % child.dim[2]);
-    const long long q = li / child.dim[2];
-    const int ry = (int)(q % child.dim[1]);
-    const int rx = (int)(q / child.dim[1]);
-    const long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
-                                 (child.lo[2] + rz) >> lgres);
-    if (pb < 0) {
-        atomicOr(err, 1);
-        return;
+    if (w < nw && ((touched[w0 + w] >> b) & 1u)) {
+        const long long li = w * 32 + b;
+        const int rz = (int)(li % child.dim[2]);
+        const long long q = li / child.dim[2];
+        const int ry = (int)(q % child.dim[1]);
+        const int rx = (int)(q / child.dim[1]);
+        const long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
+                                     (child.lo[2] + rz) >> lgres);
+        if (pb < 0) {
+            atomicOr(err, 1);
+        } else if (use_smem) {
+            const long long lb = pb - parent.bitbase;
+            atomicOr(&sbm[lb >> 5], 1u << (lb & 31));
+        } else {
+            set_bit(touched, pb);
+        }
     }
-    set_bit(touched, pb);
+    if (use_smem) {
+        __syncthreads();
+        for (long long k = threadIdx.x; k < pnw; k += blockDim.x) {
+            const uint32_t v = sbm[k];
+            if (v && (__ldcg(touched + pw0 + k) & v) != v) atomicOr(touched + pw0 + k, v);
+        }
+    }
 }
 
 // a warp per touched-bitmap word of level `lev`, a lane per bit: getPosParent(pos, lev)
@@ -615,7 +652,9 @@ inline unsigned grid_stride_blocks(long long n, int t) {
 }  // namespace
 
 void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s) {
-    k_bbox<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, out6);
+    // at most 4 blocks per SM: each block ends with six same-address atomics
+    const unsigned b = std::min<unsigned>(grid_stride_blocks(p.n, 512), 152u * 4u);
+    k_bbox<<<b, 512, 0, s>>>(p, orig, out6);
 }
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
                        uint32_t* bitmap, int* err, cudaStream_t s) {
@@ -644,9 +683,21 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
             dd.dim[a] = dom.d[0].dim[a] + 2;
         }
         cudaMemsetAsync(dirs, 0, (size_t)touch_dirs_words(dom) * 4, s);
-        if (p.n > 0)
+        if (p.n > 0) {
+            // every 64th point first: it fills most entries while few points contend for
+            // them, so that in the full pass nearly every point finds its bits set and
+            // issues no atomic (when all points start on empty entries, the atomics of a
+            // dense region pile up on its few entries)
+            if (p.n >= 64 * 1024) {
+                PointSrc q = p;
+                q.stride = p.stride * 64;
+                q.n = (p.n + 63) / 64;
+                k_touch_dirs<4><<<grid_stride_blocks(q.n, 256), 256, 0, s>>>(q, orig, radius, hr, t.lgrange[0], rlo,
+                                                                             rhi, dd, dirs, err);
+            }
             k_touch_dirs<4><<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi,
                                                                          dd, dirs, err);
+        }
         const long long nw = (dom.d[0].nbits + 31) >> 5;
         k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
     } else {
@@ -659,7 +710,10 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
     }
     for (int lev = 1; lev < depth; lev++) {
         long long nw = (dom.d[lev - 1].nbits + 31) >> 5;
-        k_touch_up<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
+        const long long pnw = (dom.d[lev].nbits + 31) >> 5;
+        const size_t smem = pnw <= kTouchSmemWords ? (size_t)pnw * 4 : 0;
+        // 1024 threads per block: fewer blocks flushing the parent words
+        k_touch_up<<<blocks_for(nw * 32, 1024), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
     }
     for (int lev = 0; lev < depth; lev++) {
         long long nw = (dom.d[lev].nbits + 31) >> 5;

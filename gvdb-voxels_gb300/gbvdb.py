@@ -42,7 +42,7 @@ EXPORTS = [
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
     "gbvdb_export_point_leaves", "gbvdb_checksum_device", "gbvdb_fill_channel4", "gbvdb_clear_channel",
     "gbvdb_get_vol_bounds", "gbvdb_get_device_bytes", "gbvdb_get_vdb_info", "gbvdb_activate_space",
-    "gbvdb_rebuild_topology_cpu", "gbvdb_tune_table_source",
+    "gbvdb_rebuild_topology_cpu", "gbvdb_tune_table_source", "gbvdb_checksum_overlap", "gbvdb_join",
     "gbvdb_server_create", "gbvdb_server_submit", "gbvdb_server_wait", "gbvdb_server_poll",
     "gbvdb_server_resident", "gbvdb_server_release", "gbvdb_server_stats", "gbvdb_server_destroy",
 ]
@@ -121,6 +121,8 @@ def load(path=LIB_PATH):
     L.gbvdb_get_vol_bounds.argtypes = [vp, fp]
     L.gbvdb_get_device_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gbvdb_get_vdb_info.argtypes = [vp, vp, i64]
+    L.gbvdb_checksum_overlap.argtypes = [vp, i32, vp, vp]
+    L.gbvdb_join.argtypes = [vp]
     L.gbvdb_activate_space.argtypes = [vp, fp, ctypes.POINTER(ctypes.c_uint64)]
     L.gbvdb_rebuild_topology_cpu.argtypes = [vp, i64, fp, vp, i32]
     L.gbvdb_get_depth.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
@@ -466,6 +468,17 @@ class Grid:
     def checksum_device(self, out, chan=0):
         """FP64 channel sum into `out` (a CUDA float64 tensor element) on the grid's stream."""
         self._check(self.L.gbvdb_checksum_device(self._h, chan, ctypes.c_void_p(out.data_ptr())), "checksum_device")
+
+    def checksum_overlap(self, out, host_out=None, chan=0):
+        """FP64 channel sum into `out` (CUDA float64 element) and `host_out` (pinned CPU float64
+        element, optional) on the grid's side stream, overlapping the grid's next calls"""
+        hp = ctypes.c_void_p(host_out.data_ptr()) if host_out is not None else None
+        self._check(self.L.gbvdb_checksum_overlap(self._h, chan, ctypes.c_void_p(out.data_ptr()), hp),
+                    "checksum_overlap")
+
+    def join(self):
+        """the grid's stream waits for a pending overlapped checksum"""
+        self._check(self.L.gbvdb_join(self._h), "join")
 
     def checksum(self, chan=0):
         out = ctypes.c_double()

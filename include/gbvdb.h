@@ -225,6 +225,17 @@ GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
  * host synchronisation (no counterpart in the reference): for pipelined callers that read
  * the result back asynchronously.  May allocate (per-slot partials). */
 GBVDB_API gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out);
+/* gbvdb_checksum_device issued on the grid's own side stream (no counterpart in the
+ * reference): ordered after the grid's work so far, it runs while the grid's stream
+ * goes on (a frame's checksum overlaps the next frame's topology and binning); every
+ * later entry point of the grid that writes or reallocates channel interiors or the
+ * atlas map (all but the topology, binning and accessor calls) makes the grid's stream
+ * wait for it first.  dev_out (device) receives the FP64 sum and host_out (pinned host
+ * memory, may be NULL) its copy, both on the side stream.  gbvdb_join makes the grid's
+ * stream wait for it explicitly: after gbvdb_join and a synchronisation of the grid's
+ * stream, host_out holds the sum. */
+GBVDB_API gbvdb_status gbvdb_checksum_overlap(gbvdb_grid g, int chan, double* dev_out, double* host_out);
+GBVDB_API gbvdb_status gbvdb_join(gbvdb_grid g);
 /* Allocation-free variant of gbvdb_checksum (no counterpart in the reference).
  * For callers that may not allocate device memory: a host application that owns
  * every device allocation and forbids its plugins to call cudaMalloc, or a

@@ -411,3 +411,38 @@ def test_checksum_device_matches_checksum(gpu_lib):
     g.checksum_device(out[1])
     torch.cuda.synchronize()
     assert out[1].item() == g.checksum(0) and out[0].item() == 0 and out[2].item() == 0
+
+
+def test_checksum_overlap_is_ordered_before_the_next_gather(gpu_lib):
+    """gbvdb_checksum_overlap runs on the grid's side stream while the next frame's
+    topology and binning go on; the next gather waits for it, so each frame's overlapped
+    sum equals that frame's gbvdb_checksum (taken on a second grid fed the same frames)"""
+    import torch
+
+    import gbvdb
+
+    pos, vel = _mini_fluid(n=60000, seed=95)
+    frames = [torch.from_numpy((pos + 0.5 * (k + 1) * vel).astype(np.float32)).cuda() for k in range(5)]
+    stream = torch.cuda.Stream()
+    g = gbvdb.Grid(0, (3, 3, 3, 4), stream=stream)
+    ref = gbvdb.Grid(0, (3, 3, 3, 4))
+    for x in (g, ref):
+        x.add_channel(0)
+    dev = torch.zeros(len(frames), dtype=torch.float64, device="cuda")
+    host = torch.zeros(len(frames), dtype=torch.float64).pin_memory()
+    expect = []
+    with torch.cuda.stream(stream):
+        for k, f in enumerate(frames):
+            for x in (g, ref):
+                n = x.set_points(f)
+                x.rebuild_topology(n, 4.0)
+                x.update_atlas()
+                _, ln = x.insert_points_subcell(4, n, 4.0)
+                x.gather_levelset(4, n, 2.0, (0, 0, 0), ln)
+                x.update_apron(0, 3.0)
+            g.checksum_overlap(dev[k], host[k])
+            expect.append(ref.checksum(0))
+        g.join()
+    torch.cuda.synchronize()
+    assert host.tolist() == expect
+    assert dev.cpu().tolist() == expect
