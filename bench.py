@@ -415,6 +415,14 @@ def bench_served(args):
                              "plain": pln, "same_results": same})
     sat = out["rates"][0]
     out["speedup_points_per_s_at_saturation"] = sat["served"]["points_per_s"] / sat["plain"]["points_per_s"]
+    # the stream with every request stored in FP32, and in FP16, at saturation
+    for name, dt in (("fp32_only", 3), ("fp16_only", 100)):
+        one = [dict(r, dtype=dt) for r in reqs]
+        srv = serve_run(one, None, args.serve_workers, 5, cap)
+        pln = serve_run(one, None, 1, 5, cap)
+        same = srv.pop("checksums") == pln.pop("checksums")
+        out[name] = {"served": srv, "plain": pln, "same_results": same,
+                     "speedup_points_per_s": srv["points_per_s"] / pln["points_per_s"]}
     return out
 
 

@@ -34,6 +34,27 @@ struct ClrSrc {
     int off;
 };
 
+#ifdef __CUDACC__
+// Positions of the four consecutive points i0 .. i0+3 (i0 a multiple of 4): three
+// 16-byte loads when the buffer is packed float3 on a 16-byte boundary (the warp then
+// reads 1,536 contiguous bytes per step), per-point loads otherwise and at the end of
+// the buffer.  Entries past p.n are left unset.
+__device__ __forceinline__ void load_pos4(const PointSrc& p, long long i0, float (&w)[4][3]) {
+    if (p.stride == 12 && p.off == 0 && ((reinterpret_cast<uintptr_t>(p.base) & 15) == 0) && i0 + 4 <= p.n) {
+        const float4* v = reinterpret_cast<const float4*>(p.base + i0 * 12);
+        const float4 a = __ldg(v), b = __ldg(v + 1), c = __ldg(v + 2);
+        w[0][0] = a.x; w[0][1] = a.y; w[0][2] = a.z;
+        w[1][0] = a.w; w[1][1] = b.x; w[1][2] = b.y;
+        w[2][0] = b.z; w[2][1] = b.w; w[2][2] = c.x;
+        w[3][0] = c.y; w[3][1] = c.z; w[3][2] = c.w;
+        return;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+        if (i0 + u < p.n) load_pos(p.base, i0 + u, p.stride, p.off, w[u][0], w[u][1], w[u][2]);
+}
+#endif
+
 // ---- scan.cu
 size_t scan_tmp_bytes(long long n);
 // exclusive scan of n u32 into out[0..n]; out[n] = total.  tmp: scan_tmp_bytes(n) bytes

@@ -117,15 +117,36 @@ template <int kU>
 __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
                             const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ nbmask,
                             uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
+    // kU = 4: four consecutive points per thread, their positions in three 16-byte loads
+    // (load_pos4); kU = 1, 2: points kU grid strides apart
+    constexpr bool kConsec = kU == 4;
     unsigned long long members = 0, orphans = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+    const long long first = kConsec ? 4ll * ((long long)blockIdx.x * blockDim.x + threadIdx.x)
+                                    : (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long step = kConsec ? 4 * stride : kU * stride;
+    for (long long i0 = first; i0 < p.n; i0 += step) {
+        auto idx = [&](int u) { return kConsec ? i0 + u : i0 + u * stride; };
         float w[kU][3];
         bool ok[kU];
+        if constexpr (kConsec) {
+            float raw[4][3];
+            load_pos4(p, i0, raw);
 #pragma unroll
-        for (int u = 0; u < kU; u++) {
-            const long long i = i0 + u * stride;
-            ok[u] = i < p.n && load_valid(p, i, trans, w[u][0], w[u][1], w[u][2]);
+            for (int u = 0; u < kU; u++) {
+                ok[u] = false;
+                if (i0 + u >= p.n || raw[u][2] == kNoHit) continue;  // PT.cuh:282, tested before +trans
+                w[u][0] = fadd(raw[u][0], trans.x);
+                w[u][1] = fadd(raw[u][1], trans.y);
+                w[u][2] = fadd(raw[u][2], trans.z);
+                ok[u] = !(w[u][0] < 0 || w[u][1] < 0 || w[u][2] < 0);
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const long long i = idx(u);
+                ok[u] = i < p.n && load_valid(p, i, trans, w[u][0], w[u][1], w[u][2]);
+            }
         }
         long long leaf[kU];
         unsigned loc[kU];
@@ -157,18 +178,24 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
         uint32_t rk[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) rk[u] = leaf[u] >= 0 ? atomicAdd(bin_cnt + bin[u], 1u) : 0u;
+        int bo[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) {
-            const long long i = i0 + u * stride;
-            if (i >= p.n) continue;
-            if (!ok[u]) {
-                bin_of[i] = -1;
-            } else if (leaf[u] < 0) {
-                bin_of[i] = -2;
-                orphans++;
-            } else {
-                rank_of[i] = rk[u];
-                bin_of[i] = (int)bin[u];
+            bo[u] = !ok[u] ? -1 : (leaf[u] < 0 ? -2 : (int)bin[u]);
+            if (ok[u] && leaf[u] < 0) orphans++;
+        }
+        if (kConsec && i0 + 4 <= p.n) {  // 16-byte stores of the four consecutive entries
+            *reinterpret_cast<int4*>(bin_of + i0) = make_int4(bo[0], bo[kU > 1 ? 1 : 0], bo[kU > 2 ? 2 : 0],
+                                                              bo[kU > 3 ? 3 : 0]);
+            *reinterpret_cast<uint4*>(rank_of + i0) = make_uint4(rk[0], rk[kU > 1 ? 1 : 0], rk[kU > 2 ? 2 : 0],
+                                                                 rk[kU > 3 ? 3 : 0]);
+        } else {
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const long long i = idx(u);
+                if (i >= p.n) continue;
+                bin_of[i] = bo[u];
+                if (bo[u] >= 0) rank_of[i] = rk[u];
             }
         }
         // number of (subcell, point) list entries each point creates
@@ -268,23 +295,57 @@ template <int kU>
 __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const int* __restrict__ bin_of,
                               const uint32_t* __restrict__ rank_of, const uint32_t* __restrict__ bin_off,
                               float4* __restrict__ sorted, ClrSrc clr, uint32_t* __restrict__ sorted_clr) {
+    // kU = 4: four consecutive points per thread (16-byte loads of their bins, ranks and
+    // positions); kU = 2, 8: points grid strides apart
+    constexpr bool kConsec = kU == 4;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+    const long long first = kConsec ? 4ll * ((long long)blockIdx.x * blockDim.x + threadIdx.x)
+                                    : (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long step = kConsec ? 4 * stride : kU * stride;
+    for (long long i0 = first; i0 < p.n; i0 += step) {
+        auto idx = [&](int u) { return kConsec ? i0 + u : i0 + u * stride; };
         int b[kU];
         uint32_t rk[kU], off[kU];
         float x[kU], y[kU], z[kU];
+        if (kConsec && i0 + 4 <= p.n) {
+            const int4 bv = *reinterpret_cast<const int4*>(bin_of + i0);
+            const int bb[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
-        for (int u = 0; u < kU; u++) {
-            const long long i = i0 + u * stride;
-            b[u] = i < p.n ? bin_of[i] : -1;
+            for (int u = 0; u < kU; u++) b[u] = bb[u < 4 ? u : 0];
+        } else {
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const long long i = idx(u);
+                b[u] = i < p.n ? bin_of[i] : -1;
+            }
         }
+        if constexpr (kConsec) {
+            const bool any = (b[0] >= 0) | (b[kU > 1 ? 1 : 0] >= 0) | (b[kU > 2 ? 2 : 0] >= 0) | (b[kU > 3 ? 3 : 0] >= 0);
+            if (any) {
+                float raw[4][3];
+                load_pos4(p, i0, raw);
+                uint4 rv = make_uint4(0, 0, 0, 0);
+                if (i0 + 4 <= p.n) rv = *reinterpret_cast<const uint4*>(rank_of + i0);
+                const uint32_t rr[4] = {rv.x, rv.y, rv.z, rv.w};
 #pragma unroll
-        for (int u = 0; u < kU; u++) {
-            const long long i = i0 + u * stride;
-            if (b[u] >= 0) {
-                rk[u] = rank_of[i];
-                off[u] = bin_off[b[u]];
-                load_pos(p.base, i, p.stride, p.off, x[u], y[u], z[u]);
+                for (int u = 0; u < kU; u++) {
+                    if (b[u] < 0) continue;
+                    rk[u] = i0 + 4 <= p.n ? rr[u < 4 ? u : 0] : rank_of[i0 + u];
+                    off[u] = bin_off[b[u]];
+                    x[u] = raw[u < 4 ? u : 0][0];
+                    y[u] = raw[u < 4 ? u : 0][1];
+                    z[u] = raw[u < 4 ? u : 0][2];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const long long i = idx(u);
+                if (b[u] >= 0) {
+                    rk[u] = rank_of[i];
+                    off[u] = bin_off[b[u]];
+                    load_pos(p.base, i, p.stride, p.off, x[u], y[u], z[u]);
+                }
             }
         }
 #pragma unroll
@@ -295,7 +356,7 @@ __global__ void k_bin_scatter(PointSrc p, float3 trans, float R, Quant qz, const
             stored_pos(qz, w, ps);
             sorted[off[u] + rk[u]] = make_float4(ps[0], ps[1], ps[2], __int_as_float(pack_ranges(w, ps, R)));
             if (sorted_clr) {
-                const long long i = i0 + u * stride;
+                const long long i = idx(u);
                 sorted_clr[off[u] + rk[u]] = __ldg(reinterpret_cast<const uint32_t*>(clr.base + i * (long long)clr.stride + clr.off));
             }
         }
@@ -1327,7 +1388,7 @@ void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 
                       const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
                       unsigned long long* totals, int unroll, cudaStream_t s) {
     if (p.n <= 0) return;
-    const unsigned b = gs_blocks(p.n, 256);
+    const unsigned b = unroll == 4 ? gs_blocks((p.n + 3) / 4, 256) : gs_blocks(p.n, 256);
     if (unroll == 1)
         k_bin_count<1><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
     else if (unroll == 4)
@@ -1339,7 +1400,7 @@ void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* b
                         const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, int unroll,
                         cudaStream_t s) {
     if (p.n <= 0) return;
-    const unsigned b = gs_blocks(p.n, 256);
+    const unsigned b = unroll == 4 ? gs_blocks((p.n + 3) / 4, 256) : gs_blocks(p.n, 256);
     uint32_t* sc = clr.base ? sorted_clr : nullptr;
     if (unroll == 2)
         k_bin_scatter<2><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);

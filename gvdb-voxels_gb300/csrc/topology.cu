@@ -296,23 +296,26 @@ struct DirDomain {
     int dim[3];
 };
 
-// kU points per thread per step: their position loads, then their entry loads, are
-// issued together (the pass is bound by the latency of that two-load chain)
+// Four consecutive points per thread per step (load_pos4): their position loads, then
+// their entry loads, are issued together (the pass is bound by the latency of that
+// two-load chain).
 template <int kU>
 __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, int lg, int3 rlo, int3 rhi,
                              DirDomain dd, uint32_t* __restrict__ dirs, int* err) {
+    static_assert(kU == 4, "four consecutive points per thread");
     const int rr = 1 << lg;
     const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < p.n; i0 += kU * stride) {
+    const long long ngroups = (p.n + 3) >> 2;
+    for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < ngroups;
+         gi += (long long)gridDim.x * blockDim.x) {
+        const long long i0 = gi << 2;
         float w[kU][3];
         bool ok[kU];
+        load_pos4(p, i0, w);
 #pragma unroll
         for (int u = 0; u < kU; u++) {
-            const long long i = i0 + u * stride;
-            ok[u] = i < p.n;
+            ok[u] = i0 + u < p.n;
             if (ok[u]) {
-                load_pos(p.base, i, p.stride, p.off, w[u][0], w[u][1], w[u][2]);
                 w[u][0] = fadd(w[u][0], orig.x);
                 w[u][1] = fadd(w[u][1], orig.y);
                 w[u][2] = fadd(w[u][2], orig.z);
@@ -692,11 +695,11 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
                 PointSrc q = p;
                 q.stride = p.stride * 64;
                 q.n = (p.n + 63) / 64;
-                k_touch_dirs<4><<<grid_stride_blocks(q.n, 256), 256, 0, s>>>(q, orig, radius, hr, t.lgrange[0], rlo,
-                                                                             rhi, dd, dirs, err);
+                k_touch_dirs<4><<<grid_stride_blocks((q.n + 3) / 4, 256), 256, 0, s>>>(q, orig, radius, hr, t.lgrange[0],
+                                                                                       rlo, rhi, dd, dirs, err);
             }
-            k_touch_dirs<4><<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi,
-                                                                         dd, dirs, err);
+            k_touch_dirs<4><<<grid_stride_blocks((p.n + 3) / 4, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo,
+                                                                                   rhi, dd, dirs, err);
         }
         const long long nw = (dom.d[0].nbits + 31) >> 5;
         k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);

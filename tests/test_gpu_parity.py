@@ -55,6 +55,18 @@ def test_fluid_frames_levelset(gpu_lib, touch_dirs):
         _full_check(o[k], g[k], 3.0)
 
 
+@pytest.mark.parametrize("unroll", [(1, 2), (2, 8), (4, 4)])
+def test_binning_variants(gpu_lib, unroll):
+    """every points-per-thread form of the binning passes (the tuning table's choices),
+    on a point count that is not a multiple of four (the four-point forms' tail)"""
+    pos, vel = _mini_fluid(n=40003, seed=71)
+    frames = [(pos + 0.5 * (k + 1) * vel).astype(np.float32) for k in range(3)]
+    _, o = H.run_oracle(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    _, g = H.run_gpu(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0, unroll=unroll)
+    for k in range(len(frames)):
+        _full_check(o[k], g[k], 3.0)
+
+
 @pytest.mark.parametrize("dense_min", [0, 2**31 - 1])
 @pytest.mark.parametrize("mode,rho", [("levelset", 2.0), ("density", 1.0), ("density", 2.5)])
 def test_gather_forms(gpu_lib, dense_min, mode, rho):
