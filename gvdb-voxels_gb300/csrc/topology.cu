@@ -357,9 +357,12 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
             }
             ent[u] = ((long long)rx * dd.dim[1] + ry) * dd.dim[2] + rz;
         }
+        // the entries of a dense region are few and hot: read them through L1 (a copy from
+        // before another point's atomic only makes this point repeat a bit: the OR is
+        // idempotent, so the table ends the same)
         uint32_t cur[kU];
 #pragma unroll
-        for (int u = 0; u < kU; u++) cur[u] = ent[u] >= 0 ? __ldcg(dirs + ent[u]) : 0xFFFFFFFFu;
+        for (int u = 0; u < kU; u++) cur[u] = ent[u] >= 0 ? __ldca(dirs + ent[u]) : 0xFFFFFFFFu;
 #pragma unroll
         for (int u = 0; u < kU; u++)
             if (ent[u] >= 0 && (cur[u] & m27[u]) != m27[u]) atomicOr(dirs + ent[u], m27[u]);
