@@ -475,6 +475,60 @@ def bench_surface(args, steps=5):
     return out
 
 
+def bench_sparse_jobs(args, reps=20):
+    """RebuildTopology cost of sparse jobs, per key-set form (TUNE_KEYSET 1: level bitmaps
+    over the points' key domain, 2: hash tables of the keys + radix sort).  Small job:
+    10,000 sphere-surface points in 4096^3 (seed 5, grid (4,4,3,4), r = 1.5), a full
+    rebuild per call.  Far clusters: 3 x 100,000 points in 80^3 boxes at far corners of a
+    65,536^3 root (grid (3,3,3,3,4), r = 2): beyond the bitmaps' 2^34 positions, so only
+    the tables.  Wall time per call (host readbacks included), after 3 warm-up calls."""
+    import time
+
+    import datasets
+    import torch
+
+    import gbvdb
+
+    def clusters(n_each, seed):
+        rng = np.random.default_rng(seed)
+        cs = ((60, 70, 80), (65300, 200, 32000), (31000, 65250, 65300))
+        return np.concatenate([np.asarray(c, np.float32) + rng.uniform(-40, 40, (n_each, 3)).astype(np.float32)
+                               for c in cs]).astype(np.float32)
+
+    surf = datasets.surface(10_000, seed=5)
+    surf = surf[np.all(surf >= 0, axis=1)]
+    jobs = [("small_job_4096", surf, (4, 4, 3, 4), 1.5, (1, 2)),
+            ("far_clusters_65536", clusters(100_000, 6), (3, 3, 3, 3, 4), 2.0, (0,))]
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, pts, dims, r, modes in jobs:
+        d = torch.from_numpy(np.ascontiguousarray(pts)).cuda()
+        res = {"points": int(pts.shape[0]), "grid_log2dims": list(dims), "radius": r}
+        for m in modes:
+            g = gbvdb.Grid(0, dims, stream=stream)
+            g.set_tuning(gbvdb.TUNE_KEYSET, m)
+            g.add_channel(0)
+            n = g.set_points(d)
+            ts = []
+            for k in range(3 + reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                g.request_full_rebuild(True)
+                g.rebuild_topology(n, r)
+                torch.cuda.synchronize()
+                if k >= 3:
+                    ts.append((time.perf_counter() - t0) * 1000.0)
+            tot, used = g.node_counts()
+            res[{0: "auto", 1: "bitmaps", 2: "tables"}[m]] = {
+                "rebuild_ms_median": float(np.median(ts)), "rebuild_ms_min": float(np.min(ts)),
+                "leaves": int(tot[0]), "hashed_key_passes": g.stats()["hashed_key_passes"]}
+            g.close()
+        out[name] = res
+        del d
+    torch.cuda.empty_cache()
+    return out
+
+
 def bench_batched(args):
     """Batched uneven grids: `count` clouds (seed 3, sizes log-uniform in [1e4, 2e6], shell or
     sphere-surface generator, grid (3,3,3,4), density rho = r = R = 1, FP32) submitted at once
@@ -732,6 +786,8 @@ def bench_ours(args):
         line["config"]["workload"] = line["config"]["workload"].replace("4,194,304", "{:,}".format(npts))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(pos, vel)
+    if rank == 0 and world == 1 and not args.no_sparse:
+        line["sparse_jobs"] = bench_sparse_jobs(args)
     if rank == 0 and world == 1 and not args.no_surface:
         grid.close()
         frames.clear()
@@ -776,6 +832,7 @@ def main():
                     help="particles per fluid frame (default: the workload's 4,194,304; smaller for profiling)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form stream")
     ap.add_argument("--no-surface", action="store_true", help="skip the 16.8M-point surface workload")
+    ap.add_argument("--no-sparse", action="store_true", help="skip the sparse-job rebuild timings")
     ap.add_argument("--serve-requests", type=int, default=10_000)
     ap.add_argument("--serve-seconds", type=float, default=8.0,
                     help="paced rates run the stream's first rate * serve_seconds requests")

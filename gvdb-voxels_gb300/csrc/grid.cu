@@ -221,6 +221,15 @@ struct gbvdb_grid_s {
     DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     DevBuf touch_dirs;          // per home leaf position: the directions its points' boxes cover
     bool touch_dirs_on = true;  // GBVDB_TUNE_TOUCH_DIRS
+    // sparse key sets (hash tables of key bits) for domains too large or too sparse for
+    // the bitmaps: the new-key and touched tables, the sorted keys and the sort's
+    // scratch, the compaction counter and level bounds (kmeta)
+    DevBuf khash, thash, ksorted, kalt, ksort_tmp, kmeta;
+    long long khash_cap = 0, thash_cap = 0;
+    int keyset_mode = 0;                         // GBVDB_TUNE_KEYSET
+    bool hashed = false;                         // the key sets of the current pass
+    unsigned long long* sorted_keys = nullptr;   // sparse form: the counted pass's keys, ascending
+    long long n_hashed_passes = 0;
     unsigned char* pinned = nullptr;
 
     // ActivateSpace / RebuildTopologyCPU: host copies of the pools (fetched from the
@@ -624,6 +633,47 @@ struct gbvdb_grid_s {
         return at;
     }
 
+    // The sparse form's count: the new-key table compacted and sorted (ascending key =
+    // the bitmap's bit order), per-level bounds by binary search; *overflow when a table
+    // ran out of probes (nothing counted: the caller grows the tables and runs the pass
+    // again).  Two readbacks.
+    std::vector<uint32_t> count_hashed(int depth, const KeyDomains& kd, long long total_bits, bool* overflow) {
+        grow(kmeta, 256);
+        unsigned int* cnt = ptr<unsigned int>(kmeta);
+        unsigned int* at_d = cnt + 16;
+        check(cudaMemsetAsync(cnt, 0, 4, stream), "key count clear");
+        grow(ksorted, (size_t)khash_cap * 8);
+        const KeyHash kh{ptr<unsigned long long>(khash), (unsigned long long)khash_cap - 1};
+        launch_hash_compact(kh, ptr<unsigned long long>(ksorted), cnt, stream);
+        check_launch("hash compact");
+        check(cudaMemcpyAsync(pinned, cnt, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        check(cudaMemcpyAsync(pinned + 4, ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        n_readback++;
+        sync();
+        unsigned int n = 0;
+        int errflag = 0;
+        memcpy(&n, pinned, 4);
+        memcpy(&errflag, pinned + 4, 4);
+        if (errflag & 2)
+            throw StatusError{GBVDB_INVALID_ARG, "a point's activation box spans more than 2^26 nodes of one level"};
+        if (errflag & 1) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
+        *overflow = (errflag & 4) != 0;
+        if (*overflow) return {};
+        int bits = 1;
+        while (bits < 63 && (1ll << bits) < total_bits) bits++;
+        grow(kalt, (size_t)std::max<long long>(n, 1) * 8);
+        grow(ksort_tmp, sort_tmp_bytes(n));
+        sorted_keys = sort_keys_u64(ptr<unsigned long long>(ksorted), ptr<unsigned long long>(kalt), n, bits,
+                                    ksort_tmp.p, stream);
+        check_launch("key sort");
+        launch_key_bounds(sorted_keys, cnt, kd, depth, at_d, stream);
+        check_launch("key bounds");
+        std::vector<uint32_t> at(depth + 1);
+        readback(at.data(), at_d, 4 * (size_t)(depth + 1));
+        n_hashed_passes++;
+        return at;
+    }
+
     // append the nodes of the counted pass to the pools in ascending key order
     long long allocate_counted(int depth, const KeyDomains& kd, const std::vector<uint32_t>& at) {
         long long added = 0;
@@ -640,10 +690,15 @@ struct gbvdb_grid_s {
             if (cnt <= 0) continue;
             long long base = ncnt[l];
             ensure_pool(l, base + cnt);
-            long long w0 = kd.d[l].bitbase / 32;
-            long long nw = ((kd.d[l].nbits + 31) / 32);
-            launch_alloc_nodes(ptr<uint32_t>(bitmap), ptr<uint32_t>(pscan), w0, nw, l, lgrange[l], kd.d[l], base,
-                               ptr<Node>(nodes[l]), stream);
+            if (hashed) {
+                launch_alloc_nodes_sorted(sorted_keys, at[l], cnt, l, lgrange[l], kd.d[l], base, ptr<Node>(nodes[l]),
+                                          stream);
+            } else {
+                long long w0 = kd.d[l].bitbase / 32;
+                long long nw = ((kd.d[l].nbits + 31) / 32);
+                launch_alloc_nodes(ptr<uint32_t>(bitmap), ptr<uint32_t>(pscan), w0, nw, l, lgrange[l], kd.d[l], base,
+                                   ptr<Node>(nodes[l]), stream);
+            }
             check_launch("alloc_nodes");
             if (l >= 1)
                 check(cudaMemsetAsync(ptr<unsigned long long>(clist[l]) + base * cl_len(l), 0xFF,
@@ -656,8 +711,50 @@ struct gbvdb_grid_s {
         return added;
     }
 
-    long long allocate_from_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
-        return allocate_counted(depth, kd, count_bitmap(depth, kd, total_bits));
+    // One key pass: clears the key sets of the pass's form, runs gen (the launches that
+    // fill them) and counts the keys; in the sparse form a table that ran out of probes
+    // is grown fourfold and the pass runs again (its launches only add keys and set leaf
+    // markers, so a repeat gives the same sets).  est_keys / est_touched: expected set sizes.
+    template <class Gen>
+    std::vector<uint32_t> key_pass(int depth, const KeyDomains& kd, long long bits, long long est_keys,
+                                   long long est_touched, Gen gen) {
+        for (int attempt = 0;; attempt++) {
+            if (hashed) {
+                clear_hash(khash, khash_cap, std::min(est_keys, bits));
+                clear_hash(thash, thash_cap, std::min(est_touched, bits));
+                grow(misc, 256);
+                check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
+            } else {
+                clear_bitmap(bits);
+            }
+            gen(key_sets());
+            if (!hashed) return count_bitmap(depth, kd, bits);
+            bool overflow = false;
+            std::vector<uint32_t> at = count_hashed(depth, kd, bits, &overflow);
+            if (!overflow) return at;
+            if (attempt >= 6) throw StatusError{GBVDB_CAPACITY, "key table overflow"};
+            est_keys *= 4;
+            est_touched *= 4;
+        }
+    }
+    void clear_hash(DevBuf& b, long long& cap, long long want) {
+        long long c = 1024;  // a multiple of 32 (k_hash_compact), load at most one half
+        while (c < 2 * want) c <<= 1;
+        cap = c;
+        grow(b, (size_t)c * 8);
+        check(cudaMemsetAsync(b.p, 0xFF, (size_t)c * 8, stream), "key table clear");
+    }
+    KeySets key_sets() {
+        if (!hashed) return KeySets{{nullptr, 0}, {nullptr, 0}};
+        return KeySets{{ptr<unsigned long long>(khash), (unsigned long long)khash_cap - 1},
+                       {ptr<unsigned long long>(thash), (unsigned long long)thash_cap - 1}};
+    }
+    // Key-set form of a pass over a domain of `bits` key bits: the level bitmaps up to
+    // kMaxBits, hash tables beyond (GBVDB_TUNE_KEYSET: 1 bitmaps while they fit, 2 always
+    // the tables).
+    bool choose_hashed(long long bits) const {
+        if (keyset_mode == 2) return true;
+        return bits > kMaxBits;
     }
 
     // rebuild the dense leaf lookup after a topology change (exact: built by traversal)
@@ -728,29 +825,32 @@ struct gbvdb_grid_s {
         long long bits = 0;
         float margin = 2.0f * std::max(radius, 0.0f) + 4.0f;
         KeyDomains kd = domains(D, margin, rpos, D, &bits);
-        if (bits > kMaxBits) throw StatusError{GBVDB_NOT_SUPPORTED, "point extent too sparse for the key bitmap"};
+        hashed = choose_hashed(bits);
         PointSrc p = pts;
         p.n = n;
         // pass 1 (ActivateBricksGPU, VG.cpp:1229-1413)
-        clear_bitmap(bits);
         TreeView t = view();
-        launch_keys_pass1(t, p, orig, D, kd, ptr<uint32_t>(bitmap), ptr<int>(misc) + 8, stream);
-        check_launch("keys_pass1");
-        allocate_from_bitmap(D, kd, bits);
+        std::vector<uint32_t> at = key_pass(D, kd, bits, n * D, 0, [&](const KeySets& ks) {
+            launch_keys_pass1(t, p, orig, D, kd, ptr<uint32_t>(bitmap), ks, ptr<int>(misc) + 8, stream);
+            check_launch("keys_pass1");
+        });
+        allocate_counted(D, kd, at);
         mark();
         link_all(D);
         build_leaf_grid();
         mark();
         // pass 2 (ActivateExtraBricksGPU, VG.cpp:931-1016), only if radius >= 1 (VG.cpp:1207)
         if (radius >= 1) {
-            clear_bitmap(bits);
             t = view();
             int rlo[3], rhi[3];
             for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
-            launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
-                            nullptr, ptr<int>(misc) + 8, touch_dirs_buf(kd), stream);
-            check_launch("keys_extra");
-            if (allocate_from_bitmap(D, kd, bits) > 0) {
+            at = key_pass(D, kd, bits, (long long)at[(size_t)D] + 1024, 4 * n + 1024, [&](const KeySets& ks) {
+                launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(touched),
+                                ptr<uint32_t>(bitmap), nullptr, ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd),
+                                ks, stream);
+                check_launch("keys_extra");
+            });
+            if (allocate_counted(D, kd, at) > 0) {
                 mark();
                 link_all(D);
                 build_leaf_grid();
@@ -769,18 +869,18 @@ struct gbvdb_grid_s {
         float margin = 2.0f * std::max(radius, 0.0f) + 4.0f;
         int rl = root_lev >= 0 ? root_lev : D;
         KeyDomains kd = domains(D, margin, root_pos, rl, &bits);
-        if (bits > kMaxBits) throw StatusError{GBVDB_NOT_SUPPORTED, "point extent too sparse for the key bitmap"};
-        clear_bitmap(bits);
+        hashed = choose_hashed(bits);
         PointSrc p = pts;
         p.n = n;
         TreeView t = view();
         int rlo[3], rhi[3];
         for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
-        launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
-                        ptr<int>(markers), ptr<int>(misc) + 8, touch_dirs_buf(kd), stream);
-        check_launch("keys_incr");
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
-        std::vector<uint32_t> at = count_bitmap(D, kd, bits);
+        std::vector<uint32_t> at = key_pass(D, kd, bits, nleaf / 4 + 1024, 4 * n + 1024, [&](const KeySets& ks) {
+            launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
+                            ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, stream);
+            check_launch("keys_incr");
+        });
         mark();
         if (at[(size_t)D] == 0) return;
         launch_apply_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), stream);
@@ -1671,7 +1771,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
                       &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab, &g->sorted_clr,
-                      &g->list_clr};
+                      &g->list_clr, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp, &g->kmeta};
     g->join_side();
     for (DevBuf* b : bufs) g->release(*b);
     for (int l = 0; l < kMaxLev; l++) { g->release(g->nodes[l]); g->release(g->clist[l]); }
@@ -2273,6 +2373,11 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
         g->touch_dirs_on = value != 0;
         return GBVDB_OK;
     }
+    if (param == GBVDB_TUNE_KEYSET) {
+        if (value < 0 || value > 2) return GBVDB_INVALID_ARG;
+        g->keyset_mode = (int)value;
+        return GBVDB_OK;
+    }
     if (param == GBVDB_TUNE_TABLE) {
         if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
         g->table_on = value != 0;
@@ -2317,6 +2422,15 @@ gbvdb_status gbvdb_get_stats(gbvdb_grid g, int64_t* out4) {
     GBVDB_END(g)
 }
 
+gbvdb_status gbvdb_get_stats_ex(gbvdb_grid g, int64_t* out, int cap) {
+    GBVDB_GUARD_NOJOIN(g)
+    if (!out || cap < 0) return GBVDB_INVALID_ARG;
+    const int64_t v[5] = {g->n_launch, g->n_readback, g->sc_len, g->sc_nbricks, g->n_hashed_passes};
+    for (int i = 0; i < cap && i < 5; i++) out[i] = v[i];
+    return GBVDB_OK;
+    GBVDB_END(g)
+}
+
 // device bytes held by the grid's buffers (pools, atlas, scratch): the server's memory accounting
 size_t gbvdb_internal_device_bytes(gbvdb_grid g);
 gbvdb_status gbvdb_get_device_bytes(gbvdb_grid g, int64_t* out) {
@@ -2335,7 +2449,8 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
                             &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
-                            &g->nbmask, &g->gtab};
+                            &g->nbmask, &g->gtab, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp,
+                            &g->kmeta};
     for (const DevBuf* d : bufs) b += d->cap;
     for (int l = 0; l < kMaxLev; l++) b += g->nodes[l].cap + g->clist[l].cap;
     for (int c = 0; c < 8; c++) b += g->ch[c].interior.cap + g->ch[c].apron_buf.cap;

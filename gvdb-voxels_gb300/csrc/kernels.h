@@ -20,6 +20,21 @@ struct KeyDomains {
     KeyDomain d[kMaxLev];
 };
 
+// Sparse form of a key set: an open-addressing table of the set's bit indices (the
+// positions the level bitmaps would hold, bitbase included), for key domains too
+// large or too sparse for bitmaps.  Free slots hold kKeyEmpty; tab == null: the
+// bitmap form.
+constexpr unsigned long long kKeyEmpty = ~0ull;
+struct KeyHash {
+    unsigned long long* tab;
+    unsigned long long mask;  // capacity - 1, capacity a power of two
+};
+// the two sets of a pass in the sparse form: new node keys, touched box positions
+struct KeySets {
+    KeyHash keys;
+    KeyHash touched;
+};
+
 struct PointSrc {
     const char* base;
     long long n;
@@ -59,18 +74,36 @@ __device__ __forceinline__ void load_pos4(const PointSrc& p, long long i0, float
 size_t scan_tmp_bytes(long long n);
 // exclusive scan of n u32 into out[0..n]; out[n] = total.  tmp: scan_tmp_bytes(n) bytes
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+// ascending sort of n distinct u64 keys, each below 2^bits (LSD radix sort, 8-bit digits;
+// one block for n <= kSortSmall); keys and alt hold n each; returns the one of the two
+// that holds the result.  tmp: sort_tmp_bytes(n) bytes
+constexpr long long kSortSmall = 4096;
+size_t sort_tmp_bytes(long long n);
+unsigned long long* sort_keys_u64(unsigned long long* keys, unsigned long long* alt, long long n, int bits, void* tmp,
+                                  cudaStream_t s);
 
 // ---- topology.cu
 void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s);
+// ks.keys.tab set: keys go to the table instead of the bitmap (err bit 4: table full)
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
-                       uint32_t* bitmap, int* err, cudaStream_t s);
+                       uint32_t* bitmap, const KeySets& ks, int* err, cudaStream_t s);
 // touched: scratch bitmap with the layout of `bitmap`, cleared by the caller; dirs (or null):
 // scratch of touch_dirs_words(dom) words for the direction-set form (boxes within one node
 // of the home node), cleared by the launcher
 long long touch_dirs_words(const KeyDomains& dom);
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
-                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, cudaStream_t s);
+                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, const KeySets& ks,
+                     cudaStream_t s);
+// sparse form: the occupied slots of h into out (any order), their number into *count
+// (cleared by the caller)
+void launch_hash_compact(const KeyHash& h, unsigned long long* out, unsigned int* count, cudaStream_t s);
+// at[l] = keys of sorted[0..n) below dom.d[l].bitbase (l < depth), at[depth] = n
+void launch_key_bounds(const unsigned long long* sorted, const unsigned int* n, const KeyDomains& dom, int depth,
+                       unsigned int* at, cudaStream_t s);
+// the nodes of level lev from sorted keys [first, first + count) at pool index base + rank
+void launch_alloc_nodes_sorted(const unsigned long long* sorted, long long first, long long count, int lev,
+                               int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s);
 void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s);

@@ -2,6 +2,12 @@
 // 3-level prefixSum/prefixFixup, cuda_gvdb_particles.cuh:856-902, VG.cpp:4760-4819).
 // Reduce-then-scan: per-tile sums, a recursive scan of the tile sums, then a
 // tile-local scan that adds the tile's offset.  Tiles of 4096 elements.
+//
+// Also the ascending sort of distinct u64 keys that the sparse key sets of
+// RebuildTopology use in place of the reference's Thrust sort of brick keys
+// (gvdb_cutils.cu:11-16): least-significant-digit radix sort, 8-bit digits, each
+// pass a per-tile digit histogram, an exclusive scan of the histograms (digit-major,
+// so every digit's tiles follow each other), and a stable scatter.
 #include "kernels.h"
 
 namespace gbvdb {
@@ -74,6 +80,92 @@ __global__ void k_tile_scan(const uint32_t* __restrict__ in, long long n, const 
     // out[n] = total, written by the thread owning the last element
     if (base <= n - 1 && n - 1 < base + kItems) out[n] = run;
 }
+
+// ---- radix sort of u64 keys
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 8;
+constexpr int kSortTile = kSortThreads * kSortRounds;
+constexpr int kSortWarps = kSortThreads / 32;
+
+// hist[digit * tiles + tile] = keys of the tile with that digit
+__global__ void __launch_bounds__(kSortThreads) k_digit_hist(const unsigned long long* __restrict__ keys, long long n,
+                                                             int shift, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kSortTile;
+#pragma unroll
+    for (int r = 0; r < kSortRounds; r++) {
+        const long long i = base + (long long)r * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(unsigned)(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(long long)threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile: the tile's keys are taken in index order, a block-wide
+// round of 256 at a time; within a round a key's place among the keys of its digit is
+// its rank among its warp's peers (match_any) plus the counts of the lower warps.
+__global__ void __launch_bounds__(kSortThreads) k_digit_scatter(const unsigned long long* __restrict__ in,
+                                                                unsigned long long* __restrict__ out, long long n,
+                                                                int shift, const uint32_t* __restrict__ offs) {
+    __shared__ uint32_t run[256];
+    __shared__ uint32_t wcnt[kSortWarps][256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    run[threadIdx.x] = offs[(long long)threadIdx.x * gridDim.x + blockIdx.x];
+    for (int w = 0; w < kSortWarps; w++) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kSortTile;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = 0; r < kSortRounds; r++) {
+        const long long i = base + (long long)r * kSortThreads + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned long long k = valid ? in[i] : 0ull;
+        const unsigned d = valid ? ((unsigned)(k >> shift) & 255u) : 256u;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const unsigned rank = __popc(peers & lt);
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            unsigned pos = run[d] + rank;
+            for (int w = 0; w < warp; w++) pos += wcnt[w][d];
+            out[pos] = k;
+        }
+        __syncthreads();
+        uint32_t tot = 0;
+        for (int w = 0; w < kSortWarps; w++) {
+            tot += wcnt[w][threadIdx.x];
+            wcnt[w][threadIdx.x] = 0;
+        }
+        run[threadIdx.x] += tot;
+        __syncthreads();
+    }
+}
+
+// up to kSortSmall keys: bitonic sort in shared memory, padded with kKeyEmpty (above
+// every key)
+__global__ void __launch_bounds__(1024) k_sort_small(unsigned long long* keys, int n) {
+    __shared__ unsigned long long v[kSortSmall];
+    int m = 1;
+    while (m < n) m <<= 1;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) v[i] = i < n ? keys[i] : kKeyEmpty;
+    __syncthreads();
+    for (int k = 2; k <= m; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = v[i], b = v[l];
+                    if ((a > b) == ((i & k) == 0)) {
+                        v[i] = b;
+                        v[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) keys[i] = v[i];
+}
 }  // namespace
 
 static long long ntiles(long long n) { return (n + kTile - 1) / kTile; }
@@ -106,6 +198,38 @@ void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tm
     k_tile_sums<<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
     scan_exclusive_u32(sums, offs, t, rest, s);
     k_tile_scan<<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
+}
+
+static long long sort_tiles(long long n) { return (n + kSortTile - 1) / kSortTile; }
+
+size_t sort_tmp_bytes(long long n) {
+    if (n <= kSortSmall) return 256;
+    const long long h = 256 * sort_tiles(n);
+    return (size_t)(2 * h + 1) * sizeof(uint32_t) + 256 + scan_tmp_bytes(h);
+}
+
+unsigned long long* sort_keys_u64(unsigned long long* keys, unsigned long long* alt, long long n, int bits, void* tmp,
+                                  cudaStream_t s) {
+    if (n <= 1) return keys;
+    if (n <= kSortSmall) {
+        k_sort_small<<<1, 1024, 0, s>>>(keys, (int)n);
+        return keys;
+    }
+    const long long t = sort_tiles(n), h = 256 * t;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(tmp);
+    uint32_t* offs = hist + h;
+    char* rest = reinterpret_cast<char*>(offs + h + 1);
+    rest = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(rest) + 255) & ~uintptr_t(255));
+    unsigned long long *src = keys, *dst = alt;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_digit_hist<<<(unsigned)t, kSortThreads, 0, s>>>(src, n, shift, hist);
+        scan_exclusive_u32(hist, offs, h, rest, s);
+        k_digit_scatter<<<(unsigned)t, kSortThreads, 0, s>>>(src, dst, n, shift, offs);
+        unsigned long long* x = src;
+        src = dst;
+        dst = x;
+    }
+    return src;
 }
 
 }  // namespace gbvdb

@@ -109,13 +109,51 @@ __device__ __forceinline__ long long key_bit(const KeyDomain& d, int x, int y, i
     return d.bitbase + ((long long)rx * d.dim[1] + ry) * d.dim[2] + rz;
 }
 
+// ---- sparse key sets (KeyHash): linear probing over a power-of-two table; a key is
+// inserted once (compare-and-swap into a free slot).  A probe run longer than
+// kKeyProbes (the table too full) sets err bit 4 and the host grows the table and runs
+// the pass again.
+constexpr int kKeyProbes = 512;
+
+// splitmix64 finaliser (Steele, Lea and Flood, "Fast splittable pseudorandom number
+// generators", 2014): spreads the x-major bit indices of a box over the table
+__device__ __forceinline__ unsigned long long key_mix(unsigned long long x) {
+    x ^= x >> 30;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 27;
+    x *= 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ void hash_insert(const KeyHash& h, unsigned long long key, int* err) {
+    unsigned long long s = key_mix(key) & h.mask;
+    for (int probe = 0; probe < kKeyProbes; probe++) {
+        unsigned long long cur = __ldcg(h.tab + s);
+        if (cur == key) return;
+        if (cur == kKeyEmpty) {
+            cur = atomicCAS(h.tab + s, kKeyEmpty, key);
+            if (cur == kKeyEmpty || cur == key) return;
+        }
+        s = (s + 1) & h.mask;
+    }
+    atomicOr(err, 4);
+}
+
+// node coordinates (relative to the domain) of the level's local bit index li
+__device__ __forceinline__ void key_coords(const KeyDomain& d, long long li, int& rx, int& ry, int& rz) {
+    rz = (int)(li % d.dim[2]);
+    const long long q = li / d.dim[2];
+    ry = (int)(q % d.dim[1]);
+    rx = (int)(q / d.dim[1]);
+}
+
 // gvdbCalcBrickId (PT.cuh:352-382): key of every level below the root for every
 // point whose coordinates are all >= 0 (bits collected per block in shared memory
 // when the bitmap fits, as for the box keys below)
 __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom, TreeView tv, uint32_t* bm,
-                             long long nwords, int* err) {
+                             long long nwords, KeyHash kh, int* err) {
     extern __shared__ uint32_t sbm[];
-    const bool use_smem = nwords <= 8192;
+    const bool use_smem = kh.tab == nullptr && nwords <= 8192;
     if (use_smem) {
         for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
         __syncthreads();
@@ -129,7 +167,9 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
             int lg = tv.lgrange[lev];
             long long b = key_bit(dom.d[lev], cover_coord(w0, lg), cover_coord(w1, lg), cover_coord(w2, lg));
             if (b < 0) { atomicOr(err, 1); continue; }
-            if (use_smem) {
+            if (kh.tab) {
+                hash_insert(kh, (unsigned long long)b, err);
+            } else if (use_smem) {
                 uint32_t bit = 1u << (b & 31);
                 if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
             } else {
@@ -178,9 +218,9 @@ __device__ __forceinline__ int trunc_mult(int x, int lg) {
 }
 
 __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, int hi_mul, int depth, int3 rlo,
-                            int3 rhi, KeyDomains dom, uint32_t* touched, long long nwords, int* err) {
+                            int3 rhi, KeyDomains dom, uint32_t* touched, long long nwords, KeyHash th, int* err) {
     extern __shared__ uint32_t sbm[];
-    const bool use_smem = nwords <= kTouchSmemWords;
+    const bool use_smem = th.tab == nullptr && nwords <= kTouchSmemWords;
     if (use_smem) {
         for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
         __syncthreads();
@@ -269,7 +309,8 @@ __global__ void k_touch_box(TreeView t, PointSrc p, float3 orig, float radius, i
                 if (nx < rlo.x || ny < rlo.y || nz < rlo.z || nx >= rhi.x || ny >= rhi.y || nz >= rhi.z) continue;
                 long long b = key_bit(dom.d[lev], nx >> lg, ny >> lg, nz >> lg);
                 if (b < 0) { atomicOr(err, 1); continue; }
-                touch_bit(sbm, use_smem, touched, b);
+                if (th.tab) hash_insert(th, (unsigned long long)b, err);
+                else touch_bit(sbm, use_smem, touched, b);
             }
         }
     }
@@ -466,9 +507,110 @@ __global__ void k_resolve_touched(TreeView t, LeafGrid lg, int lev, KeyDomain d,
     if (b == 0 && m) keys[w0 + w] = m;  // each word has one owner warp
 }
 
+// k_touch_up over the sparse form: a thread per table slot; the level-(lev-1)
+// entries insert their parents (entries this launch adds are of level lev and skipped)
+__global__ void k_touch_up_hashed(KeyHash th, KeyDomain child, KeyDomain parent, int lgres, int* err) {
+    const unsigned long long cap = th.mask + 1;
+    const unsigned long long lo = (unsigned long long)child.bitbase, hi = lo + (unsigned long long)child.nbits;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cap;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long e = __ldcg(th.tab + s);
+        if (e == kKeyEmpty || e < lo || e >= hi) continue;
+        int rx, ry, rz;
+        key_coords(child, (long long)(e - lo), rx, ry, rz);
+        const long long pb = key_bit(parent, (child.lo[0] + rx) >> lgres, (child.lo[1] + ry) >> lgres,
+                                     (child.lo[2] + rz) >> lgres);
+        if (pb < 0) atomicOr(err, 1);
+        else hash_insert(th, (unsigned long long)pb, err);
+    }
+}
+
+// k_resolve_touched over the sparse form, all levels in one launch: a thread per
+// touched-table slot; missing -> key, reachable leaf -> marker
+__global__ void k_resolve_hashed(TreeView t, LeafGrid lg, int depth, KeyDomains dom, KeyHash th, KeyHash kh,
+                                 int* markers, int* err) {
+    const unsigned long long cap = th.mask + 1;
+    for (unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; s < cap;
+         s += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long e = th.tab[s];
+        if (e == kKeyEmpty) continue;
+        int lev = -1;
+        for (int l = 0; l < depth; l++)
+            if (e >= (unsigned long long)dom.d[l].bitbase &&
+                e < (unsigned long long)(dom.d[l].bitbase + dom.d[l].nbits))
+                lev = l;
+        if (lev < 0) continue;
+        const KeyDomain& d = dom.d[lev];
+        int rx, ry, rz;
+        key_coords(d, (long long)e - d.bitbase, rx, ry, rz);
+        const int lgr = t.lgrange[lev];
+        const int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
+        const long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
+        if (pid < 0) hash_insert(kh, e, err);
+        else if (lev == 0 && markers) markers[pid] = 1;
+    }
+}
+
+// occupied slots -> out (warp-aggregated append; the table's capacity is a multiple of 32)
+__global__ void k_hash_compact(KeyHash h, unsigned long long* __restrict__ out, unsigned int* count) {
+    const unsigned long long cap = h.mask + 1;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long nw = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    for (unsigned long long w = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 32 < cap;
+         w += nw) {
+        const unsigned long long e = h.tab[w * 32 + lane];
+        const bool occ = e != kKeyEmpty;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, occ);
+        if (!m) continue;
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(count, (unsigned)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (occ) out[base + __popc(m & ((1u << lane) - 1u))] = e;
+    }
+}
+
+__global__ void k_key_bounds(const unsigned long long* __restrict__ sorted, const unsigned int* n, KeyDomains dom,
+                             int depth, unsigned int* at) {
+    const int l = threadIdx.x;
+    if (l > depth) return;
+    const unsigned int cnt = *n;
+    if (l == depth) {
+        at[l] = cnt;
+        return;
+    }
+    const unsigned long long key = (unsigned long long)dom.d[l].bitbase;
+    unsigned int lo = 0, hi = cnt;  // first index with sorted[i] >= key
+    while (lo < hi) {
+        const unsigned int mid = lo + ((hi - lo) >> 1);
+        if (sorted[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    at[l] = lo;
+}
+
 __global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32_t* __restrict__ cnt) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += (long long)gridDim.x * blockDim.x)
         cnt[i] = __popc(bm[i]);
+}
+
+// the node record of local key li of level lev (SetupNode, VG.cpp:2512-2524) at pool index idx
+__device__ __forceinline__ Node key_node(int lev, int lgrange, const KeyDomain& d, long long li, long long idx) {
+    int rx, ry, rz;
+    key_coords(d, li, rx, ry, rz);
+    Node n;
+    n.lev = (uint8_t)lev;
+    n.flags = 1;
+    n.prio = 0;
+    n.pad = 0;
+    n.pos[0] = (d.lo[0] + rx) << lgrange;
+    n.pos[1] = (d.lo[1] + ry) << lgrange;
+    n.pos[2] = (d.lo[2] + rz) << lgrange;
+    n.value[0] = n.value[1] = n.value[2] = -1;
+    n.vrange[0] = n.vrange[1] = n.vrange[2] = 0.f;
+    n.parent = kUndefL;
+    n.childlist = lev > 0 ? elem(1, lev, (unsigned long long)idx) : kUndefL;
+    n.mask = 0;
+    return n;
 }
 
 // one thread per bitmap word of one level; every set bit becomes a node record
@@ -484,25 +626,16 @@ __global__ void k_alloc_nodes(const uint32_t* __restrict__ bm, const uint32_t* _
     if (!((bits >> b) & 1u)) return;
     const long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0] + __popc(bits & ((1u << b) - 1u));
     const long long li = (word0 + w) * 32 + b - d.bitbase;  // bitbase is word aligned
-    const int rz = (int)(li % d.dim[2]);
-    const long long q = li / d.dim[2];
-    const int ry = (int)(q % d.dim[1]);
-    const int rx = (int)(q / d.dim[1]);
-    const long long idx = base + rank;
-    Node n;
-    n.lev = (uint8_t)lev;
-    n.flags = 1;
-    n.prio = 0;
-    n.pad = 0;
-    n.pos[0] = (d.lo[0] + rx) << lgrange;
-    n.pos[1] = (d.lo[1] + ry) << lgrange;
-    n.pos[2] = (d.lo[2] + rz) << lgrange;
-    n.value[0] = n.value[1] = n.value[2] = -1;
-    n.vrange[0] = n.vrange[1] = n.vrange[2] = 0.f;
-    n.parent = kUndefL;
-    n.childlist = lev > 0 ? elem(1, lev, (unsigned long long)idx) : kUndefL;
-    n.mask = 0;
-    nodes[idx] = n;
+    nodes[base + rank] = key_node(lev, lgrange, d, li, base + rank);
+}
+
+// the sparse form's allocation: a thread per sorted key of the level
+__global__ void k_alloc_nodes_sorted(const unsigned long long* __restrict__ sorted, long long first, long long count,
+                                     int lev, int lgrange, KeyDomain d, long long base, Node* nodes) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const long long li = (long long)sorted[first + i] - d.bitbase;
+    nodes[base + i] = key_node(lev, lgrange, d, li, base + i);
 }
 
 __global__ void k_write_node(Node* dst, Node v) { *dst = v; }
@@ -663,12 +796,12 @@ void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s) {
     k_bbox<<<b, 512, 0, s>>>(p, orig, out6);
 }
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
-                       uint32_t* bitmap, int* err, cudaStream_t s) {
+                       uint32_t* bitmap, const KeySets& ks, int* err, cudaStream_t s) {
     long long nwords = 0;
     for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
-    size_t smem = nwords <= 8192 ? (size_t)nwords * 4 : 0;
+    size_t smem = !ks.keys.tab && nwords <= 8192 ? (size_t)nwords * 4 : 0;
     unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-    k_keys_pass1<<<blocks, 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, err);
+    k_keys_pass1<<<blocks, 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, ks.keys, err);
 }
 long long touch_dirs_words(const KeyDomains& dom) {
     return (long long)(dom.d[0].dim[0] + 2) * (dom.d[0].dim[1] + 2) * (dom.d[0].dim[2] + 2);
@@ -676,11 +809,25 @@ long long touch_dirs_words(const KeyDomains& dom) {
 
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
-                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, cudaStream_t s) {
+                     uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, const KeySets& ks,
+                     cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
     const float hr = hi_mul == 2 ? 2.0f * radius : radius;
     const float rr = (float)(1 << t.lgrange[0]);
+    if (ks.touched.tab) {
+        // sparse form: the per-point walk into the touched table, parents level by level,
+        // then every touched position resolved in one pass
+        k_touch_box<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
+                                                                 nullptr, 0, ks.touched, err);
+        const unsigned long long cap = ks.touched.mask + 1;
+        for (int lev = 1; lev < depth; lev++)
+            k_touch_up_hashed<<<grid_stride_blocks((long long)cap, 256), 256, 0, s>>>(ks.touched, dom.d[lev - 1],
+                                                                                      dom.d[lev], t.lgres[lev], err);
+        k_resolve_hashed<<<grid_stride_blocks((long long)cap, 256), 256, 0, s>>>(t, lg, depth, dom, ks.touched, ks.keys,
+                                                                                 markers, err);
+        return;
+    }
     if (dirs && radius <= rr && hr <= rr) {
         // boxes within one node of the home node: direction sets per home node
         DirDomain dd;
@@ -712,7 +859,8 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
         size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
         // fewer, fuller blocks when each one flushes a shared bitmap
         unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-        k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords, err);
+        k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords,
+                                              KeyHash{nullptr, 0}, err);
     }
     for (int lev = 1; lev < depth; lev++) {
         long long nw = (dom.d[lev - 1].nbits + 31) >> 5;
@@ -740,6 +888,18 @@ void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long wo
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
     if (nwords <= 0) return;
     k_alloc_nodes<<<blocks_for(nwords * 32, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
+}
+void launch_hash_compact(const KeyHash& h, unsigned long long* out, unsigned int* count, cudaStream_t s) {
+    k_hash_compact<<<grid_stride_blocks((long long)(h.mask + 1), 256), 256, 0, s>>>(h, out, count);
+}
+void launch_key_bounds(const unsigned long long* sorted, const unsigned int* n, const KeyDomains& dom, int depth,
+                       unsigned int* at, cudaStream_t s) {
+    k_key_bounds<<<1, 32, 0, s>>>(sorted, n, dom, depth, at);
+}
+void launch_alloc_nodes_sorted(const unsigned long long* sorted, long long first, long long count, int lev,
+                               int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
+    if (count <= 0) return;
+    k_alloc_nodes_sorted<<<blocks_for(count, 256), 256, 0, s>>>(sorted, first, count, lev, lgrange, d, base, nodes);
 }
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<1, 1, 0, s>>>(dst, v); }
 void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s) {

@@ -37,7 +37,7 @@ EXPORTS = [
     "gbvdb_get_node_counts", "gbvdb_get_point_bounds", "gbvdb_export_nodes", "gbvdb_export_childlist",
     "gbvdb_get_atlas_info", "gbvdb_export_atlas_bricks", "gbvdb_export_atlas_map", "gbvdb_export_subcells",
     "gbvdb_checksum", "gbvdb_get_atlas_device", "gbvdb_set_profile", "gbvdb_get_stage_times",
-    "gbvdb_get_stats", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
+    "gbvdb_get_stats", "gbvdb_get_stats_ex", "gbvdb_checksum_noalloc", "gbvdb_set_tuning", "gbvdb_save_vbx", "gbvdb_load_vbx",
     "gbvdb_update_neighbors", "gbvdb_export_neighbors", "gbvdb_update_apron_faces", "gbvdb_compute",
     "gbvdb_insert_points_subcell_fp16", "gbvdb_gather_levelset_fp16", "gbvdb_insert_points", "gbvdb_scatter_density",
     "gbvdb_export_point_leaves", "gbvdb_checksum_device", "gbvdb_fill_channel4", "gbvdb_clear_channel",
@@ -70,6 +70,7 @@ TUNE_TABLE = 5
 TUNE_BIN_UNROLL = 6
 TUNE_SCATTER_UNROLL = 7
 TUNE_GATHER_BLOCKS = 8
+TUNE_KEYSET = 9
 FUNC_SMOOTH = 113
 
 
@@ -139,6 +140,7 @@ def load(path=LIB_PATH):
     L.gbvdb_set_profile.argtypes = [vp, i32]
     L.gbvdb_get_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
     L.gbvdb_get_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.gbvdb_get_stats_ex.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
     L.gbvdb_checksum_noalloc.argtypes = [vp, i32, vp]
     L.gbvdb_set_tuning.argtypes = [vp, i32, i64]
     L.gbvdb_save_vbx.argtypes = [vp, ctypes.c_char_p]
@@ -492,9 +494,10 @@ class Grid:
         self._check(self.L.gbvdb_set_profile(self._h, int(on)), "set_profile")
 
     def stats(self):
-        out = (ctypes.c_int64 * 4)()
-        self._check(self.L.gbvdb_get_stats(self._h, out), "get_stats")
-        return {"launches": out[0], "readbacks": out[1], "sc_len": out[2], "bricks": out[3]}
+        out = (ctypes.c_int64 * 5)()
+        self._check(self.L.gbvdb_get_stats_ex(self._h, out, 5), "get_stats_ex")
+        return {"launches": out[0], "readbacks": out[1], "sc_len": out[2], "bricks": out[3],
+                "hashed_key_passes": out[4]}
 
     def stage_times(self, cap=32):
         out = (ctypes.c_double * cap)()

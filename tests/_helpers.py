@@ -55,7 +55,7 @@ def snapshot_oracle(g, ln):
 
 def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
             boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True,
-            fp16_subcells=False, dense_min=None, fused_apron=None, touch_dirs=None, unroll=None):
+            fp16_subcells=False, dense_min=None, fused_apron=None, touch_dirs=None, unroll=None, keyset=None):
     import torch
 
     import gbvdb
@@ -68,6 +68,8 @@ def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1
         g.set_tuning(gbvdb.TUNE_FUSED_APRON, fused_apron)
     if touch_dirs is not None:  # 0: the box passes walk every point's box positions
         g.set_tuning(gbvdb.TUNE_TOUCH_DIRS, touch_dirs)
+    if keyset is not None:  # 2: RebuildTopology's key sets as hash tables (the sparse form)
+        g.set_tuning(gbvdb.TUNE_KEYSET, keyset)
     if unroll is not None:  # (points per thread of the count pass, of the scatter pass)
         g.set_tuning(gbvdb.TUNE_BIN_UNROLL, unroll[0])
         g.set_tuning(gbvdb.TUNE_SCATTER_UNROLL, unroll[1])
