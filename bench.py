@@ -740,6 +740,13 @@ def bench_ours(args):
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": traffic.get("bytes_per_launch") if traffic else None,
                 "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": g_ms, "bytes_formula": formula}
+    if traffic:
+        # the DRAM bytes this kernel really moves (ncu, one launch of the same workload) over
+        # the same event time: its use of HBM, as opposed to the reference-algorithmic rate
+        # above (whose subcell-list term the binned form never writes or reads)
+        dram_gbs = traffic["bytes_per_launch"] / (g_ms / 1000.0) / 1e9
+        roofline["dram_achieved_gbs"] = dram_gbs
+        roofline["dram_frac"] = dram_gbs / peak
 
     # per-stage roofline: the ideal bytes each stage must move (N points, S subcell-list
     # entries, B linked bricks, n_L nodes at level L, 4-byte voxels) over the stage's
