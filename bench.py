@@ -476,8 +476,9 @@ def bench_surface(args, steps=5):
 
 
 def bench_sparse_jobs(args, reps=20):
-    """RebuildTopology cost of sparse jobs, per key-set form (TUNE_KEYSET 1: level bitmaps
-    over the points' key domain, 2: hash tables of the keys + radix sort).  Small job:
+    """RebuildTopology cost of sparse jobs, per key-set form (TUNE_KEYSET 0: the default
+    choice, 1: level bitmaps over the points' key domain, 2: hash tables of the keys +
+    radix sort).  Small job:
     10,000 sphere-surface points in 4096^3 (seed 5, grid (4,4,3,4), r = 1.5), a full
     rebuild per call.  Far clusters: 3 x 100,000 points in 80^3 boxes at far corners of a
     65,536^3 root (grid (3,3,3,3,4), r = 2): beyond the bitmaps' 2^34 positions, so only
@@ -497,7 +498,7 @@ def bench_sparse_jobs(args, reps=20):
 
     surf = datasets.surface(10_000, seed=5)
     surf = surf[np.all(surf >= 0, axis=1)]
-    jobs = [("small_job_4096", surf, (4, 4, 3, 4), 1.5, (1, 2)),
+    jobs = [("small_job_4096", surf, (4, 4, 3, 4), 1.5, (0, 1, 2)),
             ("far_clusters_65536", clusters(100_000, 6), (3, 3, 3, 3, 4), 2.0, (0,))]
     out = {}
     stream = torch.cuda.current_stream()

@@ -121,16 +121,11 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
     // (load_pos4); kU = 1, 2: points kU grid strides apart
     constexpr bool kConsec = kU == 4;
     unsigned long long members = 0, orphans = 0;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long per_lane = kConsec ? 4 : 1;
-    const long long first = per_lane * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    const long long first = kConsec ? 4ll * ((long long)blockIdx.x * blockDim.x + threadIdx.x)
+                                    : (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long step = kConsec ? 4 * stride : kU * stride;
-    // the loop runs while any lane of the warp has points (the counting atomics are
-    // combined across the warp); lanes past the end carry no valid point
-    for (long long w0 = first - per_lane * lane; w0 < p.n; w0 += step) {
-        const long long i0 = w0 + per_lane * lane;
+    for (long long i0 = first; i0 < p.n; i0 += step) {
         auto idx = [&](int u) { return kConsec ? i0 + u : i0 + u * stride; };
         float w[kU][3];
         bool ok[kU];
@@ -180,19 +175,9 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
             bin[u] = leaf[u] >= 0 ? __ldg(scmap + leaf[u]) * 64u + loc[u] : 0u;
             nbm[u] = (nbmask && leaf[u] >= 0) ? __ldg(nbmask + leaf[u]) : 0u;
         }
-        // one atomic per distinct bin of the warp (points of a dense region share their
-        // bins with their neighbours in the buffer): the leader adds the group's size, each
-        // point's rank is the old count plus its place among the group's lanes
         uint32_t rk[kU];
 #pragma unroll
-        for (int u = 0; u < kU; u++) {
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, leaf[u] >= 0 ? bin[u] : 0xFFFFFFFFu);
-            const int leader = __ffs(peers) - 1;
-            uint32_t old = 0;
-            if (leaf[u] >= 0 && lane == leader) old = atomicAdd(bin_cnt + bin[u], (uint32_t)__popc(peers));
-            old = __shfl_sync(0xFFFFFFFFu, old, leader);
-            rk[u] = leaf[u] >= 0 ? old + (uint32_t)__popc(peers & lt) : 0u;
-        }
+        for (int u = 0; u < kU; u++) rk[u] = leaf[u] >= 0 ? atomicAdd(bin_cnt + bin[u], 1u) : 0u;
         int bo[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) {

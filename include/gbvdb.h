@@ -291,11 +291,13 @@ GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** int
 #define GBVDB_TUNE_BIN_UNROLL 6   /* points per thread of the subcell count pass: 1, 2 or 4 (0: table / default 2) */
 #define GBVDB_TUNE_SCATTER_UNROLL 7 /* points per thread of the binning scatter: 2, 4 or 8 (0: table / default 4) */
 #define GBVDB_TUNE_GATHER_BLOCKS 8  /* resident blocks per SM the gather is built for: 10 or 8 (0: table / 10) */
-#define GBVDB_TUNE_KEYSET 9  /* key sets of RebuildTopology's passes.  0 (default): per-level bitmaps over the
-                                points' key domain (bounding box plus margin, clipped to the root) while the
-                                domain has at most 2^34 node positions, else hash tables of the keys, compacted
-                                and radix-sorted (no domain limit; the reference's Thrust sort of brick keys);
-                                1: the same; 2: always the tables.  Same pools either way. */
+#define GBVDB_TUNE_KEYSET 9  /* key sets of RebuildTopology's passes: per-level bitmaps over the points' key
+                                domain (bounding box plus margin, clipped to the root; cost grows with the
+                                domain, at most 2^34 node positions), or hash tables of the keys, compacted and
+                                radix-sorted (cost grows with the points; no domain limit, as the reference's
+                                Thrust sort of brick keys).  0 (default): the tables when the domain has more
+                                than 64 positions per point key (n points x levels) + 2^21, or more than 2^34;
+                                1: the bitmaps while they fit; 2: always the tables.  Same pools either way. */
 GBVDB_API gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value);
 /* where the tuning table was read from, or "" when none was loaded */
 GBVDB_API const char* gbvdb_tune_table_source(void);
