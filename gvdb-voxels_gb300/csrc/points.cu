@@ -213,16 +213,17 @@ __global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, f
             if (!any) continue;
             if (nbmask && leaf[u] >= 0) {
                 // R <= 11: the member range reaches only the 27 bricks around the home
-                // brick; their linked flags are nbm (k_nb_mask)
-                int c[3][3];
-#pragma unroll
-                for (int a = 0; a < 3; a++)
-#pragma unroll
-                    for (int d = 0; d < 3; d++) c[a][d] = range_in_brick(lo[a], hi[a], hb[u][a] + 16 * (d - 1));
+                // brick; their linked flags are nbm (k_nb_mask).  All 27 linked: every
+                // member subcell counts
                 if (nbm[u] == 0x7FFFFFFu) {
-                    members += (unsigned long long)(c[0][0] + c[0][1] + c[0][2]) * (unsigned)(c[1][0] + c[1][1] + c[1][2]) *
-                               (unsigned)(c[2][0] + c[2][1] + c[2][2]);
+                    members += (unsigned long long)(((hi[0] - lo[0]) >> 2) + 1) * (unsigned)(((hi[1] - lo[1]) >> 2) + 1) *
+                               (unsigned)(((hi[2] - lo[2]) >> 2) + 1);
                 } else {
+                    int c[3][3];
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+#pragma unroll
+                        for (int d = 0; d < 3; d++) c[a][d] = range_in_brick(lo[a], hi[a], hb[u][a] + 16 * (d - 1));
                     unsigned long long m = 0;
 #pragma unroll
                     for (int dz = 0; dz < 3; dz++)

@@ -841,12 +841,14 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
             // them, so that in the full pass nearly every point finds its bits set and
             // issues no atomic (when all points start on empty entries, the atomics of a
             // dense region pile up on its few entries)
+            // (64-thread blocks: the sample's 16,384 threads per 4 M points then spread over
+            // every SM instead of 64 of them)
             if (p.n >= 64 * 1024) {
                 PointSrc q = p;
                 q.stride = p.stride * 64;
                 q.n = (p.n + 63) / 64;
-                k_touch_dirs<4><<<grid_stride_blocks((q.n + 3) / 4, 256), 256, 0, s>>>(q, orig, radius, hr, t.lgrange[0],
-                                                                                       rlo, rhi, dd, dirs, err);
+                k_touch_dirs<4><<<grid_stride_blocks((q.n + 3) / 4, 64), 64, 0, s>>>(q, orig, radius, hr, t.lgrange[0],
+                                                                                     rlo, rhi, dd, dirs, err);
             }
             k_touch_dirs<4><<<grid_stride_blocks((p.n + 3) / 4, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo,
                                                                                    rhi, dd, dirs, err);

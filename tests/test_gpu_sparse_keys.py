@@ -88,10 +88,10 @@ def test_far_clusters_take_the_sparse_form(gpu_lib):
 
 @pytest.mark.parametrize("keyset", [0, 1, 2])
 def test_surface_4096_each_form(gpu_lib, keyset):
-    """sphere surfaces in 4096^3, grid (4,4,3,4): a domain of about 2^24 leaf positions
-    for 40,000 points, where the default takes the tables; the bitmaps forced, the tables
-    forced and the default all match the oracle"""
-    pts = datasets.sphere_surface(40_000, seed=21, domain=4096.0, nspheres=6)
+    """sphere surfaces in 4096^3, grid (4,4,3,4): a key domain of about 4.6 M positions
+    for 8,423 points (25,269 point keys), where the default takes the tables; the bitmaps
+    forced, the tables forced and the default all match the oracle"""
+    pts = datasets.sphere_surface(10_000, seed=21, domain=4096.0, nspheres=6)
     pts = pts[np.all(pts >= 0, axis=1)]
     _, o = H.run_oracle(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5)
     g, gs = H.run_gpu(pts, log2dims=(4, 4, 3, 4), radius=1.5, R=1.5, rho=1.5, keyset=keyset)
