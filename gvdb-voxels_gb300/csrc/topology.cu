@@ -340,10 +340,14 @@ struct DirDomain {
 // Four consecutive points per thread per step (load_pos4): their position loads, then
 // their entry loads, are issued together (the pass is bound by the latency of that
 // two-load chain).
-template <int kU>
+// kIntR: radius and the upper reach hr are whole numbers (below 2^20), so for a point
+// coordinate below 2^23 the box bounds int(float(ip) -/+ r) are ip -/+ r exactly, in
+// integer arithmetic (the float form's conversions are what bound this pass's issue)
+template <int kU, bool kIntR>
 __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, int lg, int3 rlo, int3 rhi,
                              DirDomain dd, uint32_t* __restrict__ dirs, int* err) {
     static_assert(kU == 4, "four consecutive points per thread");
+    const int ir = (int)radius, ihr = (int)hr;
     const int rr = 1 << lg;
     const int rl[3] = {rlo.x, rlo.y, rlo.z}, rh[3] = {rhi.x - 1, rhi.y - 1, rhi.z - 1};
     const long long ngroups = (p.n + 3) >> 2;
@@ -374,8 +378,16 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 const int ip = (int)w[u][a];
-                const float fi = (float)ip;
-                int lo = trunc_mult((int)fsub(fi, radius), lg), hi = trunc_mult((int)fadd(fi, hr), lg);
+                int bl, bh;
+                if (kIntR && ip < (1 << 23)) {
+                    bl = ip - ir;
+                    bh = ip + ihr;
+                } else {
+                    const float fi = (float)ip;
+                    bl = (int)fsub(fi, radius);
+                    bh = (int)fadd(fi, hr);
+                }
+                int lo = trunc_mult(bl, lg), hi = trunc_mult(bh, lg);
                 if (lo < rl[a]) lo += ((rl[a] - lo + rr - 1) >> lg) << lg;
                 if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
                 hb[a] = ip >> lg;
@@ -843,15 +855,17 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
             // dense region pile up on its few entries)
             // (64-thread blocks: the sample's 16,384 threads per 4 M points then spread over
             // every SM instead of 64 of them)
+            const bool int_r = radius >= 0.0f && radius == floorf(radius) && hr == floorf(hr) && hr <= 1048576.0f;
+            auto touch = int_r ? k_touch_dirs<4, true> : k_touch_dirs<4, false>;
             if (p.n >= 64 * 1024) {
                 PointSrc q = p;
                 q.stride = p.stride * 64;
                 q.n = (p.n + 63) / 64;
-                k_touch_dirs<4><<<grid_stride_blocks((q.n + 3) / 4, 64), 64, 0, s>>>(q, orig, radius, hr, t.lgrange[0],
-                                                                                     rlo, rhi, dd, dirs, err);
+                touch<<<grid_stride_blocks((q.n + 3) / 4, 64), 64, 0, s>>>(q, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
+                                                                            dirs, err);
             }
-            k_touch_dirs<4><<<grid_stride_blocks((p.n + 3) / 4, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo,
-                                                                                   rhi, dd, dirs, err);
+            touch<<<grid_stride_blocks((p.n + 3) / 4, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
+                                                                          dirs, err);
         }
         const long long nw = (dom.d[0].nbits + 31) >> 5;
         k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
