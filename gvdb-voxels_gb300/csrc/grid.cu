@@ -806,7 +806,8 @@ struct gbvdb_grid_s {
 
     // scratch of the direction-set form of the box pass (null: the per-point walk)
     uint32_t* touch_dirs_buf(const KeyDomains& kd) {
-        if (!touch_dirs_on) return nullptr;
+        // a word per level-0 position: beyond 2^28 words (1 GiB) the per-point walk
+        if (!touch_dirs_on || touch_dirs_words(kd) > (1ll << 28)) return nullptr;
         grow(touch_dirs, (size_t)touch_dirs_words(kd) * 4);
         return ptr<uint32_t>(touch_dirs);
     }

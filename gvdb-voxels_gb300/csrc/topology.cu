@@ -367,7 +367,7 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
             }
         }
         uint32_t m27[kU];
-        long long ent[kU];
+        int ent[kU];
 #pragma unroll
         for (int u = 0; u < kU; u++) {
             m27[u] = 0;
@@ -387,7 +387,10 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
                     bl = (int)fsub(fi, radius);
                     bh = (int)fadd(fi, hr);
                 }
-                int lo = trunc_mult(bl, lg), hi = trunc_mult(bh, lg);
+                // x / rr * rr with C truncation (bl >= -(r + 1) and bh >= 0 stay far from
+                // INT_MIN, so 32-bit negation is safe)
+                int lo = bl >= 0 ? (bl >> lg) << lg : -(((-bl) >> lg) << lg);
+                int hi = bh >= 0 ? (bh >> lg) << lg : -(((-bh) >> lg) << lg);
                 if (lo < rl[a]) lo += ((rl[a] - lo + rr - 1) >> lg) << lg;
                 if (hi > rh[a]) hi -= ((hi - rh[a] + rr - 1) >> lg) << lg;
                 hb[a] = ip >> lg;
@@ -396,11 +399,11 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
                 m[a] = hi >= lo ? (((1 << (h - l + 1)) - 1) << (l + 1)) & 7 : 0;
             }
             if (!any) continue;
-#pragma unroll
-            for (int dz = 0; dz < 3; dz++)
-#pragma unroll
-                for (int dy = 0; dy < 3; dy++)
-                    if (((m[2] >> dz) & (m[1] >> dy)) & 1) m27[u] |= (uint32_t)m[0] << (dz * 9 + dy * 3);
+            // the product of the three 3-bit masks: bit (dz*9 + dy*3 + dx) for every
+            // (dx, dy, dz) they hold; the shifted copies of a mask never overlap, so
+            // multiplying by a sum of powers of two places them without carries
+            const uint32_t ym = (uint32_t)m[0] * (uint32_t)((m[1] & 1) | ((m[1] & 2) << 2) | ((m[1] & 4) << 4));
+            m27[u] = ym * (uint32_t)((m[2] & 1) | ((m[2] & 2) << 8) | ((m[2] & 4) << 16));
             const int rx = hb[0] - dd.lo[0], ry = hb[1] - dd.lo[1], rz = hb[2] - dd.lo[2];
             if ((unsigned)rx >= (unsigned)dd.dim[0] || (unsigned)ry >= (unsigned)dd.dim[1] ||
                 (unsigned)rz >= (unsigned)dd.dim[2]) {
@@ -408,7 +411,7 @@ __global__ void k_touch_dirs(PointSrc p, float3 orig, float radius, float hr, in
                 m27[u] = 0;
                 continue;
             }
-            ent[u] = ((long long)rx * dd.dim[1] + ry) * dd.dim[2] + rz;
+            ent[u] = (rx * dd.dim[1] + ry) * dd.dim[2] + rz;  // the table has < 2^28 entries
         }
         // the entries of a dense region are few and hot: read them through L1 (a copy from
         // before another point's atomic only makes this point repeat a bit: the OR is
