@@ -174,6 +174,9 @@ struct gbvdb_grid_s {
     DevBuf nodes[kMaxLev], clist[kMaxLev];
     long long ncnt[kMaxLev] = {0}, nused[kMaxLev] = {0};
     bool nused0_stale = false;  // nused[0] awaits a count of the flagged leaves
+    // 8 bytes that the next key-count readback brings back with the counts (null: none)
+    const void* rb_extra = nullptr;
+    unsigned long long rb_extra_val = 0;
     int rebuild_topo = 1;
     int curr_depth = -1;
     int last_depth = 0;
@@ -623,10 +626,12 @@ struct gbvdb_grid_s {
         }
         int errflag = 0;
         check(cudaMemcpyAsync(pinned + 4 * (depth + 1), ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        if (rb_extra) check(cudaMemcpyAsync(pinned + 128, rb_extra, 8, cudaMemcpyDeviceToHost, stream), "rb");
         n_readback++;
         sync();
         memcpy(at.data(), pinned, 4 * (depth + 1));
         memcpy(&errflag, pinned + 4 * (depth + 1), 4);
+        if (rb_extra) memcpy(&rb_extra_val, pinned + 128, 8);
         if (errflag & 2)
             throw StatusError{GBVDB_INVALID_ARG, "a point's activation box spans more than 2^26 nodes of one level"};
         if (errflag) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
@@ -648,12 +653,14 @@ struct gbvdb_grid_s {
         check_launch("hash compact");
         check(cudaMemcpyAsync(pinned, cnt, 4, cudaMemcpyDeviceToHost, stream), "rb");
         check(cudaMemcpyAsync(pinned + 4, ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
+        if (rb_extra) check(cudaMemcpyAsync(pinned + 128, rb_extra, 8, cudaMemcpyDeviceToHost, stream), "rb");
         n_readback++;
         sync();
         unsigned int n = 0;
         int errflag = 0;
         memcpy(&n, pinned, 4);
         memcpy(&errflag, pinned + 4, 4);
+        if (rb_extra) memcpy(&rb_extra_val, pinned + 128, 8);
         if (errflag & 2)
             throw StatusError{GBVDB_INVALID_ARG, "a point's activation box spans more than 2^26 nodes of one level"};
         if (errflag & 1) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
@@ -881,12 +888,19 @@ struct gbvdb_grid_s {
         TreeView t = view();
         int rlo[3], rhi[3];
         for (int a = 0; a < 3; a++) { rlo[a] = root_pos[a]; rhi[a] = (int)std::min<long long>(root_pos[a] + range[rl], 0x7FFFFFFF); }
-        // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066)
+        // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066).
+        // The kept leaves (non-zero markers) come back with the counts: with the new
+        // leaves they are the flagged-leaf count, so UpdateAtlas needs no readback of its own
+        unsigned long long* kept = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 72);
+        rb_extra = kept;
         std::vector<uint32_t> at = key_pass(D, kd, bits, nleaf / 4 + 1024, 4 * n + 1024, [&](const KeySets& ks) {
             launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
                             ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, stream);
             check_launch("keys_incr");
+            launch_count_markers(ptr<int>(markers), nleaf, kept, stream);
+            check_launch("count_markers");
         });
+        rb_extra = nullptr;
         mark();
         if (at[(size_t)D] == 0) return;
         launch_apply_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), stream);
@@ -901,9 +915,10 @@ struct gbvdb_grid_s {
             check_launch("delink_upper");
         }
         build_leaf_grid();
-        // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148): counted when next
-        // needed (UpdateAtlas counts the flagged leaves anyway), not with a readback here
-        nused0_stale = true;
+        // usedCnt(0,0) = number of flagged leaves (VG.cpp:1144-1148): the kept old leaves
+        // plus the new ones
+        nused[0] = (long long)rb_extra_val + ((long long)at[1] - (long long)at[0]);
+        nused0_stale = false;
         mark();
     }
 
@@ -998,9 +1013,13 @@ struct gbvdb_grid_s {
             launch_node_flags(ptr<Node>(nodes[0]), total, 0, ptr<uint32_t>(flags), stream);
             scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(flags_scan), total, scan_tmp.p, stream);
             check_launch("atlas scan");
-            uint32_t f = 0;
-            readback(&f, ptr<uint32_t>(flags_scan) + total, 4);
-            F = f;
+            if (nused0_stale) {
+                uint32_t f = 0;
+                readback(&f, ptr<uint32_t>(flags_scan) + total, 4);
+                F = f;
+            } else {
+                F = nused[0];  // the flagged-leaf count, kept exact by every topology change
+            }
         }
         if (F > layer * az) az = (int)std::ceil((double)((float)F / (float)layer));  // AtlasAlloc growth, AL.cpp:695-698
         if (nused0_stale) {  // F is the flagged-leaf count

@@ -117,6 +117,8 @@ void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStr
 void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s);
 void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s);
 void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s);
+// *out = non-zero markers (cleared by the launcher)
+void launch_count_markers(const int* markers, long long n, unsigned long long* out, cudaStream_t s);
 void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s);
 
 // ---- atlas.cu

@@ -768,6 +768,15 @@ __global__ void k_count_flags(const Node* nodes, long long n, unsigned long long
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
 }
 
+// leaves an incremental pass keeps flagged: the non-zero markers
+__global__ void k_count_markers(const int* markers, long long n, unsigned long long* out) {
+    unsigned c = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        c += markers[i] ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+}
+
 // ComputeBounds (VG.cpp:1792-1816): both corners start at the position of leaf 0 of
 // the pool (flagged or not); every flagged leaf widens them by [pos, pos + range0).
 // One block; out6 = {min xyz, max xyz}, written whole (no initialisation needed).
@@ -943,6 +952,11 @@ void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s) {
 void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s) {
     if (n <= 0) return;
     k_delink_upper<<<blocks_for(n, 128), 128, 0, s>>>(t, lev, n);
+}
+void launch_count_markers(const int* markers, long long n, unsigned long long* out, cudaStream_t s) {
+    cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+    if (n <= 0) return;
+    k_count_markers<<<grid_stride_blocks(n, 256), 256, 0, s>>>(markers, n, out);
 }
 void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s) {
     if (n <= 0) return;

@@ -3,7 +3,12 @@ particles, seed 1, dam-break layout in 512^3, p += 0.5 v per frame; grid
 (3,3,3,4), RebuildTopology(r=4), InsertPointsSubcell(4, R=4), GatherLevelSet(rho=2),
 UpdateApron(0, 3.0)) through the C ABI against the FP64 oracle on all host cores.
 
-Three calls, as the reference takes them: the first two are full rebuilds (the
+Also the surface workload at its stated size (16,777,216 points, seed 2, grid
+(4,4,3,4), atlas axis counts (64, 64), RebuildTopology(r=1.5),
+InsertPointsSubcell(4, R=1.5), GatherDensity(rho=1.5), UpdateApron(0, 0.0)), one full
+rebuild, compared the same way.
+
+Fluid: three calls, as the reference takes them: the first two are full rebuilds (the
 second call always rebuilds, gvdb_volume_gvdb.cpp:1195-1205), the third is
 incremental.  Frames 2 and 3 are compared: node pools, child lists and atlas map
 bit-exact, the subcell list length exact, every voxel of every brick within 1e-5
@@ -61,3 +66,45 @@ def test_fluid_frames_full_size(gpu_lib):
         lim = float((1e-6 + 1e-5 * np.abs(inner)).sum())
         assert abs(s["checksum"] - o["checksum"]) <= lim, (k, s["checksum"], o["checksum"], lim)
         del o, s, inner
+
+
+def test_surface_full_size(gpu_lib):
+    import torch
+
+    import gbvdb
+    import oracle
+
+    pts = datasets.surface(16_777_216, seed=2)
+    og = oracle.OracleGrid((4, 4, 3, 4))
+    og.add_channel(0, 3, 1, (64, 64, 1))
+    assert og.rebuild_topology(pts, 1.5) == 0
+    og.update_atlas()
+    _, ln_o = og.insert_points_subcell(pts, 1.5)
+    og.gather_density(1.5)
+    og.update_apron(0, 0.0)
+    g = gbvdb.Grid(0, (4, 4, 3, 4))
+    g.set_channel_default(64, 64, 1)
+    g.add_channel(0)
+    d = torch.from_numpy(pts).cuda()
+    n = g.set_points(d)
+    g.rebuild_topology(n, 1.5)
+    g.update_atlas()
+    _, ln = g.insert_points_subcell(4, n, 1.5)
+    g.gather_density(4, n, 1.5, (0, 0, 0), ln)
+    g.update_apron(0, 0.0)
+    torch.cuda.synchronize()
+    del d
+    o = {"depth": og.depth, "top": og.top_lev, "used": og.used_count(0),
+         "nodes": [og.nodes(l) for l in range(og.levs)], "clist": [og.childlist(l) for l in range(og.levs)],
+         "atlas_dims": og.atlas_dims(), "amap": og.atlas_map(), "bricks": og.atlas_bricks(0),
+         "checksum": og.checksum(0)}
+    s = snapshot_gpu(g, ln, export_subcells=False)
+    assert o["depth"] == 3
+    compare_topology(o, s)
+    assert ln == ln_o, (ln, ln_o)
+    compare_values(o, s)
+    check_apron_self(s, np.float32(0.0))
+    inner = o["bricks"][:, 1:17, 1:17, 1:17]
+    lim = float((1e-6 + 1e-5 * np.abs(inner)).sum())
+    assert abs(s["checksum"] - o["checksum"]) <= lim, (s["checksum"], o["checksum"], lim)
+

@@ -154,3 +154,35 @@ def test_batched_grids_config(gpu_lib):
     for a, m in zip(alone, res):
         assert m["status"] == gbvdb.OK
         assert (m["sc_len"], m["bricks"], m["checksum"]) == (a["sc_len"], a["bricks"], a["checksum"])
+
+
+def test_batched_grids_against_the_oracle(gpu_lib):
+    """Batched uneven grids of config 4 (the shell / sphere-surface mix, density rho = r = R
+    = 1, FP32), all submitted at once: every grid's list length exactly and its FP64 total
+    within the summed per-voxel tolerance of the oracle's, and for every fourth grid every
+    brick of the plain path against the oracle (topology bit-exact, voxels within 1e-5
+    relative / 1e-6 absolute)."""
+    import gbvdb
+
+    import _helpers as H
+
+    clouds = datasets.batched(count=24, seed=3, lo=1e4, hi=3e5)
+    jobs = [dict(points=c, mode=0, dtype=3, radius=1.0, gather_radius=1.0, boundval=0.0) for c in clouds]
+    srv = gbvdb.Server(0, workers=16)
+    try:
+        res = [srv.wait(t) for t in [_submit(srv, j) for j in jobs]]
+    finally:
+        srv.close()
+    for k, (j, m) in enumerate(zip(jobs, res)):
+        assert m["status"] == gbvdb.OK
+        og, outs = H.run_oracle(j["points"], radius=1.0, R=1.0, rho=1.0, mode="density", boundval=0.0)
+        o = outs[0]
+        assert m["sc_len"] == o["len"], (k, m["sc_len"], o["len"])
+        inner = o["bricks"][:, 1:17, 1:17, 1:17]
+        lim = float((1e-6 + 1e-5 * np.abs(inner)).sum())
+        assert abs(m["checksum"] - o["checksum"]) <= lim, (k, m["checksum"], o["checksum"], lim)
+        if k % 4 == 0:
+            _, gs = H.run_gpu(j["points"], radius=1.0, R=1.0, rho=1.0, mode="density", boundval=0.0)
+            H.compare_topology(o, gs[0])
+            H.compare_subcells(o, gs[0])
+            H.compare_values(o, gs[0])
