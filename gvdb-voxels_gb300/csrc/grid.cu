@@ -255,6 +255,9 @@ struct gbvdb_grid_s {
     // wait for it on the device (join_side).
     cudaStream_t side = nullptr;
     cudaEvent_t side_start = nullptr, side_done = nullptr;
+    // a readback's copies are done: the host waits on this instead of the whole stream
+    // when independent work is queued behind them
+    cudaEvent_t rb_ev = nullptr;
     bool side_pending = false;
     void join_side() {
         if (!side_pending) return;
@@ -1102,25 +1105,28 @@ struct gbvdb_grid_s {
         grow(scan_tmp, scan_tmp_bytes(nbins));
         scan_exclusive_u32(ptr<uint32_t>(bin_cnt), ptr<uint32_t>(bin_off), nbins, scan_tmp.p, stream);
         check_launch("bin scan");
-        unsigned long long tot[2];
-        uint32_t binned = 0, nb = 0;
-        check(cudaMemcpyAsync(pinned, totals, 16, cudaMemcpyDeviceToHost, stream), "rb");
-        check(cudaMemcpyAsync(pinned + 16, ptr<uint32_t>(bin_off) + nbins, 4, cudaMemcpyDeviceToHost, stream), "rb");
-        check(cudaMemcpyAsync(pinned + 20, ptr<uint32_t>(scmap) + ncnt[0], 4, cudaMemcpyDeviceToHost, stream), "rb");
-        n_readback++;
-        sync();
-        memcpy(tot, pinned, 16);
-        memcpy(&binned, pinned + 16, 4);
-        memcpy(&nb, pinned + 20, 4);
-        sc_nbricks = nb;
-        mark();
-        grow(sorted, (size_t)std::max<uint32_t>(binned, 1) * 16);
+        // The totals are read back while the scatter runs: the host waits for the copies
+        // (an event before the scatter), not for the stream, so the caller's next calls
+        // queue behind the scatter with no idle gap.  The binned records are at most one
+        // per point, so the buffers are sized by the point count.
+        grow(sorted, (size_t)std::max<long long>(p.n, 1) * 16);
         // the list entries carry the points' colours when SetPoints gave a colour buffer
         // (InsertPointsSubcell, VG.cpp:5063-5075)
-        if (clr.base) grow(sorted_clr, (size_t)std::max<uint32_t>(binned, 1) * 4);
+        if (clr.base) grow(sorted_clr, (size_t)std::max<long long>(p.n, 1) * 4);
+        unsigned long long tot[2];
+        uint32_t nb = 0;
+        check(cudaMemcpyAsync(pinned, totals, 16, cudaMemcpyDeviceToHost, stream), "rb");
+        check(cudaMemcpyAsync(pinned + 20, ptr<uint32_t>(scmap) + ncnt[0], 4, cudaMemcpyDeviceToHost, stream), "rb");
+        check(cudaEventRecord(rb_ev, stream), "readback event");
+        n_readback++;
+        mark();
         launch_bin_scatter(p, trans, R, qz, ptr<int>(bin_of), ptr<uint32_t>(rank_of), ptr<uint32_t>(bin_off),
                            ptr<float4>(sorted), clr, ptr<uint32_t>(sorted_clr), scatter_unroll(p.n), stream);
         check_launch("bin_scatter");
+        check(cudaEventSynchronize(rb_ev), "readback wait");
+        memcpy(tot, pinned, 16);
+        memcpy(&nb, pinned + 20, 4);
+        sc_nbricks = nb;
         mark();
         sc_valid = true;
         lists_valid = false;
@@ -1783,6 +1789,7 @@ gbvdb_status gbvdb_create(int device, gbvdb_grid* out) {
         return GBVDB_OUT_OF_MEMORY;
     }
     for (int i = 0; i < 64; i++) cudaEventCreate(&g->ev[i]);
+    cudaEventCreateWithFlags(&g->rb_ev, cudaEventDisableTiming);
     for (int i = 0; i < 2 * gbvdb_grid_s::kTuneN; i++) cudaEventCreate(&g->tune_ev[i]);
     *out = g;
     return GBVDB_OK;
@@ -1806,6 +1813,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (g->side_start) cudaEventDestroy(g->side_start);
     if (g->side_done) cudaEventDestroy(g->side_done);
     for (int i = 0; i < 64; i++) cudaEventDestroy(g->ev[i]);
+    if (g->rb_ev) cudaEventDestroy(g->rb_ev);
     for (int i = 0; i < 2 * gbvdb_grid_s::kTuneN; i++) cudaEventDestroy(g->tune_ev[i]);
     cudaFreeHost(g->pinned);
     delete g;
