@@ -852,6 +852,7 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
                                 f32x2 fzz = f2pack(fz, fz + 1.0f);
                                 const f32x2 two = f2pack(2.0f, 2.0f);
                                 int z = za;
+#pragma unroll 2
                                 for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
                                     const f32x2 dz = f2sub(pzz, fzz);
                                     const f32x2 d = f2fma(dz, dz, dxy2);
@@ -928,8 +929,10 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
             };
             float wmax = needy_max();
             int nq = 0;
+            bool drained = false;  // a drain since wmax was last taken
             // evaluate the queued points [0, nq) against the column's 4 voxels
             auto drain = [&]() {
+                drained = true;
                 const int n4 = (nq + 3) & ~3;
                 if (lane < n4 - nq) {  // pad with points at infinity (d^2 = inf)
                     qx[nq + lane] = __int_as_float(0x7F800000);
@@ -1029,15 +1032,21 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
                             if (nq >= 32) drain();
                         }
                     }
-                    if (nq) drain();
-                    // merge the halves' minima; wmax = the largest needy minimum
-                    m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
-                    m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
-                    m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
-                    m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
-                    wmax = needy_max();
+                    // wmax after a drain: the largest needy minimum over both halves'
+                    // partial minima, an upper bound of the merged one (so the bins and
+                    // points it skips still cannot lower any needy voxel)
+                    if (drained) {
+                        wmax = needy_max();
+                        drained = false;
+                    }
                 }
             }
+            if (nq) drain();
+            // merge the halves' minima
+            m0 = fminf(m0, __shfl_xor_sync(0xFFFFFFFFu, m0, 16));
+            m1 = fminf(m1, __shfl_xor_sync(0xFFFFFFFFu, m1, 16));
+            m2 = fminf(m2, __shfl_xor_sync(0xFFFFFFFFu, m2, 16));
+            m3 = fminf(m3, __shfl_xor_sync(0xFFFFFFFFu, m3, 16));
             if (hf == 0) {
                 tile[tv] = __float_as_uint(m0);
                 tile[tv + 256] = __float_as_uint(m1);
