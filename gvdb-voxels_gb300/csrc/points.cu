@@ -479,6 +479,10 @@ __device__ void write_tile(const GatherParams& gp, uint32_t* tile, T* out, bool 
 }
 
 constexpr int kGatherThreads = 128;
+// 1 / n for n = 1 .. 16 (entry 0 unused): the sparse walk's row-major column split
+__constant__ float kRcp16[17] = {0.0f,       1.0f,       0.5f,       1.0f / 3,  0.25f,     0.2f,
+                                 1.0f / 6,   1.0f / 7,   0.125f,     1.0f / 9,  0.1f,      1.0f / 11,
+                                 1.0f / 12,  1.0f / 13,  1.0f / 14,  1.0f / 15, 0.0625f};
 constexpr int kQueue = 64;  // per-warp point queue of the gather form (SoA x, y, z)
 constexpr int kLive = 256;  // live points per batch of the scatter form
 constexpr int kScratch = kLive * 16 > (kGatherThreads / 32) * 3 * kQueue * 4 ? kLive * 16
@@ -704,10 +708,11 @@ __global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ l
 // neighbourhood (either form is exact; the choice only affects speed):
 //
 // scatter (sparse bricks): every thread loads one neighbourhood point at a time
-//   (all loads in flight together) and derives its member subcells in this
-//   brick; each warp then walks its live points: for each member subcell, 2
-//   voxels per lane, min d^2 reduced into the shared tile with shared atomics
-//   (skipped when d^2 >= the static cutoff T).
+//   (all loads in flight together) and derives its reach in this brick (member
+//   subcells cut to the cutoff box); each warp then walks its live points: the
+//   reach's voxel columns 32 at a time, each lane one column, z two at a time
+//   over the part of the cutoff sphere above the group's nearest column, min d^2
+//   reduced into the shared tile with shared atomics.
 // gather (dense bricks): each warp owns whole subcells in turn.  It visits
 //   candidate home bins in ascending order of their lower-bound distance lb^2 to
 //   the subcell (host table) and stops at the first bin with lb^2 >= wmax, the
@@ -778,8 +783,8 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
         // voxels within rcut of it on every axis (brick-local voxel box).  The
         // live points of a batch of candidates go to a shared list; then the warps
         // take the list's entries in turn, each covering its entry's whole reach
-        // (lanes: 8 columns x 4 rows; rows in groups of 4, x in groups of 8, z
-        // walked two at a time over the group's reach) with shared atomicMin.
+        // (its columns row-major, 32 per group, a lane per column; z walked two at
+        // a time over the group's reach) with shared atomicMin.
         float4* live_pts = reinterpret_cast<float4*>(scratch);
         for (uint32_t cbase = 0; cbase < ncand; cbase += kLive) {
             if (threadIdx.x == 0) nlive = 0;
@@ -813,7 +818,6 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
             }
             __syncthreads();
             const int nl = nlive;
-            const int xl = lane & 7, yl = lane >> 3;
             const float rc2 = __fmul_rn(gp.rcut, gp.rcut);
             // warps take the live entries in turn; a warp covers all of its entry's
             // reach (rows in groups of 4), so an entry is decoded once, not once per
@@ -824,48 +828,46 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
                 const int x0 = bx & 15, x1 = (bx >> 4) & 15;
                 const int Y0 = (bx >> 8) & 15, Y1 = (bx >> 12) & 15;
                 const int z0 = (bx >> 16) & 15, z1 = (bx >> 20) & 15;
-                // brick-local position
-                const float lx = fsub(L.x, (float)ox), ly = fsub(L.y, (float)oy), lz = fsub(L.z, (float)oz);
-                for (int ys = Y0; ys <= Y1; ys += 4) {
-                    const int ye = min(ys + 3, Y1);
-                    // distance from the point to the nearest row of this group (warp-uniform)
-                    const float gy = fmaxf(0.0f, fmaxf((float)ys - ly, ly - (float)ye));
-                    const int y = ys + yl;
-                    const float dy = fsub(L.y, (float)(oy + y));
-                    for (int xs = x0; xs <= x1; xs += 8) {
-                        // z reach of this group of 8 columns: the sphere of radius rcut cut at
-                        // the group's nearest column (a superset of every voxel with d^2 < T)
-                        const int xe = min(xs + 7, x1);
-                        const float gx = fmaxf(0.0f, fmaxf((float)xs - lx, lx - (float)xe));
-                        const float zr2 = rc2 - __fmaf_rn(gy, gy, gx * gx);
-                        if (!(zr2 >= 0.0f)) continue;
-                        const float zr = sqrt_approx(zr2);  // rcut's margin (>= 0.01) covers its error
-                        const int za = max(z0, (int)ceilf(lz - zr)), zb = min(z1, (int)floorf(lz + zr));
-                        const int x = xs + xl;
-                        if (za <= zb && x <= xe && y <= ye) {
-                            const float dx = fsub(L.x, (float)(ox + x));
-                            const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
-                            if (__float_as_uint(dxy) < gp.tbits) {
-                                uint32_t* col = tile + (za << 8) + (y << 4) + x;
-                                const float fz = (float)(oz + za);  // integer-valued: steps of 1 and 2 are exact
-                                const f32x2 pzz = f2pack(L.z, L.z), dxy2 = f2pack(dxy, dxy);
-                                f32x2 fzz = f2pack(fz, fz + 1.0f);
-                                const f32x2 two = f2pack(2.0f, 2.0f);
-                                int z = za;
+                const int nx = x1 - x0 + 1, ncol = nx * (Y1 - Y0 + 1);
+                const float rnx = kRcp16[nx];
+                const float lz = fsub(L.z, (float)oz);  // brick-local z
+                const f32x2 pzz = f2pack(L.z, L.z);
+                const f32x2 two = f2pack(2.0f, 2.0f);
+                // the reach's columns, row-major over its rectangle, 32 per group
+                for (int kb = 0; kb < ncol; kb += 32) {
+                    const int k = kb + lane;
+                    // k / nx: (k + 0.5) / nx is at least 1/32 away from an integer and the
+                    // product's error is below 1e-4 for k < 512, so truncation is exact
+                    const int ry = (int)__fmul_rn((float)k + 0.5f, rnx);
+                    const int x = x0 + (k - ry * nx), y = Y0 + ry;
+                    const float dx = fsub(L.x, (float)(ox + x)), dy = fsub(L.y, (float)(oy + y));
+                    const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                    const bool in = k < ncol && __float_as_uint(dxy) < gp.tbits;
+                    // z reach of the group: the sphere of radius rcut cut at its column
+                    // nearest the point (a superset of every voxel with d^2 < T); no column
+                    // in: mn = inf, zr2 < 0
+                    const uint32_t mn = __reduce_min_sync(0xFFFFFFFFu, in ? __float_as_uint(dxy) : 0x7F800000u);
+                    const float zr2 = fsub(rc2, __uint_as_float(mn));
+                    if (!(zr2 >= 0.0f)) continue;
+                    const float zr = sqrt_approx(zr2);  // rcut's margin (>= 0.01) covers its error
+                    const int za = max(z0, (int)ceilf(lz - zr)), zb = min(z1, (int)floorf(lz + zr));
+                    if (!in || za > zb) continue;
+                    uint32_t* col = tile + (za << 8) + (y << 4) + x;
+                    const float fz = (float)(oz + za);  // integer-valued: steps of 1 and 2 are exact
+                    const f32x2 dxy2 = f2pack(dxy, dxy);
+                    f32x2 fzz = f2pack(fz, fz + 1.0f);
+                    int z = za;
 #pragma unroll 2
-                                for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
-                                    const f32x2 dz = f2sub(pzz, fzz);
-                                    const f32x2 d = f2fma(dz, dz, dxy2);
-                                    fzz = f2add(fzz, two);
-                                    atomicMin(col, __float_as_uint(f2lo(d)));
-                                    atomicMin(col + 256, __float_as_uint(f2hi(d)));
-                                }
-                                if (z == zb) {
-                                    const float dz = fsub(L.z, f2lo(fzz));
-                                    atomicMin(col, __float_as_uint(__fmaf_rn(dz, dz, dxy)));
-                                }
-                            }
-                        }
+                    for (; z < zb; z += 2, col += 512) {  // two z per step, packed FP32
+                        const f32x2 dz = f2sub(pzz, fzz);
+                        const f32x2 d = f2fma(dz, dz, dxy2);
+                        fzz = f2add(fzz, two);
+                        atomicMin(col, __float_as_uint(f2lo(d)));
+                        atomicMin(col + 256, __float_as_uint(f2hi(d)));
+                    }
+                    if (z == zb) {
+                        const float dz = fsub(L.z, f2lo(fzz));
+                        atomicMin(col, __float_as_uint(__fmaf_rn(dz, dz, dxy)));
                     }
                 }
             }
