@@ -3,14 +3,14 @@ first grid creation (tune_table.json beside the library, or $GBVDB_TUNE_TABLE).
 
 For each bucket a representative size is timed on three seeded workloads (a thick
 shell with density r = R = rho = 1; dam-break fluid particles with r = R = 4 and a
-level set of rho = 2; sphere surfaces in 4096^3 with density rho = 1.5 and grid
-(4,4,3,4)).  The binning settings (points per thread of the count and scatter
+level set of rho = 2, on their third frame, an incremental rebuild; sphere surfaces
+in 4096^3 with density rho = 1.5 and grid (4,4,3,4)).  The binning settings (points per thread of the count and scatter
 passes) are chosen on the InsertPointsSubcell time, the gather settings (dense-form
 threshold, resident blocks per SM) on the gather time; each candidate's time is
 taken relative to the best candidate of its workload and the lowest mean wins.
 Results do not depend on the settings, only times do.
 
-    python gvdb-voxels_gb300/tune.py [--out PATH] [--reps 3]
+    python gvdb-voxels_gb300/tune.py [--out PATH] [--reps 5]
 """
 import argparse
 import json
@@ -26,19 +26,22 @@ sys.path.insert(0, PKG)
 BUCKETS = [(30_000, 10_000), (300_000, 100_000), (1_500_000, 1_000_000), (8_000_000, 4_194_304),
            (1 << 62, 16_777_216)]
 BIN = [(u, s) for u in (1, 2, 4) for s in (2, 4, 8)]
-GATHER = [(d, b) for d in (1024, 2048, 4096, 8192) for b in (10, 8)]
+GATHER = [(d, b) for d in (1024, 2048, 4096, 8192, 16384, 32768) for b in (10, 8)]
 
 
 def workloads(n, seed):
     import datasets
 
     shell = datasets.shell(n, seed=seed)
-    pos, _ = datasets.fluid(n, seed=seed + 1)
+    pos, vel = datasets.fluid(n, seed=seed + 1)
+    # the fluid is timed on its third frame (p += 0.5 v per frame): an incremental
+    # rebuild, as in a running simulation
+    fluid = [(pos + 0.5 * (k + 1) * vel).astype(np.float32) for k in range(3)]
     surf = datasets.surface(n, seed=seed + 2)
     surf = surf[np.all(surf >= 0, axis=1)]
-    return [("shell", shell, (3, 3, 3, 4), 0, 1.0, 1.0, (16, 16, 1)),
-            ("fluid", pos, (3, 3, 3, 4), 1, 4.0, 2.0, (16, 16, 1)),
-            ("surface", surf, (4, 4, 3, 4), 0, 1.5, 1.5, (64, 64, 1))]
+    return [("shell", [shell], (3, 3, 3, 4), 0, 1.0, 1.0, (16, 16, 1)),
+            ("fluid", fluid, (3, 3, 3, 4), 1, 4.0, 2.0, (16, 16, 1)),
+            ("surface", [surf], (4, 4, 3, 4), 0, 1.5, 1.5, (64, 64, 1))]
 
 
 def time_calls(torch, stream, fn, reps):
@@ -54,16 +57,17 @@ def time_calls(torch, stream, fn, reps):
 
 
 def tune_workload(gbvdb, torch, wl, reps):
-    name, pts, dims, mode, r, rho, axis = wl
+    name, frames, dims, mode, r, rho, axis = wl
     stream = torch.cuda.current_stream()
     g = gbvdb.Grid(0, dims, stream=stream)
     g.set_tuning(gbvdb.TUNE_TABLE, 0)
     g.set_channel_default(*axis)
     g.add_channel(0)
-    d = torch.from_numpy(np.ascontiguousarray(pts, dtype=np.float32)).cuda()
-    n = g.set_points(d)
-    g.rebuild_topology(n, r)
-    g.update_atlas()
+    for pts in frames:  # the last frame's topology is the one timed
+        d = torch.from_numpy(np.ascontiguousarray(pts, dtype=np.float32)).cuda()
+        n = g.set_points(d)
+        g.rebuild_topology(n, r)
+        g.update_atlas()
     state = {}
 
     def insert():
@@ -107,7 +111,7 @@ def main():
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(PKG, "tune_table.json"))
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--reps", type=int, default=5)
     args = ap.parse_args()
     build_lib.build()
     torch.cuda.set_device(0)
