@@ -112,11 +112,14 @@ __device__ __forceinline__ int range_in_brick(int lo, int hi, int o) {
 // loads and the counting atomics of the kU points are each issued together (the pass
 // is bound by the latency of that dependent chain).  kU comes from the tuning table
 // (1, 2 or 4); measured on the fluid frame: kU = 1 or 2 (54 / 63 registers) beat 3 and
-// 4 (72 / 80 registers, fewer resident warps) by about 10 us.
+// 4 (72 / 80 registers, fewer resident warps) by about 10 us.  kU = 1 is held to 42
+// registers (6 blocks of 256 per SM, no spills): the InsertPointsSubcell stage 0.233 ->
+// 0.216 ms in a timing run of that stage alone; 8 blocks spill and lose.
 template <int kU>
-__global__ void k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
-                            const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ nbmask,
-                            uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
+__global__ void __launch_bounds__(256, kU == 1 ? 6 : (kU == 2 ? 4 : 1))
+    k_bin_count(TreeView t, LeafGrid lg, PointSrc p, float3 trans, float R, Quant qz,
+                const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ nbmask, uint32_t* bin_cnt,
+                int* bin_of, uint32_t* rank_of, unsigned long long* totals) {
     // kU = 4: four consecutive points per thread, their positions in three 16-byte loads
     // (load_pos4); kU = 1, 2: points kU grid strides apart
     constexpr bool kConsec = kU == 4;
@@ -964,6 +967,9 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
             // front (one memory round trip per group instead of one per bin)
             bool done = false;
             for (int g0 = 0; g0 < noffs && !done; g0 += 32) {
+                // sorted by lb^2: a group starting at or beyond wmax ends the subcell (tested
+                // before the group's bin ranges are loaded)
+                if ((float)__ldg(&offs[g0].w) >= wmax) break;
                 const int e = g0 + lane;
                 uint32_t gbeg = 0, gcnt = 0;
                 int gneed = 0;
@@ -987,8 +993,6 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
                         }
                     }
                 }
-                // sorted by lb^2: a group starting at or beyond wmax ends the subcell
-                if (__shfl_sync(0xFFFFFFFFu, glb, 0) >= wmax) break;
                 unsigned nonempty = __ballot_sync(0xFFFFFFFFu, gcnt > 0);
                 while (nonempty) {
                     const int l = __ffs(nonempty) - 1;
