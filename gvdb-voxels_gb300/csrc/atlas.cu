@@ -525,9 +525,9 @@ void launch_export_bricks(const void* interior, const void* apron, int used, int
                                                                        used, (__half*)out);
 }
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
-                           double* out, cudaStream_t s) {
+                           double* out, cudaStream_t s, int blocks_per_sm) {
     if (used > 0) {
-        unsigned blocks = (unsigned)std::min(used, 152 * 8);
+        unsigned blocks = (unsigned)std::min(used, 152 * std::max(blocks_per_sm, 1));
         if (dtype == 3)
             k_slot_sums<float><<<blocks, 256, 0, s>>>(amap, used, (const float*)interior, partials);
         else if (dtype == 100)

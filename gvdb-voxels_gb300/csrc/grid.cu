@@ -177,6 +177,14 @@ struct gbvdb_grid_s {
     // 8 bytes that the next key-count readback brings back with the counts (null: none)
     const void* rb_extra = nullptr;
     unsigned long long rb_extra_val = 0;
+    // Speculative incremental passes: the last pass's key domains (bitmap form) and, for
+    // the pass that runs on the next frame's points before their bounds are known, the
+    // device bounds brought back with its counts and whether its keys all fell inside
+    KeyDomains last_kd{};
+    int last_kd_depth = -1;
+    bool spec_pass = false, spec_failed = false;
+    const void* rb_bbox = nullptr;
+    int rb_bbox_val[6] = {0};
     int rebuild_topo = 1;
     int curr_depth = -1;
     int last_depth = 0;
@@ -432,6 +440,7 @@ struct gbvdb_grid_s {
 
     void clear_topology() {  // Clear (VG.cpp:2487-2503)
         layout_changed();
+        last_kd_depth = -1;
         for (int l = 0; l < kMaxLev; l++) { ncnt[l] = 0; nused[l] = 0; }
         nused0_stale = false;
         nbr_count = -1;
@@ -561,25 +570,34 @@ struct gbvdb_grid_s {
         return -1;
     }
 
-    void compute_bbox(long long n, float3 orig) {  // GetBoundingBox (VG.cpp:5404-5467)
+    // GetBoundingBox (VG.cpp:5404-5467): the min / max of the points into d6 (misc)
+    int* launch_compute_bbox(long long n, float3 orig) {
         int init[6];
         for (int a = 0; a < 3; a++) { init[a] = 0x7F800000; init[3 + a] = (int)(0xFF800000u ^ 0x7FFFFFFFu); }
         grow(misc, 256);
         int* d6 = ptr<int>(misc);
-        memcpy(pinned, init, sizeof(init));
-        check(cudaMemcpyAsync(d6, pinned, sizeof(init), cudaMemcpyHostToDevice, stream), "bbox init");
+        memcpy(pinned + 256, init, sizeof(init));
+        check(cudaMemcpyAsync(d6, pinned + 256, sizeof(init), cudaMemcpyHostToDevice, stream), "bbox init");
         PointSrc p = pts;
         p.n = n;
         launch_bbox(p, orig, d6, stream);
         check_launch("bbox");
-        int out[6];
-        readback(out, d6, sizeof(out));
+        return d6;
+    }
+    // mPosMin = max(0, min - 1), mPosMax = max(0, max + 2)
+    static void bbox_bounds(const int out[6], float pmin[3], float pmax[3]) {
         for (int a = 0; a < 3; a++) {
             float mn = o2f(out[a]), mx = o2f(out[3 + a]);
             float lo = mn - 1.0f, hi = mx + 2.0f;
-            posmin[a] = 0 > lo ? 0 : lo;
-            posmax[a] = 0 > hi ? 0 : hi;
+            pmin[a] = 0 > lo ? 0 : lo;
+            pmax[a] = 0 > hi ? 0 : hi;
         }
+    }
+    void compute_bbox(long long n, float3 orig) {
+        int* d6 = launch_compute_bbox(n, orig);
+        int out[6];
+        readback(out, d6, sizeof(out));
+        bbox_bounds(out, posmin, posmax);
     }
 
     // key domains of levels [0, depth): node coordinates that any pass can emit,
@@ -630,11 +648,17 @@ struct gbvdb_grid_s {
         int errflag = 0;
         check(cudaMemcpyAsync(pinned + 4 * (depth + 1), ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
         if (rb_extra) check(cudaMemcpyAsync(pinned + 128, rb_extra, 8, cudaMemcpyDeviceToHost, stream), "rb");
+        if (rb_bbox) check(cudaMemcpyAsync(pinned + 160, rb_bbox, 24, cudaMemcpyDeviceToHost, stream), "rb");
         n_readback++;
         sync();
         memcpy(at.data(), pinned, 4 * (depth + 1));
         memcpy(&errflag, pinned + 4 * (depth + 1), 4);
         if (rb_extra) memcpy(&rb_extra_val, pinned + 128, 8);
+        if (rb_bbox) memcpy(rb_bbox_val, pinned + 160, 24);
+        if (spec_pass && errflag) {  // a key outside the guessed domains: the pass is redone
+            spec_failed = true;
+            return at;
+        }
         if (errflag & 2)
             throw StatusError{GBVDB_INVALID_ARG, "a point's activation box spans more than 2^26 nodes of one level"};
         if (errflag) throw StatusError{GBVDB_CAPACITY, "node key outside its key domain"};
@@ -873,18 +897,66 @@ struct gbvdb_grid_s {
             }
             mark();
         }
+        last_kd = kd;
+        last_kd_depth = hashed ? -1 : D;
     }
 
-    void activate_incremental(long long n, float radius, float3 orig, int D, bool accum) {
+    // The last pass's key domains one node wider on each side, clipped to the root: the
+    // domains an incremental pass guesses before the frame's bounds are read back
+    bool widened_last_domains(int D, int rl, KeyDomains* out, long long* total_bits) const {
+        KeyDomains kd{};
+        long long bit = 0;
+        const long long rg_root = range[rl];
+        for (int l = 0; l < D; l++) {
+            KeyDomain& d = kd.d[l];
+            for (int a = 0; a < 3; a++) {
+                long long lo = (long long)last_kd.d[l].lo[a] - 1, hi = (long long)last_kd.d[l].lo[a] + last_kd.d[l].dim[a];
+                const long long rlo = (long long)root_pos[a] >> lgrange[l];
+                const long long rhi = ((long long)root_pos[a] + rg_root - 1) >> lgrange[l];
+                lo = std::max(std::max(lo, rlo), 0ll);
+                hi = std::min(hi, rhi);
+                if (hi < lo) hi = lo;
+                d.lo[a] = (int)lo;
+                d.dim[a] = (int)(hi - lo + 1);
+            }
+            d.bitbase = bit;
+            d.nbits = (long long)d.dim[0] * d.dim[1] * d.dim[2];
+            bit += (d.nbits + 31) & ~31ll;
+        }
+        *out = kd;
+        *total_bits = bit;
+        return bit <= kMaxBits;
+    }
+    static bool domains_contain(const KeyDomains& outer, const KeyDomains& inner, int D) {
+        for (int l = 0; l < D; l++)
+            for (int a = 0; a < 3; a++)
+                if (inner.d[l].lo[a] < outer.d[l].lo[a] ||
+                    (long long)inner.d[l].lo[a] + inner.d[l].dim[a] > (long long)outer.d[l].lo[a] + outer.d[l].dim[a])
+                    return false;
+        return true;
+    }
+
+    // guess (speculative pass): run on the last pass's widened domains while the frame's
+    // bounds are computed on the device; they come back with the key counts, and the pass
+    // stands only if the frame keeps its depth and all its keys lie in the guessed
+    // domains (then the key sets, and so the pools, are those of the exact domains).
+    // Returns false when it does not stand; nothing but scratch was written then.
+    bool activate_incremental(long long n, float radius, float3 orig, int D, bool accum, bool guess = false) {
         long long nleaf = ncnt[0];
-        if (nleaf == 0) return;  // VG.cpp:1022
-        grow(markers, (size_t)nleaf * 4);
-        launch_init_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), accum ? 1 : 0, stream);
-        check_launch("init_markers");
+        if (nleaf == 0) return !guess;  // VG.cpp:1022
         long long bits = 0;
         float margin = 2.0f * std::max(radius, 0.0f) + 4.0f;
         int rl = root_lev >= 0 ? root_lev : D;
-        KeyDomains kd = domains(D, margin, root_pos, rl, &bits);
+        KeyDomains kd{};
+        if (guess) {
+            if (!widened_last_domains(D, rl, &kd, &bits) || choose_hashed(bits, n * D)) return false;
+            rb_bbox = launch_compute_bbox(n, orig);
+        } else {
+            kd = domains(D, margin, root_pos, rl, &bits);
+        }
+        grow(markers, (size_t)nleaf * 4);
+        launch_init_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), accum ? 1 : 0, stream);
+        check_launch("init_markers");
         hashed = choose_hashed(bits, n * D);
         PointSrc p = pts;
         p.n = n;
@@ -896,6 +968,8 @@ struct gbvdb_grid_s {
         // leaves they are the flagged-leaf count, so UpdateAtlas needs no readback of its own
         unsigned long long* kept = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 72);
         rb_extra = kept;
+        spec_pass = guess;
+        spec_failed = false;
         std::vector<uint32_t> at = key_pass(D, kd, bits, nleaf / 4 + 1024, 4 * n + 1024, [&](const KeySets& ks) {
             launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
                             ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, stream);
@@ -904,8 +978,24 @@ struct gbvdb_grid_s {
             check_launch("count_markers");
         });
         rb_extra = nullptr;
+        rb_bbox = nullptr;
+        spec_pass = false;
+        if (guess) {
+            if (spec_failed) return false;
+            float pmin[3], pmax[3];
+            bbox_bounds(rb_bbox_val, pmin, pmax);
+            for (int a = 0; a < 3; a++) { posmin[a] = pmin[a]; posmax[a] = pmax[a]; }
+            int rpos[3];
+            if (determine_depth(rpos) != D) return false;  // the caller's full path clears the tree
+            long long exact_bits = 0;
+            if (!domains_contain(kd, domains(D, margin, root_pos, rl, &exact_bits), D)) return false;
+        }
         mark();
-        if (at[(size_t)D] == 0) return;
+        if (at[(size_t)D] == 0) {
+            last_kd = kd;
+            last_kd_depth = hashed ? -1 : D;
+            return true;
+        }
         launch_apply_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), stream);
         check_launch("apply_markers");
         allocate_counted(D, kd, at);
@@ -922,7 +1012,10 @@ struct gbvdb_grid_s {
         // plus the new ones
         nused[0] = (long long)rb_extra_val + ((long long)at[1] - (long long)at[0]);
         nused0_stale = false;
+        last_kd = kd;
+        last_kd_depth = hashed ? -1 : D;
         mark();
+        return true;
     }
 
     // the flagged-leaf count, when an incremental rebuild left it to be counted
@@ -945,6 +1038,18 @@ struct gbvdb_grid_s {
         if (!pts.base) throw StatusError{GBVDB_INVALID_ARG, "SetPoints was not called"};
         if (pts.n > 0 && n > pts.n) throw StatusError{GBVDB_INVALID_ARG, "num_pnts exceeds the point buffer"};
         stage_begin();
+        // an incremental frame of unchanged depth: its key pass runs on the last pass's
+        // domains, widened, with the frame's bounds read back together with the key counts
+        // instead of before the pass (one host round trip less); otherwise, or when the
+        // guess does not stand, the pass on the exact domains below
+        if (!accumulate && !rebuild_topo && curr_depth > 0 && last_kd_depth == curr_depth &&
+            activate_incremental(n, radius, orig, curr_depth, false, true)) {
+            last_depth = curr_depth;
+            sc_valid = false;
+            lists_valid = false;
+            stage_end();
+            return GBVDB_OK;
+        }
         compute_bbox(n, orig);
         mark();
         int rpos[3];

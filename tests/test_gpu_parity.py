@@ -458,3 +458,21 @@ def test_checksum_overlap_is_ordered_before_the_next_gather(gpu_lib):
     torch.cuda.synchronize()
     assert host.tolist() == expect
     assert dev.cpu().tolist() == expect
+
+
+def test_incremental_frames_after_a_jump(gpu_lib):
+    """Incremental frames run their key pass on the last pass's key domains, widened by a
+    node, and read the frame's bounds back with the key counts; a frame whose keys leave
+    those domains (here all points jump 40 voxels in x) is redone on its exact domains.
+    Every frame against the oracle."""
+    pos, vel = _mini_fluid(n=30000, seed=17)
+    f1 = pos
+    f2 = (pos + 0.5 * vel).astype(np.float32)
+    f3 = (f2 + 0.5 * vel).astype(np.float32)
+    f4 = (f3 + np.array([40.0, 0.0, 0.0], np.float32)).astype(np.float32)
+    f5 = (f4 + 0.5 * vel).astype(np.float32)
+    frames = [np.maximum(f, 0.0).astype(np.float32) for f in (f1, f2, f3, f4, f5)]
+    _, o = H.run_oracle(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    _, g = H.run_gpu(None, frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0)
+    for k in range(len(frames)):
+        _full_check(o[k], g[k], 3.0)
