@@ -942,6 +942,14 @@ struct gbvdb_grid_s {
     // domains (then the key sets, and so the pools, are those of the exact domains).
     // Returns false when it does not stand; nothing but scratch was written then.
     bool activate_incremental(long long n, float radius, float3 orig, int D, bool accum, bool guess = false) {
+        struct RbReset {  // the pass's readback extras end with it, thrown out of or not
+            gbvdb_grid_s* g;
+            ~RbReset() {
+                g->rb_extra = nullptr;
+                g->rb_bbox = nullptr;
+                g->spec_pass = false;
+            }
+        } rb_reset{this};
         long long nleaf = ncnt[0];
         if (nleaf == 0) return !guess;  // VG.cpp:1022
         long long bits = 0;
