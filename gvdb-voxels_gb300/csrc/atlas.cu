@@ -286,7 +286,7 @@ __global__ void k_slot_sums(const AtlasNode* __restrict__ amap, int used, const 
     for (int j = blockIdx.x; j < used; j += gridDim.x) {
         const int s = used - 1 - j;
         float hi = 0.0f, lo = 0.0f;
-        if (amap[s].leaf >= 0) {
+        if (amap == nullptr || amap[s].leaf >= 0) {  // null: every slot below used is assigned
             // all of this thread's 16-byte loads of the brick in flight together
             const uint4* src = reinterpret_cast<const uint4*>(interior + (size_t)s * 4096);
             constexpr int kLoads = 4096 / V / 256;

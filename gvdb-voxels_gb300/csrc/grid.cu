@@ -1097,6 +1097,9 @@ struct gbvdb_grid_s {
     // ------------------------------------------------------------- atlas
     void resize_channels(long long slots) {
         layout_changed();
+        bool grows = false;
+        for (int c = 0; c < 8; c++) grows |= ch[c].used && ch[c].cap_slots < slots;
+        if (grows) join_side();  // an overlapped checksum still reads the interiors being moved
         for (int c = 0; c < 8; c++) {
             Channel& C = ch[c];
             if (!C.used || C.cap_slots >= slots) continue;
@@ -2138,7 +2141,7 @@ gbvdb_status gbvdb_finish_topology(gbvdb_grid g, int commit_pool, int compute_bo
 }
 
 gbvdb_status gbvdb_update_atlas(gbvdb_grid g) {
-    GBVDB_GUARD(g)
+    GBVDB_GUARD_NOJOIN(g)  // joins an overlapped checksum only when the atlas grows (resize_channels)
     return g->update_atlas();
     GBVDB_END(g)
 }
@@ -2396,7 +2399,10 @@ gbvdb_status gbvdb_checksum_overlap(gbvdb_grid g, int chan, double* dev_out, dou
     g->grow(g->csum_part, (size_t)std::max(g->atlas_last, 1) * 8);
     g->check(cudaEventRecord(g->side_start, g->stream), "side event");
     g->check(cudaStreamWaitEvent(g->side, g->side_start, 0), "side wait");
-    launch_checksum_slots(g->ptr<AtlasNode>(g->amap), g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
+    // the atlas map is not read (UpdateAtlas assigns slots 0 .. atlas_last - 1), so the
+    // next frame's UpdateAtlas may rewrite it while this runs; the interiors are waited
+    // for by their next writer (a gather, a fill, or an atlas that grows)
+    launch_checksum_slots(nullptr, g->atlas_last, g->ch[chan].dtype, g->ch[chan].interior.p,
                           g->ptr<double>(g->csum_part), dev_out, g->side);
     g->check_launch("checksum");
     if (host_out) g->check(cudaMemcpyAsync(host_out, dev_out, 8, cudaMemcpyDeviceToHost, g->side), "checksum copy");

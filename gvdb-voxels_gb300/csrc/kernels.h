@@ -151,7 +151,8 @@ void launch_sort_points(PointSrc p, float3 trans, const int* pnode, const uint32
 void launch_scatter_density(const Node* leaves, long long nleaf, const uint32_t* goff, const float* pts3, float radius,
                             int expand, int res0, int ax, int ay, float* interior, float* apron, cudaStream_t s);
 // deterministic FP64 channel sum: per-slot partials, then one fixed-order block (the
-// grid size, blocks_per_sm x 152 at most, does not change the result)
+// grid size, blocks_per_sm x 152 at most, does not change the result); amap null: the
+// slots below used are all assigned (as UpdateAtlas leaves them), no map is read
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
                            double* out, cudaStream_t s, int blocks_per_sm = 8);
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value,
