@@ -257,10 +257,10 @@ struct gbvdb_grid_s {
     long long nbr_count = -1;
     DevBuf csum_part;  // per-slot partial sums of gbvdb_checksum_device
     // Side stream of gbvdb_checksum_overlap: the checksum of a frame reads the channel
-    // interiors while the grid's stream goes on with the next frame's topology and
-    // binning; every entry point that writes or reallocates interiors or the atlas map
-    // (all but the topology, binning and accessor calls) first makes the grid's stream
-    // wait for it on the device (join_side).
+    // interiors (not the atlas map) while the grid's stream goes on with the next frame's
+    // topology, atlas and binning; every entry point that writes or reallocates the
+    // interiors (all but the topology, atlas, binning and accessor calls; UpdateAtlas when
+    // the atlas grows) first makes the grid's stream wait for it on the device (join_side).
     cudaStream_t side = nullptr;
     cudaEvent_t side_start = nullptr, side_done = nullptr;
     // a readback's copies are done: the host waits on this instead of the whole stream

@@ -227,10 +227,10 @@ GBVDB_API gbvdb_status gbvdb_checksum(gbvdb_grid g, int chan, double* out);
 GBVDB_API gbvdb_status gbvdb_checksum_device(gbvdb_grid g, int chan, double* dev_out);
 /* gbvdb_checksum_device issued on the grid's own side stream (no counterpart in the
  * reference): ordered after the grid's work so far, it runs while the grid's stream
- * goes on (a frame's checksum overlaps the next frame's topology and binning); every
- * later entry point of the grid that writes or reallocates channel interiors or the
- * atlas map (all but the topology, binning and accessor calls) makes the grid's stream
- * wait for it first.  dev_out (device) receives the FP64 sum and host_out (pinned host
+ * goes on (a frame's checksum overlaps the next frame's topology, atlas and binning);
+ * it reads the channel interiors only, so every later entry point of the grid that
+ * writes or reallocates them (the gathers, fills, apron and operator calls, and an
+ * UpdateAtlas that grows the atlas) makes the grid's stream wait for it first.  dev_out (device) receives the FP64 sum and host_out (pinned host
  * memory, may be NULL) its copy, both on the side stream.  gbvdb_join makes the grid's
  * stream wait for it explicitly: after gbvdb_join and a synchronisation of the grid's
  * stream, host_out holds the sum. */
