@@ -229,7 +229,8 @@ struct gbvdb_grid_s {
     uint32_t offs_T = 0;
 
     // scratch
-    DevBuf bitmap, touched, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    long long touched_off = 0;  // the touched bitmap follows the key bitmap in one buffer (words)
     DevBuf touch_dirs;          // per home leaf position: the directions its points' boxes cover
     bool touch_dirs_on = true;  // GBVDB_TUNE_TOUCH_DIRS
     // sparse key sets (hash tables of key bits) for domains too large or too sparse for
@@ -751,7 +752,7 @@ struct gbvdb_grid_s {
     // markers, so a repeat gives the same sets).  est_keys / est_touched: expected set sizes.
     template <class Gen>
     std::vector<uint32_t> key_pass(int depth, const KeyDomains& kd, long long bits, long long est_keys,
-                                   long long est_touched, Gen gen) {
+                                   long long est_touched, Gen gen, bool err_ready = false) {
         for (int attempt = 0;; attempt++) {
             if (hashed) {
                 clear_hash(khash, khash_cap, std::min(est_keys, bits));
@@ -759,7 +760,7 @@ struct gbvdb_grid_s {
                 grow(misc, 256);
                 check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
             } else {
-                clear_bitmap(bits);
+                clear_bitmap(bits, err_ready);
             }
             gen(key_sets());
             if (!hashed) return count_bitmap(depth, kd, bits);
@@ -827,14 +828,17 @@ struct gbvdb_grid_s {
         }
     }
 
-    void clear_bitmap(long long total_bits) {
-        grow(bitmap, (size_t)(total_bits / 8) + 64);
-        check(cudaMemsetAsync(bitmap.p, 0, (size_t)(total_bits / 8), stream), "bitmap clear");
-        grow(touched, (size_t)(total_bits / 8) + 64);
-        check(cudaMemsetAsync(touched.p, 0, (size_t)(total_bits / 8), stream), "touched clear");
+    // the key and touched bitmaps, one buffer, one clear (err_ready: the pass's error
+    // flag was cleared by its setup launch)
+    void clear_bitmap(long long total_bits, bool err_ready = false) {
+        const long long words = ((total_bits / 32) + 63) & ~63ll;  // 256-byte aligned
+        touched_off = words;
+        grow(bitmap, (size_t)(2 * words) * 4 + 64);
+        check(cudaMemsetAsync(bitmap.p, 0, (size_t)(2 * words) * 4, stream), "bitmap clear");
         grow(misc, 256);
-        check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
+        if (!err_ready) check(cudaMemsetAsync(ptr<int>(misc) + 8, 0, 4, stream), "err clear");
     }
+    uint32_t* touched_bits() { return ptr<uint32_t>(bitmap) + touched_off; }
 
     static constexpr long long kMaxBits = 1ll << 34;
 
@@ -885,7 +889,7 @@ struct gbvdb_grid_s {
             int rlo[3], rhi[3];
             for (int a = 0; a < 3; a++) { rlo[a] = rpos[a]; rhi[a] = (int)std::min<long long>(rpos[a] + range[D], 0x7FFFFFFF); }
             at = key_pass(D, kd, bits, (long long)at[(size_t)D] + 1024, 4 * n + 1024, [&](const KeySets& ks) {
-                launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, ptr<uint32_t>(touched),
+                launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, touched_bits(),
                                 ptr<uint32_t>(bitmap), nullptr, ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd),
                                 ks, stream);
                 check_launch("keys_extra");
@@ -958,13 +962,25 @@ struct gbvdb_grid_s {
         KeyDomains kd{};
         if (guess) {
             if (!widened_last_domains(D, rl, &kd, &bits) || choose_hashed(bits, n * D)) return false;
-            rb_bbox = launch_compute_bbox(n, orig);
         } else {
             kd = domains(D, margin, root_pos, rl, &bits);
         }
+        // markers, the error flag, the kept-leaf counter and (a guess) the bounds' initial
+        // values in one launch, then (a guess) the bounds
         grow(markers, (size_t)nleaf * 4);
-        launch_init_markers(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), accum ? 1 : 0, stream);
-        check_launch("init_markers");
+        grow(misc, 256);
+        unsigned long long* kept = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 72);
+        int* d6 = guess ? ptr<int>(misc) : nullptr;
+        launch_incr_setup(ptr<Node>(nodes[0]), nleaf, ptr<int>(markers), accum ? 1 : 0, ptr<int>(misc) + 8, kept, d6,
+                          stream);
+        check_launch("incr_setup");
+        if (guess) {
+            PointSrc pb = pts;
+            pb.n = n;
+            launch_bbox(pb, orig, d6, stream);
+            check_launch("bbox");
+            rb_bbox = d6;
+        }
         hashed = choose_hashed(bits, n * D);
         PointSrc p = pts;
         p.n = n;
@@ -974,17 +990,18 @@ struct gbvdb_grid_s {
         // count new keys before touching the tree: nothing missing -> return (VG.cpp:1066).
         // The kept leaves (non-zero markers) come back with the counts: with the new
         // leaves they are the flagged-leaf count, so UpdateAtlas needs no readback of its own
-        unsigned long long* kept = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 72);
         rb_extra = kept;
         spec_pass = guess;
         spec_failed = false;
         std::vector<uint32_t> at = key_pass(D, kd, bits, nleaf / 4 + 1024, 4 * n + 1024, [&](const KeySets& ks) {
-            launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, ptr<uint32_t>(touched), ptr<uint32_t>(bitmap),
+            // (the sparse form may run the pass again: its count starts from zero each time)
+            if (hashed) check(cudaMemsetAsync(kept, 0, 8, stream), "kept clear");
+            launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, touched_bits(), ptr<uint32_t>(bitmap),
                             ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, stream);
             check_launch("keys_incr");
             launch_count_markers(ptr<int>(markers), nleaf, kept, stream);
             check_launch("count_markers");
-        });
+        }, true);
         rb_extra = nullptr;
         rb_bbox = nullptr;
         spec_pass = false;
@@ -1915,7 +1932,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
                       &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab, &g->sorted_clr,
@@ -2598,7 +2615,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->sorted_clr, &g->list_cnt, &g->list_off, &g->list_pts, &g->list_clr,
                             &g->offs_buf, &g->lgrid,
-                            &g->touched, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
+                            &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
                             &g->nbmask, &g->gtab, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp,

@@ -112,13 +112,16 @@ void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long wo
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s);
 // tag: ncnt[lev+1]*res^3 ints, slot_of: count long longs (scratch)
 void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s);
-void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s);
 void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s);
 void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s);
 void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s);
 void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s);
-// *out = non-zero markers (cleared by the launcher)
+// *out += non-zero markers (cleared by the caller)
 void launch_count_markers(const int* markers, long long n, unsigned long long* out, cudaStream_t s);
+// incremental pass setup: markers (0 or the old flags), *err = 0, *kept = 0, and bbox6
+// (when set) to the bounds' initial values
+void launch_incr_setup(const Node* leaves, long long n, int* markers, int accum, int* err, unsigned long long* kept,
+                       int* bbox6, cudaStream_t s);
 void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s);
 
 // ---- atlas.cu

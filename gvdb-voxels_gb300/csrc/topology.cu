@@ -496,13 +496,19 @@ __global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_
     }
 }
 
-// a warp per touched-bitmap word of level `lev`, a lane per bit: getPosParent(pos, lev)
-// for every touched position; missing -> key bit, reachable leaf -> marker
-__global__ void k_resolve_touched(TreeView t, LeafGrid lg, int lev, KeyDomain d, const uint32_t* __restrict__ touched,
-                                  uint32_t* keys, int* markers) {
+// a warp per touched-bitmap word of levels [0, depth) (their words follow each other:
+// each level's bitbase is word aligned), a lane per bit: getPosParent(pos, lev) for every
+// touched position; missing -> key bit, reachable leaf -> marker
+__global__ void k_resolve_touched(TreeView t, LeafGrid lg, int depth, KeyDomains dom,
+                                  const uint32_t* __restrict__ touched, uint32_t* keys, int* markers) {
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = g >> 5, w0 = d.bitbase >> 5, nw = (d.nbits + 31) >> 5;
-    if (w >= nw) return;  // whole warps leave together (blockDim is a multiple of 32)
+    const long long wg = g >> 5;  // global word
+    int lev = -1;
+    for (int l = 0; l < depth; l++)
+        if (wg >= (dom.d[l].bitbase >> 5) && wg < (dom.d[l].bitbase >> 5) + ((dom.d[l].nbits + 31) >> 5)) lev = l;
+    if (lev < 0) return;  // whole warps leave together (blockDim is a multiple of 32)
+    const KeyDomain& d = dom.d[lev];
+    const long long w0 = d.bitbase >> 5, w = wg - w0;
     const int b = (int)(g & 31);
     const uint32_t bits = touched[w0 + w];
     bool miss = false;
@@ -704,9 +710,24 @@ __global__ void k_build_leaf_grid(TreeView t, long long n, int* cells, int3 lo, 
     cells[((long long)bx * dim.y + by) * dim.z + bz] = (int)i;
 }
 
-__global__ void k_init_markers(const Node* leaves, long long n, int* markers, int accum) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// the setup of an incremental pass in one launch: the leaf markers (InitMarkers:
+// 0, or the old flags when accumulating), the key pass's error flag and kept-leaf
+// counter cleared, and (bbox6 set) the bounds' initial values (min +inf, max -inf as
+// ordered ints)
+__global__ void k_incr_setup(const Node* leaves, long long n, int* markers, int accum, int* err,
+                             unsigned long long* kept, int* bbox6) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) markers[i] = accum ? (int)leaves[i].flags : 0;
+    if (i == 0) {
+        *err = 0;
+        *kept = 0ull;
+        if (bbox6) {
+            for (int a = 0; a < 3; a++) {
+                bbox6[a] = 0x7F800000;
+                bbox6[3 + a] = (int)(0xFF800000u ^ 0x7FFFFFFFu);
+            }
+        }
+    }
 }
 
 __global__ void k_apply_markers(Node* leaves, long long n, const int* markers) {
@@ -897,10 +918,8 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
         // 1024 threads per block: fewer blocks flushing the parent words
         k_touch_up<<<blocks_for(nw * 32, 1024), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
     }
-    for (int lev = 0; lev < depth; lev++) {
-        long long nw = (dom.d[lev].nbits + 31) >> 5;
-        k_resolve_touched<<<blocks_for(nw * 32, 128), 128, 0, s>>>(t, lg, lev, dom.d[lev], touched, bitmap, markers);
-    }
+    const long long nw_all = (dom.d[depth - 1].bitbase + dom.d[depth - 1].nbits + 31) >> 5;
+    k_resolve_touched<<<blocks_for(nw_all * 32, 128), 128, 0, s>>>(t, lg, depth, dom, touched, bitmap, markers);
 }
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s) {
@@ -937,10 +956,6 @@ void launch_link(const TreeView& t, int lev, long long count, int* tag, long lon
     k_link_claim<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
     k_link_write<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
 }
-void launch_init_markers(const Node* leaves, long long n, int* markers, int accum, cudaStream_t s) {
-    if (n <= 0) return;
-    k_init_markers<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, markers, accum);
-}
 void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s) {
     if (n <= 0) return;
     k_apply_markers<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, markers);
@@ -953,8 +968,11 @@ void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s
     if (n <= 0) return;
     k_delink_upper<<<blocks_for(n, 128), 128, 0, s>>>(t, lev, n);
 }
+void launch_incr_setup(const Node* leaves, long long n, int* markers, int accum, int* err, unsigned long long* kept,
+                       int* bbox6, cudaStream_t s) {
+    k_incr_setup<<<blocks_for(std::max(n, 1ll), 256), 256, 0, s>>>(leaves, n, markers, accum, err, kept, bbox6);
+}
 void launch_count_markers(const int* markers, long long n, unsigned long long* out, cudaStream_t s) {
-    cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
     if (n <= 0) return;
     k_count_markers<<<grid_stride_blocks(n, 256), 256, 0, s>>>(markers, n, out);
 }
