@@ -229,7 +229,7 @@ struct gbvdb_grid_s {
     uint32_t offs_T = 0;
 
     // scratch
-    DevBuf bitmap, pcnt, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    DevBuf bitmap, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
     long long touched_off = 0;  // the touched bitmap follows the key bitmap in one buffer (words)
     DevBuf touch_dirs;          // per home leaf position: the directions its points' boxes cover
     bool touch_dirs_on = true;  // GBVDB_TUNE_TOUCH_DIRS
@@ -634,13 +634,10 @@ struct gbvdb_grid_s {
     // popcounts at each level's first word, and the total; one readback
     std::vector<uint32_t> count_bitmap(int depth, const KeyDomains& kd, long long total_bits) {
         long long nwords = total_bits / 32;
-        grow(pcnt, (size_t)(nwords + 1) * 4);
         grow(pscan, (size_t)(nwords + 1) * 4);
         grow(scan_tmp, scan_tmp_bytes(nwords));
-        launch_popc(ptr<uint32_t>(bitmap), nwords, ptr<uint32_t>(pcnt), stream);
-        check_launch("popc");
-        scan_exclusive_u32(ptr<uint32_t>(pcnt), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
-        check_launch("scan");
+        scan_exclusive_popc(ptr<uint32_t>(bitmap), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
+        check_launch("popcount scan");
         std::vector<uint32_t> at(depth + 1);
         for (int l = 0; l <= depth; l++) {
             long long w = l < depth ? kd.d[l].bitbase / 32 : nwords;
@@ -1932,7 +1929,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     if (!g) return GBVDB_INVALID_ARG;
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
-                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan,
+                      &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touch_dirs, &g->bitmap, &g->pscan,
                       &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
                       &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab, &g->sorted_clr,
@@ -2615,7 +2612,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->sorted_clr, &g->list_cnt, &g->list_off, &g->list_pts, &g->list_clr,
                             &g->offs_buf, &g->lgrid,
-                            &g->touch_dirs, &g->bitmap, &g->pcnt, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
+                            &g->touch_dirs, &g->bitmap, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
                             &g->nbmask, &g->gtab, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp,

@@ -74,6 +74,8 @@ __device__ __forceinline__ void load_pos4(const PointSrc& p, long long i0, float
 size_t scan_tmp_bytes(long long n);
 // exclusive scan of n u32 into out[0..n]; out[n] = total.  tmp: scan_tmp_bytes(n) bytes
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+// the same over the popcounts of n words (out[i] = set bits in words [0, i))
+void scan_exclusive_popc(const uint32_t* words, uint32_t* out, long long n, void* tmp, cudaStream_t s);
 // ascending sort of n distinct u64 keys, each below 2^bits (LSD radix sort, 8-bit digits;
 // one block for n <= kSortSmall); keys and alt hold n each; returns the one of the two
 // that holds the result.  tmp: sort_tmp_bytes(n) bytes
@@ -106,7 +108,6 @@ void launch_alloc_nodes_sorted(const unsigned long long* sorted, long long first
                                int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s);
-void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s);
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s);
 void launch_write_node(Node* dst, const Node& v, cudaStream_t s);

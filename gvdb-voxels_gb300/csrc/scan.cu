@@ -27,13 +27,20 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     return v;
 }
 
+// kPopc: the elements are the popcounts of the input words (a bitmap's set bits per word)
+template <bool kPopc>
+__device__ __forceinline__ uint32_t elem(const uint32_t* __restrict__ in, long long i) {
+    return kPopc ? (uint32_t)__popc(in[i]) : in[i];
+}
+
+template <bool kPopc>
 __global__ void k_tile_sums(const uint32_t* __restrict__ in, long long n, uint32_t* __restrict__ sums) {
     long long base = (long long)blockIdx.x * kTile;
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         long long i = base + (long long)k * kThreads + threadIdx.x;
-        if (i < n) s += in[i];
+        if (i < n) s += elem<kPopc>(in, i);
     }
     // block reduce
     __shared__ uint32_t red[32];
@@ -48,6 +55,7 @@ __global__ void k_tile_sums(const uint32_t* __restrict__ in, long long n, uint32
 }
 
 // each thread owns kItems consecutive elements
+template <bool kPopc>
 __global__ void k_tile_scan(const uint32_t* __restrict__ in, long long n, const uint32_t* __restrict__ tile_off,
                             uint32_t* __restrict__ out) {
     __shared__ uint32_t warp_sums[32];
@@ -57,7 +65,7 @@ __global__ void k_tile_scan(const uint32_t* __restrict__ in, long long n, const 
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         long long i = base + k;
-        v[k] = (i < n) ? in[i] : 0u;
+        v[k] = (i < n) ? elem<kPopc>(in, i) : 0u;
         s += v[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -181,23 +189,32 @@ size_t scan_tmp_bytes(long long n) {
     return bytes + 256;
 }
 
-void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+template <bool kPopc>
+static void scan_exclusive(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
         return;
     }
     long long t = ntiles(n);
     if (t == 1) {
-        k_tile_scan<<<1, kThreads, 0, s>>>(in, n, nullptr, out);
+        k_tile_scan<kPopc><<<1, kThreads, 0, s>>>(in, n, nullptr, out);
         return;
     }
     uint32_t* sums = reinterpret_cast<uint32_t*>(tmp);
     uint32_t* offs = sums + t;
     char* rest = reinterpret_cast<char*>(offs + t + 1);
     rest = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(rest) + 255) & ~uintptr_t(255));
-    k_tile_sums<<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
-    scan_exclusive_u32(sums, offs, t, rest, s);
-    k_tile_scan<<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
+    k_tile_sums<kPopc><<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
+    scan_exclusive<false>(sums, offs, t, rest, s);
+    k_tile_scan<kPopc><<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
+}
+
+void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+    scan_exclusive<false>(in, out, n, tmp, s);
+}
+
+void scan_exclusive_popc(const uint32_t* words, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+    scan_exclusive<true>(words, out, n, tmp, s);
 }
 
 static long long sort_tiles(long long n) { return (n + kSortTile - 1) / kSortTile; }

@@ -609,11 +609,6 @@ __global__ void k_key_bounds(const unsigned long long* __restrict__ sorted, cons
     at[l] = lo;
 }
 
-__global__ void k_popc(const uint32_t* __restrict__ bm, long long nwords, uint32_t* __restrict__ cnt) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += (long long)gridDim.x * blockDim.x)
-        cnt[i] = __popc(bm[i]);
-}
-
 // the node record of local key li of level lev (SetupNode, VG.cpp:2512-2524) at pool index idx
 __device__ __forceinline__ Node key_node(int lev, int lgrange, const KeyDomain& d, long long li, long long idx) {
     int rx, ry, rz;
@@ -926,10 +921,6 @@ void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const in
     if (n <= 0) return;
     k_build_leaf_grid<<<blocks_for(n, 256), 256, 0, s>>>(t, n, cells, make_int3(lo[0], lo[1], lo[2]),
                                                          make_int3(dim[0], dim[1], dim[2]), lgrange0);
-}
-void launch_popc(const uint32_t* bm, long long nwords, uint32_t* cnt, cudaStream_t s) {
-    if (nwords <= 0) return;
-    k_popc<<<grid_stride_blocks(nwords, 256), 256, 0, s>>>(bm, nwords, cnt);
 }
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
