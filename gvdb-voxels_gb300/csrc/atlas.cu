@@ -23,12 +23,6 @@ namespace gbvdb {
 
 namespace {
 
-__global__ void k_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    flag[i] = mode == 0 ? (nodes[i].flags ? 1u : 0u) : (nodes[i].parent != kUndef64 ? 1u : 0u);
-}
-
 // flagged leaves in pool order get consecutive slot ids (VG.cpp:2655-2662)
 __global__ void k_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -477,10 +471,6 @@ inline unsigned gs_blocks(long long n, int t) {
 }
 }  // namespace
 
-void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag, cudaStream_t s) {
-    if (n <= 0) return;
-    k_node_flags<<<blocks_for(n, 256), 256, 0, s>>>(nodes, n, mode, flag);
-}
 void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
                          cudaStream_t s) {
     if (n <= 0) return;

@@ -229,7 +229,7 @@ struct gbvdb_grid_s {
     uint32_t offs_T = 0;
 
     // scratch
-    DevBuf bitmap, pscan, scan_tmp, markers, flags, flags_scan, misc, xfer, link_tag, link_slot;
+    DevBuf bitmap, pscan, scan_tmp, markers, flags_scan, misc, xfer, link_tag, link_slot;
     long long touched_off = 0;  // the touched bitmap follows the key bitmap in one buffer (words)
     DevBuf touch_dirs;          // per home leaf position: the directions its points' boxes cover
     bool touch_dirs_on = true;  // GBVDB_TUNE_TOUCH_DIRS
@@ -1140,11 +1140,9 @@ struct gbvdb_grid_s {
         if (used > layer * az) az = (int)std::ceil((double)((float)used / (float)layer));
         long long F = 0;
         if (total > 0) {
-            grow(flags, (size_t)(total + 1) * 4);
             grow(flags_scan, (size_t)(total + 1) * 4);
             grow(scan_tmp, scan_tmp_bytes(total));
-            launch_node_flags(ptr<Node>(nodes[0]), total, 0, ptr<uint32_t>(flags), stream);
-            scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(flags_scan), total, scan_tmp.p, stream);
+            scan_exclusive_node_flags(ptr<Node>(nodes[0]), 0, ptr<uint32_t>(flags_scan), total, scan_tmp.p, stream);
             check_launch("atlas scan");
             if (nused0_stale) {
                 uint32_t f = 0;
@@ -1177,11 +1175,9 @@ struct gbvdb_grid_s {
     // -------------------------------------------------------- subcells
     void build_linked() {
         long long nleaf = ncnt[0];
-        grow(flags, (size_t)(nleaf + 1) * 4);
         grow(scmap, (size_t)(nleaf + 1) * 4);
         grow(scan_tmp, scan_tmp_bytes(nleaf));
-        launch_node_flags(ptr<Node>(nodes[0]), nleaf, 1, ptr<uint32_t>(flags), stream);
-        scan_exclusive_u32(ptr<uint32_t>(flags), ptr<uint32_t>(scmap), nleaf, scan_tmp.p, stream);
+        scan_exclusive_node_flags(ptr<Node>(nodes[0]), 1, ptr<uint32_t>(scmap), nleaf, scan_tmp.p, stream);
         check_launch("scmap");
         // the linked count scmap[nleaf] is read back with the binning totals
         grow(linked, (size_t)(nleaf + 1) * 4);
@@ -1930,7 +1926,7 @@ gbvdb_status gbvdb_destroy(gbvdb_grid g) {
     cudaSetDevice(g->device);
     DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                       &g->sorted, &g->list_cnt, &g->list_off, &g->list_pts, &g->offs_buf, &g->lgrid, &g->touch_dirs, &g->bitmap, &g->pscan,
-                      &g->scan_tmp, &g->markers, &g->flags, &g->flags_scan, &g->misc, &g->xfer,
+                      &g->scan_tmp, &g->markers, &g->flags_scan, &g->misc, &g->xfer,
                       &g->link_tag, &g->link_slot, &g->nbr_table, &g->pnode, &g->pndx, &g->gcnt, &g->goff,
                       &g->psort, &g->csum_part, &g->push_bad, &g->nbmask, &g->gtab, &g->sorted_clr,
                       &g->list_clr, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp, &g->kmeta};
@@ -2612,7 +2608,7 @@ size_t gbvdb_internal_device_bytes(gbvdb_grid g) {
     const DevBuf* bufs[] = {&g->amap, &g->scmap, &g->linked, &g->bin_cnt, &g->bin_off, &g->bin_of, &g->rank_of,
                             &g->sorted, &g->sorted_clr, &g->list_cnt, &g->list_off, &g->list_pts, &g->list_clr,
                             &g->offs_buf, &g->lgrid,
-                            &g->touch_dirs, &g->bitmap, &g->pscan, &g->scan_tmp, &g->markers, &g->flags,
+                            &g->touch_dirs, &g->bitmap, &g->pscan, &g->scan_tmp, &g->markers,
                             &g->flags_scan, &g->misc, &g->xfer, &g->link_tag, &g->link_slot, &g->nbr_table,
                             &g->pnode, &g->pndx, &g->gcnt, &g->goff, &g->psort, &g->csum_part, &g->push_bad,
                             &g->nbmask, &g->gtab, &g->khash, &g->thash, &g->ksorted, &g->kalt, &g->ksort_tmp,

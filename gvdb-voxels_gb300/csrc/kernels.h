@@ -76,6 +76,8 @@ size_t scan_tmp_bytes(long long n);
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
 // the same over the popcounts of n words (out[i] = set bits in words [0, i))
 void scan_exclusive_popc(const uint32_t* words, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+// the same over n nodes' flags (mode 0: mFlags != 0, mode 1: mParent defined)
+void scan_exclusive_node_flags(const Node* nodes, int mode, uint32_t* out, long long n, void* tmp, cudaStream_t s);
 // ascending sort of n distinct u64 keys, each below 2^bits (LSD radix sort, 8-bit digits;
 // one block for n <= kSortSmall); keys and alt hold n each; returns the one of the two
 // that holds the result.  tmp: sort_tmp_bytes(n) bytes
@@ -126,8 +128,6 @@ void launch_incr_setup(const Node* leaves, long long n, int* markers, int accum,
 void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s);
 
 // ---- atlas.cu
-// flag[i] = (mode 0: node.flags != 0, mode 1: node.parent != UNDEF64)
-void launch_node_flags(const Node* nodes, long long n, int mode, uint32_t* flag, cudaStream_t s);
 void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
                          cudaStream_t s);
 void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s);

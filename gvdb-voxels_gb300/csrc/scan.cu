@@ -27,20 +27,28 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     return v;
 }
 
-// kPopc: the elements are the popcounts of the input words (a bitmap's set bits per word)
-template <bool kPopc>
-__device__ __forceinline__ uint32_t elem(const uint32_t* __restrict__ in, long long i) {
-    return kPopc ? (uint32_t)__popc(in[i]) : in[i];
+// Element i of a scan's input: kind 0 the u32 value, 1 the popcount of a bitmap word,
+// 2 whether node i is flagged (mFlags != 0), 3 whether node i is linked (mParent set)
+struct ScanIn {
+    const uint32_t* words;
+    const Node* nodes;
+};
+template <int kKind>
+__device__ __forceinline__ uint32_t elem(const ScanIn& in, long long i) {
+    if (kKind == 0) return in.words[i];
+    if (kKind == 1) return (uint32_t)__popc(in.words[i]);
+    if (kKind == 2) return in.nodes[i].flags ? 1u : 0u;
+    return in.nodes[i].parent != kUndef64 ? 1u : 0u;
 }
 
-template <bool kPopc>
-__global__ void k_tile_sums(const uint32_t* __restrict__ in, long long n, uint32_t* __restrict__ sums) {
+template <int kKind>
+__global__ void k_tile_sums(ScanIn in, long long n, uint32_t* __restrict__ sums) {
     long long base = (long long)blockIdx.x * kTile;
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         long long i = base + (long long)k * kThreads + threadIdx.x;
-        if (i < n) s += elem<kPopc>(in, i);
+        if (i < n) s += elem<kKind>(in, i);
     }
     // block reduce
     __shared__ uint32_t red[32];
@@ -55,9 +63,8 @@ __global__ void k_tile_sums(const uint32_t* __restrict__ in, long long n, uint32
 }
 
 // each thread owns kItems consecutive elements
-template <bool kPopc>
-__global__ void k_tile_scan(const uint32_t* __restrict__ in, long long n, const uint32_t* __restrict__ tile_off,
-                            uint32_t* __restrict__ out) {
+template <int kKind>
+__global__ void k_tile_scan(ScanIn in, long long n, const uint32_t* __restrict__ tile_off, uint32_t* __restrict__ out) {
     __shared__ uint32_t warp_sums[32];
     long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t v[kItems];
@@ -65,7 +72,7 @@ __global__ void k_tile_scan(const uint32_t* __restrict__ in, long long n, const 
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
         long long i = base + k;
-        v[k] = (i < n) ? elem<kPopc>(in, i) : 0u;
+        v[k] = (i < n) ? elem<kKind>(in, i) : 0u;
         s += v[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -189,32 +196,37 @@ size_t scan_tmp_bytes(long long n) {
     return bytes + 256;
 }
 
-template <bool kPopc>
-static void scan_exclusive(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+template <int kKind>
+static void scan_exclusive(ScanIn in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
         return;
     }
     long long t = ntiles(n);
     if (t == 1) {
-        k_tile_scan<kPopc><<<1, kThreads, 0, s>>>(in, n, nullptr, out);
+        k_tile_scan<kKind><<<1, kThreads, 0, s>>>(in, n, nullptr, out);
         return;
     }
     uint32_t* sums = reinterpret_cast<uint32_t*>(tmp);
     uint32_t* offs = sums + t;
     char* rest = reinterpret_cast<char*>(offs + t + 1);
     rest = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(rest) + 255) & ~uintptr_t(255));
-    k_tile_sums<kPopc><<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
-    scan_exclusive<false>(sums, offs, t, rest, s);
-    k_tile_scan<kPopc><<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
+    k_tile_sums<kKind><<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
+    scan_exclusive<0>(ScanIn{sums, nullptr}, offs, t, rest, s);
+    k_tile_scan<kKind><<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
 }
 
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
-    scan_exclusive<false>(in, out, n, tmp, s);
+    scan_exclusive<0>(ScanIn{in, nullptr}, out, n, tmp, s);
 }
 
 void scan_exclusive_popc(const uint32_t* words, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
-    scan_exclusive<true>(words, out, n, tmp, s);
+    scan_exclusive<1>(ScanIn{words, nullptr}, out, n, tmp, s);
+}
+
+void scan_exclusive_node_flags(const Node* nodes, int mode, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+    if (mode == 0) scan_exclusive<2>(ScanIn{nullptr, nodes}, out, n, tmp, s);
+    else scan_exclusive<3>(ScanIn{nullptr, nodes}, out, n, tmp, s);
 }
 
 static long long sort_tiles(long long n) { return (n + kSortTile - 1) / kSortTile; }
