@@ -1201,14 +1201,16 @@ struct gbvdb_grid_s {
         long long nbins = ncnt[0] * 64;  // upper bound: bins of unlinked leaves stay empty
         grow(bin_cnt, (size_t)(nbins + 1) * 4);
         grow(bin_off, (size_t)(nbins + 1) * 4);
-        check(cudaMemsetAsync(bin_cnt.p, 0, (size_t)(nbins + 1) * 4, stream), "bin clear");
         PointSrc p = pts;
         p.n = std::max(n, 0ll);
         grow(bin_of, (size_t)std::max(p.n, 1ll) * 4);
         grow(rank_of, (size_t)std::max(p.n, 1ll) * 4);
         grow(misc, 256);
         unsigned long long* totals = reinterpret_cast<unsigned long long*>(ptr<char>(misc) + 128);
-        check(cudaMemsetAsync(totals, 0, 16, stream), "totals clear");
+        if (R > 11.0f) {  // (else the neighbour-mask pass below clears them)
+            check(cudaMemsetAsync(bin_cnt.p, 0, (size_t)(nbins + 1) * 4, stream), "bin clear");
+            check(cudaMemsetAsync(totals, 0, 16, stream), "totals clear");
+        }
         TreeView t = view();
         // InsertPointsSubcell_FP16 quantises over the bounds of the last GetBoundingBox
         // (VG.cpp:5458-5462: PosRange = PosMax - PosMin)
@@ -1222,7 +1224,7 @@ struct gbvdb_grid_s {
         const uint32_t* nbm = nullptr;
         if (R <= 11.0f) {
             grow(nbmask, (size_t)std::max(ncnt[0], 1ll) * 4);
-            launch_nb_mask(t, lgv, ncnt[0], ptr<uint32_t>(nbmask), stream);
+            launch_nb_mask(t, lgv, ncnt[0], ptr<uint32_t>(nbmask), ptr<uint32_t>(bin_cnt), totals, stream);
             nbm = ptr<uint32_t>(nbmask);
         }
         launch_bin_count(t, lgv, p, trans, R, qz, ptr<uint32_t>(scmap), nbm, ptr<uint32_t>(bin_cnt), ptr<int>(bin_of),

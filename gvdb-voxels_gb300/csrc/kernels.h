@@ -175,7 +175,9 @@ struct Quant {
     int on;
 };
 // linked flags of the 27 bricks around every linked leaf (bit (dz+1)*9 + (dy+1)*3 + (dx+1))
-void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s);
+// (bin_cnt, totals: when set, cleared too: bin_cnt[0, 64 n) and totals[0..1])
+void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, uint32_t* bin_cnt,
+                    unsigned long long* totals, cudaStream_t s);
 // nbmask (or null): from launch_nb_mask; only for R <= 11, where member ranges stay within those 27 bricks
 // unroll: points per thread per step (1, 2 or 4)
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q, const uint32_t* scmap,

@@ -87,10 +87,18 @@ __device__ __forceinline__ long long linked_leaf(const LeafGrid& lg, const TreeV
 // leaves: bit (dz+1)*9 + (dy+1)*3 + (dx+1); positions with a negative coordinate
 // count as not linked, as in the list-length count.  One warp per leaf, a lane
 // per direction.
-__global__ void k_nb_mask(TreeView t, LeafGrid lg, long long n, uint32_t* __restrict__ nbmask) {
+// Also clears the binning counters it runs before (bin_cnt: 64 per leaf, every leaf;
+// totals: 2) when they are given.
+__global__ void k_nb_mask(TreeView t, LeafGrid lg, long long n, uint32_t* __restrict__ nbmask,
+                          uint32_t* __restrict__ bin_cnt, unsigned long long* totals) {
     const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int d = threadIdx.x & 31;
+    if (totals && i == 0 && d < 2) totals[d] = 0ull;
     if (i >= n) return;
+    if (bin_cnt) {
+        bin_cnt[i * 64 + d] = 0u;
+        bin_cnt[i * 64 + 32 + d] = 0u;
+    }
     const Node& nd = t.nodes[0][i];
     if (nd.parent == kUndef64) return;
     bool on = false;
@@ -1396,9 +1404,9 @@ void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, 
     if (n <= 0) return;
     k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
 }
-void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, cudaStream_t s) {
-    if (n <= 0) return;
-    k_nb_mask<<<blocks_for(n * 32, 256), 256, 0, s>>>(t, lg, n, nbmask);
+void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, uint32_t* bin_cnt,
+                    unsigned long long* totals, cudaStream_t s) {
+    k_nb_mask<<<blocks_for(std::max(n, 1ll) * 32, 256), 256, 0, s>>>(t, lg, n, nbmask, bin_cnt, totals);
 }
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
