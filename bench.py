@@ -835,7 +835,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA kernels")
-    ap.add_argument("--e2e-repeats", type=int, default=3, help="repeats of the timed e2e loop (median reported)")
+    ap.add_argument("--e2e-repeats", type=int, default=5, help="repeats of the timed e2e loop (median reported)")
     ap.add_argument("--fluid-points", type=int, default=N_FLUID,
                     help="particles per fluid frame (default: the workload's 4,194,304; smaller for profiling)")
     ap.add_argument("--no-served", action="store_true", help="skip the served-form stream")

@@ -639,20 +639,25 @@ struct gbvdb_grid_s {
         scan_exclusive_popc(ptr<uint32_t>(bitmap), ptr<uint32_t>(pscan), nwords, scan_tmp.p, stream);
         check_launch("popcount scan");
         std::vector<uint32_t> at(depth + 1);
-        for (int l = 0; l <= depth; l++) {
-            long long w = l < depth ? kd.d[l].bitbase / 32 : nwords;
-            check(cudaMemcpyAsync(pinned + 4 * l, ptr<uint32_t>(pscan) + w, 4, cudaMemcpyDeviceToHost, stream), "rb");
-        }
-        int errflag = 0;
-        check(cudaMemcpyAsync(pinned + 4 * (depth + 1), ptr<int>(misc) + 8, 4, cudaMemcpyDeviceToHost, stream), "rb");
-        if (rb_extra) check(cudaMemcpyAsync(pinned + 128, rb_extra, 8, cudaMemcpyDeviceToHost, stream), "rb");
-        if (rb_bbox) check(cudaMemcpyAsync(pinned + 160, rb_bbox, 24, cudaMemcpyDeviceToHost, stream), "rb");
+        // the level prefixes, the error flag and the extras staged in kmeta: one copy
+        CountStage st{};
+        for (int l = 0; l <= depth; l++) st.words[l] = l < depth ? kd.d[l].bitbase / 32 : nwords;
+        st.nlev = depth;
+        st.err = ptr<int>(misc) + 8;
+        st.kept = reinterpret_cast<const unsigned long long*>(rb_extra);
+        st.bbox = reinterpret_cast<const int*>(rb_bbox);
+        grow(kmeta, 256);
+        uint32_t* stage = ptr<uint32_t>(kmeta) + 32;  // (bytes 128..255; 0..127: the sparse form's)
+        launch_stage_counts(ptr<uint32_t>(pscan), st, stage, stream);
+        check_launch("stage counts");
+        check(cudaMemcpyAsync(pinned, stage, 104, cudaMemcpyDeviceToHost, stream), "rb");
         n_readback++;
         sync();
+        int errflag = 0;
         memcpy(at.data(), pinned, 4 * (depth + 1));
-        memcpy(&errflag, pinned + 4 * (depth + 1), 4);
-        if (rb_extra) memcpy(&rb_extra_val, pinned + 128, 8);
-        if (rb_bbox) memcpy(rb_bbox_val, pinned + 160, 24);
+        memcpy(&errflag, pinned + 64, 4);
+        if (rb_extra) memcpy(&rb_extra_val, pinned + 72, 8);
+        if (rb_bbox) memcpy(rb_bbox_val, pinned + 80, 24);
         if (spec_pass && errflag) {  // a key outside the guessed domains: the pass is redone
             spec_failed = true;
             return at;

@@ -99,6 +99,17 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
                      uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, const KeySets& ks,
                      cudaStream_t s);
+// the key-count readback staged for one copy (k_stage_counts): prefix words of levels
+// [0, nlev) and the total (words[nlev]), the error flag, the kept-leaf count and the point
+// bounds (both optional)
+struct CountStage {
+    long long words[kMaxLev + 1];
+    int nlev;
+    const int* err;
+    const unsigned long long* kept;
+    const int* bbox;
+};
+void launch_stage_counts(const uint32_t* pscan, const CountStage& st, uint32_t* out, cudaStream_t s);
 // sparse form: the occupied slots of h into out (any order), their number into *count
 // (cleared by the caller)
 void launch_hash_compact(const KeyHash& h, unsigned long long* out, unsigned int* count, cudaStream_t s);

@@ -784,6 +784,17 @@ __global__ void k_count_flags(const Node* nodes, long long n, unsigned long long
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
 }
 
+// The key-count readback in one copy: out[l] = the prefix at level l's first word
+// (l <= nlev; the last entry is the total), out[16] = the pass's error flag, out[18..19]
+// = the kept-leaf count (u64), out[20..25] = the point bounds (when given)
+__global__ void k_stage_counts(const uint32_t* __restrict__ pscan, CountStage st, uint32_t* __restrict__ out) {
+    const int t = threadIdx.x;
+    if (t <= st.nlev) out[t] = pscan[st.words[t]];
+    if (t == 16) out[16] = (uint32_t)*st.err;
+    if (t == 17 && st.kept) *reinterpret_cast<unsigned long long*>(out + 18) = *st.kept;
+    if (t >= 20 && t < 26 && st.bbox) out[t] = (uint32_t)st.bbox[t - 20];
+}
+
 // leaves an incremental pass keeps flagged: the non-zero markers
 __global__ void k_count_markers(const int* markers, long long n, unsigned long long* out) {
     unsigned c = 0;
@@ -958,6 +969,9 @@ void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s) {
 void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s) {
     if (n <= 0) return;
     k_delink_upper<<<blocks_for(n, 128), 128, 0, s>>>(t, lev, n);
+}
+void launch_stage_counts(const uint32_t* pscan, const CountStage& st, uint32_t* out, cudaStream_t s) {
+    k_stage_counts<<<1, 32, 0, s>>>(pscan, st, out);
 }
 void launch_incr_setup(const Node* leaves, long long n, int* markers, int accum, int* err, unsigned long long* kept,
                        int* bbox6, cudaStream_t s) {
