@@ -17,8 +17,10 @@
 // max / min over its subcell's members, so it does not depend on visiting order:
 //   density   max(0, max_j (rho - |p_j - v|)) = max(0, rho - sqrt(min_j d_j^2))
 //   level set min(3, min_j (|p_j - v| - rho)) = min(3, sqrt(min_j d_j^2) - rho)
-// (sqrt and the subtraction are monotonic under round-to-nearest, so both forms
-// round identically).  The kernels reduce min d^2 per voxel.
+// (with a correctly rounded sqrt both forms round identically, sqrt and the
+// subtraction being monotonic).  The kernels reduce min d^2 per voxel and take its
+// square root with sqrt.approx.f32, as the reference's kernels do (they are built
+// with --use_fast_math): within one unit in the last place of the rounded root.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -447,6 +449,14 @@ __device__ __forceinline__ void push_apron(const uint32_t* tile, const int* pslo
     }
 }
 
+// PTX sqrt.approx.f32 (the reference's kernels are built with --use_fast_math, so their
+// sqrtf is this instruction too)
+__device__ __forceinline__ float sqrt_approx(float a) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+    return r;
+}
+
 // Final values from the tile of minima, one coalesced write of the brick.  keep:
 // the final values' storage bits replace the minima in the tile (fused apron).
 template <typename T>
@@ -462,7 +472,7 @@ __device__ void write_tile(const GatherParams& gp, uint32_t* tile, T* out, bool 
         if (__any_sync(__activemask(), any)) {
 #pragma unroll
             for (int k = 0; k < 4; k++)
-                if (mv[k] != gp.tbits) c[k] = __fsqrt_rn(__uint_as_float(mv[k]));
+                if (mv[k] != gp.tbits) c[k] = sqrt_approx(__uint_as_float(mv[k]));
         }
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -525,11 +535,6 @@ __device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
 __device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
     f32x2 r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-__device__ __forceinline__ float sqrt_approx(float a) {
-    float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
     return r;
 }
 __device__ __forceinline__ float fmin3(float a, float b, float c) {
