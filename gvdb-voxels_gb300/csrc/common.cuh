@@ -193,7 +193,8 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 // GetCoveringNode float version (PT.cuh:88-100) as a node coordinate
 __device__ __forceinline__ int cover_coord(float w, int lgrange) {
     float fr = (float)(1 << lgrange);
-    float np = __fmul_rn(ceilf(__fdiv_rn(w, fr)), fr);
+    // w / 2^lg as w * 2^-lg: a power-of-two scaling, exact (the same float as the division)
+    float np = __fmul_rn(ceilf(__fmul_rn(w, __int_as_float((127 - lgrange) << 23))), fr);
     int ni = (int)np;
     if (w < (float)ni) ni -= (1 << lgrange);
     return ni >> lgrange;  // ni >= 0 for w >= 0
