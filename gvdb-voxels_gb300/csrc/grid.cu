@@ -72,15 +72,20 @@ uint16_t f2h_bits(float f) {  // round to nearest even, float -> IEEE half
 }
 // ------------------------------------------------------------- tuning table
 // Per point-count bucket: the gather's dense-form threshold, the gather's resident
-// blocks per SM and the binning passes' points per thread, chosen by a tuning run
+// blocks per SM, the candidate count from which its bricks are launched first and
+// the binning passes' points per thread, chosen by a tuning run
 // (gvdb-voxels_gb300/tune.py) and read from JSON at the first grid creation:
 //   {"buckets": [{"max_points": 100000, "dense_min": 2048, "gather_blocks": 10,
-//                 "bin_unroll": 2, "scatter_unroll": 4}, ...]}
+//                 "gather_long_min": 2048, "bin_unroll": 2, "scatter_unroll": 4}, ...]}
 // from $GBVDB_TUNE_TABLE, else tune_table.json beside libgbvdb.so.  An insert or gather
 // of n points takes the first bucket with max_points >= n (the last one beyond).
+// the gather launches bricks with more candidate points than this first (tuning table
+// field gather_long_min; -1 keeps the linked order)
+constexpr int kGatherLongMin = 2048;
 struct TuneEntry {
     long long max_points = 0;
     int dense_min = 2048, gather_blocks = 10, bin_unroll = 2, scatter_unroll = 4;
+    int gather_long_min = kGatherLongMin;
 };
 struct TuneTable {
     std::vector<TuneEntry> b;
@@ -131,6 +136,7 @@ TuneTable load_tune_table() {
         e.max_points = v;
         if (json_int(obj, "dense_min", &v) && v >= 0) e.dense_min = (int)std::min<long long>(v, 1ll << 31);
         if (json_int(obj, "gather_blocks", &v)) e.gather_blocks = v == 8 ? 8 : 10;
+        if (json_int(obj, "gather_long_min", &v)) e.gather_long_min = (int)std::max(-1ll, std::min(v, 1ll << 30));
         if (json_int(obj, "bin_unroll", &v)) e.bin_unroll = (v == 1 || v == 4) ? (int)v : 2;
         if (json_int(obj, "scatter_unroll", &v)) e.scatter_unroll = (v == 2 || v == 8) ? (int)v : 4;
         t.b.push_back(e);
@@ -299,6 +305,10 @@ struct gbvdb_grid_s {
     int gather_blocks(long long n) const {
         const TuneEntry* e = tune_entry(n);
         return gather_blocks_set > 0 ? gather_blocks_set : (e ? e->gather_blocks : 10);
+    }
+    int gather_long_min(long long n) const {
+        const TuneEntry* e = tune_entry(n);
+        return e ? e->gather_long_min : kGatherLongMin;
     }
     int dense_min = 2048;
     // Dense-form threshold autotuner (on until GBVDB_TUNE_DENSE_MIN is set): the
@@ -1410,15 +1420,20 @@ struct gbvdb_grid_s {
             const TuneEntry* te = tune_auto ? tune_entry(sc_pts.n) : nullptr;
             gp.dense_min = te ? te->dense_min : tune_pick(sc_nbricks, &tslot);
             gp.min_blocks = gather_blocks(sc_pts.n);
+            // long bricks first: the gather form's and the scatter form's fullest
+            const int lm = gather_long_min(sc_pts.n);
+            gp.long_min = lm < 0 ? -1 : std::min(lm, gp.dense_min);
             // fused apron: needs the dense leaf lookup (the apron pass resolves
             // neighbours with the same table) and an apron of one voxel
             const bool push = fused_apron && lgv.cells && ch[chan].apron == 1 && atlas_last > 0;
             gp.apron = push ? ch[chan].apron_buf.p : nullptr;
             build_offsets(gp.lo_off, gp.hi_off, T, sc_R);
+            // push_bad: the push check's flag, then the gather's two launch-order counters
+            grow(push_bad, 16);
+            if (push || gp.long_min >= 0) check(cudaMemsetAsync(push_bad.p, 0, 12, stream), "push check clear");
+            gp.order = ptr<unsigned>(push_bad) + 1;
             if (push) {
-                grow(push_bad, 16);
                 gp.apron_bad = ptr<int>(push_bad);
-                check(cudaMemsetAsync(push_bad.p, 0, 4, stream), "push check clear");
                 launch_push_check(t, lgv, ptr<uint32_t>(scmap), ptr<AtlasNode>(amap), atlas_last, ax, ay, ncnt[0],
                                   ptr<int>(push_bad), stream);
             }

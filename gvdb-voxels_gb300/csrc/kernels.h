@@ -215,6 +215,10 @@ struct GatherParams {
     void* apron;
     const int* apron_bad;  // set by the push check: the grid is not in the state the push assumes
     int min_blocks;        // resident blocks per SM the gather is compiled for (10 or 8)
+    // launch order of the bricks: those with more than long_min candidate points first
+    // (< 0: linked order); order: two counters, zero before the launch
+    int long_min;
+    unsigned* order;
 };
 // fused-apron precondition (one thread per leaf); *bad must be 0 before the launch
 void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,

@@ -685,36 +685,72 @@ __global__ void k_push_check(TreeView t, LeafGrid lg, const uint32_t* __restrict
 // origin and atlas slot.  Done here with every warp's loads in flight at once,
 // so that a gather block starts from one coalesced 512-byte read instead of a
 // chain of dependent lookups.
-__global__ void k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ linked, long long nbricks,
-                              const uint32_t* __restrict__ scmap, const uint32_t* __restrict__ bin_off, int ax, int ay,
-                              int4* __restrict__ gtab) {
+//
+// Launch order (long_min >= 0): the records of the bricks with more than long_min
+// points homed around them (the gather form's bricks and the scatter form's
+// fullest, whose blocks run longest) fill the table from the front, the others
+// from the back, so that the gather starts its long blocks first and the short
+// ones fill in behind them; a long block launched late is the kernel's tail.
+// ctr[0], ctr[1] (zero on entry) count the two kinds.  The order within each kind
+// varies from run to run; the result does not (every brick writes only its own
+// slot and the apron voxels it is the one source of).  long_min < 0: linked order.
+constexpr int kPrepThreads = 256;
+__global__ void __launch_bounds__(kPrepThreads) k_gather_prep(TreeView t, LeafGrid lg, const int* __restrict__ linked,
+                                                              long long nbricks, const uint32_t* __restrict__ scmap,
+                                                              const uint32_t* __restrict__ bin_off, int ax, int ay,
+                                                              int long_min, unsigned* ctr, int4* __restrict__ gtab) {
+    __shared__ int kind[kPrepThreads / 32];  // 1 long, 0 short, -1 no brick
+    __shared__ unsigned base[2];
     const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (b >= nbricks) return;
-    const int leaf = linked[b];
-    const Node& nd = t.nodes[0][leaf];
-    const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool have = b < nbricks;
     int4 e = make_int4(-1, 0, 0, 0);
-    if (lane < 27) {
-        const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
-        int r = -1;
-        if ((dx | dy | dz) == 0) {
-            r = (int)scmap[leaf];
-        } else {
-            const int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
-            if (px >= 0 && py >= 0 && pz >= 0) {
-                const long long l = linked_leaf(lg, t, px, py, pz);
-                if (l >= 0) r = (int)scmap[l];
+    if (have) {
+        const int leaf = linked[b];
+        const Node& nd = t.nodes[0][leaf];
+        const int ox = nd.pos[0], oy = nd.pos[1], oz = nd.pos[2];
+        if (lane < 27) {
+            const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+            int r = -1;
+            if ((dx | dy | dz) == 0) {
+                r = (int)scmap[leaf];
+            } else {
+                const int px = ox + 16 * dx, py = oy + 16 * dy, pz = oz + 16 * dz;
+                if (px >= 0 && py >= 0 && pz >= 0) {
+                    const long long l = linked_leaf(lg, t, px, py, pz);
+                    if (l >= 0) r = (int)scmap[l];
+                }
             }
+            if (r >= 0) {
+                const uint32_t beg = __ldg(bin_off + (size_t)r * 64);
+                e = make_int4(r, (int)beg, (int)(__ldg(bin_off + (size_t)r * 64 + 64) - beg), 0);
+            }
+        } else if (lane == 27) {
+            e = make_int4(ox, oy, oz, slot_of_value(nd.value, ax, ay));
         }
-        if (r >= 0) {
-            const uint32_t beg = __ldg(bin_off + (size_t)r * 64);
-            e = make_int4(r, (int)beg, (int)(__ldg(bin_off + (size_t)r * 64 + 64) - beg), 0);
-        }
-    } else if (lane == 27) {
-        e = make_int4(ox, oy, oz, slot_of_value(nd.value, ax, ay));
     }
-    if (lane < 28) gtab[b * 32 + lane] = e;
+    if (long_min < 0) {
+        if (have && lane < 28) gtab[b * 32 + lane] = e;
+        return;
+    }
+    // the neighbourhood's points (the gather's candidate count)
+    const unsigned ncand = __reduce_add_sync(0xFFFFFFFFu, lane < 27 ? (unsigned)e.z : 0u);
+    const int k = have ? (ncand > (unsigned)long_min ? 1 : 0) : -1;
+    if (lane == 0) kind[warp] = k;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned n[2] = {0, 0};
+        for (int w = 0; w < kPrepThreads / 32; w++)
+            if (kind[w] >= 0) n[kind[w]]++;
+        base[1] = n[1] ? atomicAdd(ctr, n[1]) : 0u;
+        base[0] = n[0] ? atomicAdd(ctr + 1, n[0]) : 0u;
+    }
+    __syncthreads();
+    if (!have) return;
+    unsigned rank = base[k];
+    for (int w = 0; w < warp; w++) rank += kind[w] == k ? 1u : 0u;
+    const long long pos = k ? (long long)rank : nbricks - 1 - (long long)rank;
+    if (lane < 28) gtab[pos * 32 + lane] = e;
 }
 
 // One block per linked leaf.  Setup: the brick's record from k_gather_prep (the
@@ -1456,8 +1492,8 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    int4* gtab, void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
-    k_gather_prep<<<blocks_for(nbricks * 32, 256), 256, 0, s>>>(t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay,
-                                                                gtab);
+    k_gather_prep<<<blocks_for(nbricks * 32, kPrepThreads), kPrepThreads, 0, s>>>(
+        t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay, gp.long_min, gp.order, gtab);
     const unsigned nb = (unsigned)nbricks;
     if (gp.min_blocks == 8) {
         if (gp.dtype == 3)
