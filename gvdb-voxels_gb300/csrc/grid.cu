@@ -294,6 +294,7 @@ struct gbvdb_grid_s {
     }
     // explicit settings (set_tuning) win over the table; -1: table or built-in default
     int bin_unroll_set = -1, scatter_unroll_set = -1, gather_blocks_set = -1;
+    int gather_long_min_set = 0;  // GBVDB_TUNE_GATHER_LONG_MIN: 0 table / default, -1 linked order
     int bin_unroll(long long n) const {
         const TuneEntry* e = tune_entry(n);
         return bin_unroll_set > 0 ? bin_unroll_set : (e ? e->bin_unroll : 2);
@@ -307,6 +308,7 @@ struct gbvdb_grid_s {
         return gather_blocks_set > 0 ? gather_blocks_set : (e ? e->gather_blocks : 10);
     }
     int gather_long_min(long long n) const {
+        if (gather_long_min_set != 0) return gather_long_min_set;
         const TuneEntry* e = tune_entry(n);
         return e ? e->gather_long_min : kGatherLongMin;
     }
@@ -2559,6 +2561,11 @@ gbvdb_status gbvdb_set_tuning(gbvdb_grid g, int param, int64_t value) {
     if (param == GBVDB_TUNE_TOUCH_DIRS) {
         if (value != 0 && value != 1) return GBVDB_INVALID_ARG;
         g->touch_dirs_on = value != 0;
+        return GBVDB_OK;
+    }
+    if (param == GBVDB_TUNE_GATHER_LONG_MIN) {
+        if (value < -1 || value > (1ll << 30)) return GBVDB_INVALID_ARG;
+        g->gather_long_min_set = (int)value;
         return GBVDB_OK;
     }
     if (param == GBVDB_TUNE_KEYSET) {

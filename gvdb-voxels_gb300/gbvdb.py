@@ -71,6 +71,7 @@ TUNE_BIN_UNROLL = 6
 TUNE_SCATTER_UNROLL = 7
 TUNE_GATHER_BLOCKS = 8
 TUNE_KEYSET = 9
+TUNE_GATHER_LONG_MIN = 10
 FUNC_SMOOTH = 113
 
 

@@ -6,7 +6,8 @@ shell with density r = R = rho = 1; dam-break fluid particles with r = R = 4 and
 level set of rho = 2, on their third frame, an incremental rebuild; sphere surfaces
 in 4096^3 with density rho = 1.5 and grid (4,4,3,4)).  The binning settings (points per thread of the count and scatter
 passes) are chosen on the InsertPointsSubcell time, the gather settings (dense-form
-threshold, resident blocks per SM) on the gather time; each candidate's time is
+threshold, resident blocks per SM, the candidate count from which bricks launch first)
+on the gather time; each candidate's time is
 taken relative to the best candidate of its workload and the lowest mean wins.
 Results do not depend on the settings, only times do.
 
@@ -26,7 +27,8 @@ sys.path.insert(0, PKG)
 BUCKETS = [(30_000, 10_000), (300_000, 100_000), (1_500_000, 1_000_000), (8_000_000, 4_194_304),
            (1 << 62, 16_777_216)]
 BIN = [(u, s) for u in (1, 2, 4) for s in (2, 4, 8)]
-GATHER = [(d, b) for d in (1024, 2048, 4096, 8192, 16384, 32768) for b in (10, 8)]
+# gather: dense-form threshold, resident blocks per SM, long-first launch threshold (-1: linked order)
+GATHER = [(d, b, l) for d in (1024, 2048, 4096, 8192, 16384, 32768) for b in (10, 8) for l in (-1, 1024, 2048, 4096)]
 
 
 def workloads(n, seed):
@@ -87,11 +89,12 @@ def tune_workload(gbvdb, torch, wl, reps):
         t_bin[(u, s)] = time_calls(torch, stream, insert, reps)
     insert()
     t_gat = {}
-    for dm, b in GATHER:
+    for dm, b, lm in GATHER:
         g.set_tuning(gbvdb.TUNE_DENSE_MIN, dm)
         g.set_tuning(gbvdb.TUNE_GATHER_BLOCKS, b)
+        g.set_tuning(gbvdb.TUNE_GATHER_LONG_MIN, lm)
         gather()
-        t_gat[(dm, b)] = time_calls(torch, stream, gather, reps)
+        t_gat[(dm, b, lm)] = time_calls(torch, stream, gather, reps)
     g.close()
     return t_bin, t_gat
 
@@ -124,13 +127,13 @@ def main():
             gats.append(tg)
             out["measured"].append({"points": n, "workload": wl[0],
                                     "insert_ms": {"%d/%d" % kk: v for kk, v in tb.items()},
-                                    "gather_ms": {"%d/%d" % kk: v for kk, v in tg.items()}})
+                                    "gather_ms": {"%d/%d/%d" % kk: v for kk, v in tg.items()}})
         (u, s), _ = best(bins)
-        (dm, b), _ = best(gats)
+        (dm, b, lm), _ = best(gats)
         out["buckets"].append({"max_points": hi, "tuned_at": n, "dense_min": dm, "gather_blocks": b,
-                               "bin_unroll": u, "scatter_unroll": s})
-        print("bucket <= %d (tuned at %d): dense_min %d, gather_blocks %d, bin_unroll %d, scatter_unroll %d"
-              % (hi, n, dm, b, u, s), flush=True)
+                               "gather_long_min": lm, "bin_unroll": u, "scatter_unroll": s})
+        print("bucket <= %d (tuned at %d): dense_min %d, gather_blocks %d, gather_long_min %d, bin_unroll %d, "
+              "scatter_unroll %d" % (hi, n, dm, b, lm, u, s), flush=True)
     with open(args.out, "w") as f:
         json.dump(out, f, indent=1)
     print(args.out)

@@ -287,10 +287,14 @@ GBVDB_API gbvdb_status gbvdb_get_atlas_device(gbvdb_grid g, int chan, void** int
                                      tune_table.json beside libgbvdb.so; written by gvdb-voxels_gb300/tune.py), an
                                      insert or gather of n points takes its bucket's settings: the dense-form
                                      threshold (in place of the autotuner), the gather's resident blocks per SM
-                                     and the binning passes' points per thread.  0: built-in defaults. */
+                                     and launch order, and the binning passes' points per thread.  0: built-in
+                                     defaults. */
 #define GBVDB_TUNE_BIN_UNROLL 6   /* points per thread of the subcell count pass: 1, 2 or 4 (0: table / default 2) */
 #define GBVDB_TUNE_SCATTER_UNROLL 7 /* points per thread of the binning scatter: 2, 4 or 8 (0: table / default 4) */
 #define GBVDB_TUNE_GATHER_BLOCKS 8  /* resident blocks per SM the gather is built for: 10 or 8 (0: table / 10) */
+#define GBVDB_TUNE_GATHER_LONG_MIN 10 /* launch order of the gather's bricks: those with more candidate points
+                                         than this (capped at the dense-form threshold) first, the rest after;
+                                         -1: linked order; 0: table / default 2048.  Same bits either way. */
 #define GBVDB_TUNE_KEYSET 9  /* key sets of RebuildTopology's passes: per-level bitmaps over the points' key
                                 domain (bounding box plus margin, clipped to the root; cost grows with the
                                 domain, at most 2^34 node positions), or hash tables of the keys, compacted and

@@ -55,7 +55,8 @@ def snapshot_oracle(g, ln):
 
 def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1.0, mode="density",
             boundval=0.0, orig=(0, 0, 0), axiscnt=(0, 0, 0), dtype=None, accumulate=False, export_subcells=True,
-            fp16_subcells=False, dense_min=None, fused_apron=None, touch_dirs=None, unroll=None, keyset=None):
+            fp16_subcells=False, dense_min=None, fused_apron=None, touch_dirs=None, unroll=None, keyset=None,
+            long_min=None):
     import torch
 
     import gbvdb
@@ -70,6 +71,8 @@ def run_gpu(points, log2dims=(3, 3, 3, 4), frames=None, radius=1.0, R=1.0, rho=1
         g.set_tuning(gbvdb.TUNE_TOUCH_DIRS, touch_dirs)
     if keyset is not None:  # 2: RebuildTopology's key sets as hash tables (the sparse form)
         g.set_tuning(gbvdb.TUNE_KEYSET, keyset)
+    if long_min is not None:  # the gather's launch order: -1 linked, k: bricks over k candidates first
+        g.set_tuning(gbvdb.TUNE_GATHER_LONG_MIN, long_min)
     if unroll is not None:  # (points per thread of the count pass, of the scatter pass)
         g.set_tuning(gbvdb.TUNE_BIN_UNROLL, unroll[0])
         g.set_tuning(gbvdb.TUNE_SCATTER_UNROLL, unroll[1])

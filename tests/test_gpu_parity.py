@@ -164,6 +164,25 @@ def test_autotuned_threshold_gives_the_same_atlas(gpu_lib):
             assert a["checksum"] == b["checksum"]
 
 
+@pytest.mark.parametrize("dense_min", [None, 0])
+def test_gather_launch_order_gives_the_same_atlas(gpu_lib, dense_min):
+    """The gather's launch order (linked, or the bricks with many candidate points first,
+    each group in an order that varies from run to run) changes no bit of the atlas,
+    apron included: every brick writes its own slot and the apron voxels it alone
+    sources.  dense_min 0 puts every brick in the gather form, so every brick is long."""
+    pos, vel = _mini_fluid(n=40000, seed=67)
+    frames = [(pos + 0.5 * k * vel).astype(np.float32) for k in range(1, 4)]
+    kw = dict(frames=frames, radius=4.0, R=4.0, rho=2.0, mode="levelset", boundval=3.0, export_subcells=False,
+              dense_min=dense_min)
+    _, linked = H.run_gpu(None, long_min=-1, **kw)
+    for lm in (1, 200, 2048):
+        _, other = H.run_gpu(None, long_min=lm, **kw)
+        for a, b in zip(linked, other):
+            # padded bricks: interiors and aprons
+            assert np.array_equal(a["bricks"].view(np.uint8), b["bricks"].view(np.uint8))
+            assert a["checksum"] == b["checksum"]
+
+
 def test_accumulate_topology(gpu_lib):
     pos, vel = _mini_fluid(n=20000, seed=5)
     frames = [pos, (pos + 3.0 * vel).astype(np.float32), (pos - 3.0 * vel).astype(np.float32)]
