@@ -1014,25 +1014,23 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
             };
             // offsets in groups of 32: each lane resolves one offset's bin range up
             // front (one memory round trip per group instead of one per bin)
-            bool done = false;
-            for (int g0 = 0; g0 < noffs && !done; g0 += 32) {
+            for (int g0 = 0; g0 < noffs; g0 += 32) {
                 // sorted by lb^2: a group starting at or beyond wmax ends the subcell (tested
                 // before the group's bin ranges are loaded)
                 if ((float)__ldg(&offs[g0].w) >= wmax) break;
                 const int e = g0 + lane;
                 uint32_t gbeg = 0, gcnt = 0;
-                int gneed = 0;
-                float glb = INFINITY;
+                int gneed = 0, gbnd = 0;
                 if (e < noffs) {
                     const int4 o = offs[e];
-                    glb = (float)o.w;
                     gneed = member_bits(o.x, o.y, o.z);
                     const int hx = Sx + o.x, hy = Sy + o.y, hz = Sz + o.z;
                     // bound for the bin's points [4h, 4h + 4) against the needy box
                     const int gx = max(0, max(4 * hx - nhx, nlx - 4 * hx - 4));
                     const int gy = max(0, max(4 * hy - nhy, nly - 4 * hy - 4));
                     const int gz = max(0, max(4 * hz - nhz, nlz - 4 * hz - 4));
-                    if (hx >= 0 && hy >= 0 && hz >= 0 && (float)(gx * gx + gy * gy + gz * gz) < wmax) {
+                    gbnd = gx * gx + gy * gy + gz * gz;  // at most 3 * 48^2: 13 bits
+                    if (hx >= 0 && hy >= 0 && hz >= 0 && (float)gbnd < wmax) {
                         const int bx = (hx >> 2) - (sx0 >> 2), by = (hy >> 2) - (sy0 >> 2), bz = (hz >> 2) - (sz0 >> 2);
                         const int r = nrank[(bz + 1) * 9 + (by + 1) * 3 + (bx + 1)];
                         if (r >= 0) {
@@ -1044,13 +1042,14 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
                 }
                 unsigned nonempty = __ballot_sync(0xFFFFFFFFu, gcnt > 0);
                 while (nonempty) {
-                    const int l = __ffs(nonempty) - 1;
-                    nonempty &= nonempty - 1;
-                    // sorted by lb^2: the first bin at or beyond wmax ends the subcell
-                    if (__shfl_sync(0xFFFFFFFFu, glb, l) >= wmax) {
-                        done = true;
-                        break;
-                    }
+                    // the group's bins nearest the needy box first (ties: lowest lane), so that
+                    // wmax falls early; a bin whose bound is at or beyond wmax ends the group,
+                    // as every bin left is at least as far (later groups: the test above)
+                    const uint32_t kmin = __reduce_min_sync(
+                        0xFFFFFFFFu, ((nonempty >> lane) & 1u) ? ((uint32_t)gbnd << 5) | (uint32_t)lane : 0xFFFFFFFFu);
+                    const int l = (int)(kmin & 31u);
+                    nonempty &= ~(1u << l);
+                    if ((float)(kmin >> 5) >= wmax) break;
                     const uint32_t beg = __shfl_sync(0xFFFFFFFFu, gbeg, l);
                     const uint32_t end = beg + __shfl_sync(0xFFFFFFFFu, gcnt, l);
                     const int need = __shfl_sync(0xFFFFFFFFu, gneed, l);
