@@ -474,11 +474,11 @@ inline unsigned gs_blocks(long long n, int t) {
 void launch_assign_slots(Node* leaves, long long n, const uint32_t* scan, int ax, int ay, AtlasNode* amap,
                          cudaStream_t s) {
     if (n <= 0) return;
-    k_assign_slots<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scan, ax, ay, amap);
+    k_assign_slots<<<counted(blocks_for(n, 256)), 256, 0, s>>>(leaves, n, scan, ax, ay, amap);
 }
 void launch_fill_u32(uint32_t* p, long long n, uint32_t v, cudaStream_t s) {
     if (n <= 0) return;
-    k_fill_u32<<<gs_blocks(n, 256), 256, 0, s>>>(p, n, v);
+    k_fill_u32<<<counted(gs_blocks(n, 256)), 256, 0, s>>>(p, n, v);
 }
 void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, int used, int ax, int ay, int esize,
                   const void* interior, void* apron, uint32_t boundbits, const int* fill_only_bad, cudaStream_t s) {
@@ -488,19 +488,19 @@ void launch_apron(const TreeView& t, const LeafGrid& lg, const AtlasNode* amap, 
         float b;
         memcpy(&b, &boundbits, 4);
         if (fill_only && lg.cells)
-            k_apron_fill<float><<<(used + 7) / 8, 256, 0, s>>>(t, lg, amap, used, ax, ay, (const float*)interior,
+            k_apron_fill<float><<<counted((used + 7) / 8), 256, 0, s>>>(t, lg, amap, used, ax, ay, (const float*)interior,
                                                                (float*)apron, b, fill_only_bad);
         else
-            k_apron<float><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const float*)interior, (float*)apron, b);
+            k_apron<float><<<counted(used), 256, 0, s>>>(t, lg, amap, ax, ay, (const float*)interior, (float*)apron, b);
     } else {
         uint16_t b16 = (uint16_t)boundbits;
         __half_raw hr;
         hr.x = b16;
         if (fill_only && lg.cells)
-            k_apron_fill<__half><<<(used + 7) / 8, 256, 0, s>>>(t, lg, amap, used, ax, ay, (const __half*)interior,
+            k_apron_fill<__half><<<counted((used + 7) / 8), 256, 0, s>>>(t, lg, amap, used, ax, ay, (const __half*)interior,
                                                                 (__half*)apron, __half(hr), fill_only_bad);
         else
-            k_apron<__half><<<used, 256, 0, s>>>(t, lg, amap, ax, ay, (const __half*)interior, (__half*)apron,
+            k_apron<__half><<<counted(used), 256, 0, s>>>(t, lg, amap, ax, ay, (const __half*)interior, (__half*)apron,
                                                  __half(hr));
     }
 }
@@ -508,10 +508,10 @@ void launch_export_bricks(const void* interior, const void* apron, int used, int
     if (used <= 0) return;
     long long total = (long long)used * 5832;
     if (esize == 4)
-        k_export_bricks<float><<<gs_blocks(total, 256), 256, 0, s>>>((const float*)interior, (const float*)apron, used,
+        k_export_bricks<float><<<counted(gs_blocks(total, 256)), 256, 0, s>>>((const float*)interior, (const float*)apron, used,
                                                                      (float*)out);
     else
-        k_export_bricks<__half><<<gs_blocks(total, 256), 256, 0, s>>>((const __half*)interior, (const __half*)apron,
+        k_export_bricks<__half><<<counted(gs_blocks(total, 256)), 256, 0, s>>>((const __half*)interior, (const __half*)apron,
                                                                        used, (__half*)out);
 }
 void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const void* interior, double* partials,
@@ -519,61 +519,61 @@ void launch_checksum_slots(const AtlasNode* amap, int used, int dtype, const voi
     if (used > 0) {
         unsigned blocks = (unsigned)std::min(used, 152 * std::max(blocks_per_sm, 1));
         if (dtype == 3)
-            k_slot_sums<float><<<blocks, 256, 0, s>>>(amap, used, (const float*)interior, partials);
+            k_slot_sums<float><<<counted(blocks), 256, 0, s>>>(amap, used, (const float*)interior, partials);
         else if (dtype == 100)
-            k_slot_sums<__half><<<blocks, 256, 0, s>>>(amap, used, (const __half*)interior, partials);
+            k_slot_sums<__half><<<counted(blocks), 256, 0, s>>>(amap, used, (const __half*)interior, partials);
         else
-            k_slot_sums<__nv_bfloat16><<<blocks, 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
+            k_slot_sums<__nv_bfloat16><<<counted(blocks), 256, 0, s>>>(amap, used, (const __nv_bfloat16*)interior, partials);
     }
-    k_sum_partials<<<1, 1024, 0, s>>>(partials, used, out);
+    k_sum_partials<<<counted(1), 1024, 0, s>>>(partials, used, out);
 }
 void launch_slab_pack(const void* interior, const void* apron, int esize, int ax, int ay, int bz, long long valid,
                       void* slab, cudaStream_t s) {
     long long n = (long long)ax * 18 * ay * 18 * 18;
     if (esize == 4)
-        k_slab_pack<float><<<gs_blocks(n, 256), 256, 0, s>>>((const float*)interior, (const float*)apron, ax, ay, bz,
+        k_slab_pack<float><<<counted(gs_blocks(n, 256)), 256, 0, s>>>((const float*)interior, (const float*)apron, ax, ay, bz,
                                                              valid, (float*)slab);
     else
-        k_slab_pack<__half><<<gs_blocks(n, 256), 256, 0, s>>>((const __half*)interior, (const __half*)apron, ax, ay,
+        k_slab_pack<__half><<<counted(gs_blocks(n, 256)), 256, 0, s>>>((const __half*)interior, (const __half*)apron, ax, ay,
                                                               bz, valid, (__half*)slab);
 }
 void launch_slab_unpack(const void* slab, int esize, int ax, int ay, int bz, void* interior, void* apron,
                         cudaStream_t s) {
     long long n = (long long)ax * 18 * ay * 18 * 18;
     if (esize == 4)
-        k_slab_unpack<float><<<gs_blocks(n, 256), 256, 0, s>>>((const float*)slab, ax, ay, bz, (float*)interior,
+        k_slab_unpack<float><<<counted(gs_blocks(n, 256)), 256, 0, s>>>((const float*)slab, ax, ay, bz, (float*)interior,
                                                                (float*)apron);
     else
-        k_slab_unpack<__half><<<gs_blocks(n, 256), 256, 0, s>>>((const __half*)slab, ax, ay, bz, (__half*)interior,
+        k_slab_unpack<__half><<<counted(gs_blocks(n, 256)), 256, 0, s>>>((const __half*)slab, ax, ay, bz, (__half*)interior,
                                                                 (__half*)apron);
 }
 void launch_neighbors(const TreeView& t, const LeafGrid& lg, long long n, int d, int* table, cudaStream_t s) {
     if (n <= 0) return;
-    k_neighbors<<<blocks_for(n, 128), 128, 0, s>>>(t, lg, n, d, table);
+    k_neighbors<<<counted(blocks_for(n, 128)), 128, 0, s>>>(t, lg, n, d, table);
 }
 void launch_apron_faces(const Node* leaves, const AtlasNode* amap, int used, int ax, int ay, const int* table,
                         int esize, void* interior, void* apron, cudaStream_t s) {
     if (used <= 0) return;
     if (esize == 4)
-        k_apron_faces<float><<<used, 128, 0, s>>>(leaves, amap, used, ax, ay, table, (float*)interior, (float*)apron);
+        k_apron_faces<float><<<counted(used), 128, 0, s>>>(leaves, amap, used, ax, ay, table, (float*)interior, (float*)apron);
     else
-        k_apron_faces<__half><<<used, 128, 0, s>>>(leaves, amap, used, ax, ay, table, (__half*)interior,
+        k_apron_faces<__half><<<counted(used), 128, 0, s>>>(leaves, amap, used, ax, ay, table, (__half*)interior,
                                                    (__half*)apron);
 }
 void launch_smooth(const AtlasNode* amap, int used, float* interior, const float* apron, float p1, float p2,
                    cudaStream_t s) {
     if (used <= 0) return;
-    k_smooth<<<used, 256, 0, s>>>(amap, interior, apron, p1, p2);
+    k_smooth<<<counted(used), 256, 0, s>>>(amap, interior, apron, p1, p2);
 }
 void launch_fill_interior(const AtlasNode* amap, int used, int dtype, void* interior, float value, cudaStream_t s) {
     if (used <= 0) return;
     long long total = (long long)used * 4096;
     if (dtype == 3)
-        k_fill_interior<float><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (float*)interior, value);
+        k_fill_interior<float><<<counted(gs_blocks(total, 256)), 256, 0, s>>>(amap, used, (float*)interior, value);
     else if (dtype == 100)
-        k_fill_interior<__half><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (__half*)interior, value);
+        k_fill_interior<__half><<<counted(gs_blocks(total, 256)), 256, 0, s>>>(amap, used, (__half*)interior, value);
     else
-        k_fill_interior<__nv_bfloat16><<<gs_blocks(total, 256), 256, 0, s>>>(amap, used, (__nv_bfloat16*)interior,
+        k_fill_interior<__nv_bfloat16><<<counted(gs_blocks(total, 256)), 256, 0, s>>>(amap, used, (__nv_bfloat16*)interior,
                                                                             value);
 }
 

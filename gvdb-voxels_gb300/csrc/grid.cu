@@ -379,11 +379,8 @@ struct gbvdb_grid_s {
     void check(cudaError_t e, const char* what) {
         if (e != cudaSuccess) throw StatusError{GBVDB_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e)};
     }
-    long long n_launch = 0, n_readback = 0;
-    void check_launch(const char* what) {
-        n_launch++;
-        check(cudaGetLastError(), what);
-    }
+    long long n_launch = 0, n_readback = 0;  // n_launch: kernels (tl_kernels, per entry point)
+    void check_launch(const char* what) { check(cudaGetLastError(), what); }
     void sync() { check(cudaStreamSynchronize(stream), "cudaStreamSynchronize"); }
 
     void grow(DevBuf& b, size_t bytes, size_t preserve = 0) {
@@ -1873,9 +1870,17 @@ struct gbvdb_grid_s {
 
 // ------------------------------------------------------------------ C ABI
 
+// the kernels an entry point launches, added to the grid's count when it returns
+struct LaunchTally {
+    long long& total;
+    long long t0;
+    explicit LaunchTally(long long& t) : total(t), t0(tl_kernels) {}
+    ~LaunchTally() { total += tl_kernels - t0; }
+};
 #define GBVDB_GUARD_NOCOMMIT(g)                           \
     if (!(g)) return GBVDB_INVALID_ARG;                   \
     std::lock_guard<std::mutex> _lk((g)->mu);             \
+    LaunchTally _tally((g)->n_launch);                    \
     try {                                                 \
         cudaSetDevice((g)->device);
 // topology, binning and accessor entry points commit pending host activations

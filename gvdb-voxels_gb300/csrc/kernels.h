@@ -8,6 +8,16 @@
 
 namespace gbvdb {
 
+// Kernels this library launched on the calling thread: every launch site passes its
+// grid size through counted(), which the launch evaluates once; the C entry points add
+// the change over the call to the grid's launch count (gbvdb_get_stats).
+extern thread_local long long tl_kernels;
+template <class T>
+inline T counted(T blocks) {
+    ++tl_kernels;
+    return blocks;
+}
+
 // Key-domain of one level: node coordinates [lo, lo+dim) per axis, bit offset into
 // the level bitmaps (x-major linear index so that bit order == key sort order).
 struct KeyDomain {

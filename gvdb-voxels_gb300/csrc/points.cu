@@ -1427,26 +1427,26 @@ inline unsigned gs_blocks(long long n, int t) {
 void launch_insert_points(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, int* pnode, uint32_t* pndx,
                           uint32_t* gcnt, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_insert_points<<<gs_blocks(p.n, 256), 256, 0, s>>>(t, lg, p, trans, pnode, pndx, gcnt);
+    k_insert_points<<<counted(gs_blocks(p.n, 256)), 256, 0, s>>>(t, lg, p, trans, pnode, pndx, gcnt);
 }
 void launch_sort_points(PointSrc p, float3 trans, const int* pnode, const uint32_t* pndx, const uint32_t* goff,
                         float* out3, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_sort_points<<<gs_blocks(p.n, 256), 256, 0, s>>>(p, trans, pnode, pndx, goff, out3);
+    k_sort_points<<<counted(gs_blocks(p.n, 256)), 256, 0, s>>>(p, trans, pnode, pndx, goff, out3);
 }
 void launch_scatter_density(const Node* leaves, long long nleaf, const uint32_t* goff, const float* pts3, float radius,
                             int expand, int res0, int ax, int ay, float* interior, float* apron, cudaStream_t s) {
     if (nleaf <= 0) return;
-    k_scatter_density<<<(unsigned)nleaf, 256, 0, s>>>(leaves, nleaf, goff, pts3, radius, expand, res0, ax, ay,
+    k_scatter_density<<<counted((unsigned)nleaf), 256, 0, s>>>(leaves, nleaf, goff, pts3, radius, expand, res0, ax, ay,
                                                       interior, apron);
 }
 void launch_linked_list(const Node* leaves, long long n, const uint32_t* scmap, int* linked, cudaStream_t s) {
     if (n <= 0) return;
-    k_linked_list<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, scmap, linked);
+    k_linked_list<<<counted(blocks_for(n, 256)), 256, 0, s>>>(leaves, n, scmap, linked);
 }
 void launch_nb_mask(const TreeView& t, const LeafGrid& lg, long long n, uint32_t* nbmask, uint32_t* bin_cnt,
                     unsigned long long* totals, cudaStream_t s) {
-    k_nb_mask<<<blocks_for(std::max(n, 1ll) * 32, 256), 256, 0, s>>>(t, lg, n, nbmask, bin_cnt, totals);
+    k_nb_mask<<<counted(blocks_for(std::max(n, 1ll) * 32, 256)), 256, 0, s>>>(t, lg, n, nbmask, bin_cnt, totals);
 }
 void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, const uint32_t* nbmask, uint32_t* bin_cnt, int* bin_of, uint32_t* rank_of,
@@ -1454,11 +1454,11 @@ void launch_bin_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 
     if (p.n <= 0) return;
     const unsigned b = unroll == 4 ? gs_blocks((p.n + 3) / 4, 256) : gs_blocks(p.n, 256);
     if (unroll == 1)
-        k_bin_count<1><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
+        k_bin_count<1><<<counted(b), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
     else if (unroll == 4)
-        k_bin_count<4><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
+        k_bin_count<4><<<counted(b), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
     else
-        k_bin_count<2><<<b, 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
+        k_bin_count<2><<<counted(b), 256, 0, s>>>(t, lg, p, trans, R, q, scmap, nbmask, bin_cnt, bin_of, rank_of, totals);
 }
 void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* bin_of, const uint32_t* rank_of,
                         const uint32_t* bin_off, float4* sorted, ClrSrc clr, uint32_t* sorted_clr, int unroll,
@@ -1467,72 +1467,72 @@ void launch_bin_scatter(PointSrc p, float3 trans, float R, Quant q, const int* b
     const unsigned b = unroll == 4 ? gs_blocks((p.n + 3) / 4, 256) : gs_blocks(p.n, 256);
     uint32_t* sc = clr.base ? sorted_clr : nullptr;
     if (unroll == 2)
-        k_bin_scatter<2><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
+        k_bin_scatter<2><<<counted(b), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
     else if (unroll == 8)
-        k_bin_scatter<8><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
+        k_bin_scatter<8><<<counted(b), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
     else
-        k_bin_scatter<4><<<b, 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
+        k_bin_scatter<4><<<counted(b), 256, 0, s>>>(p, trans, R, q, bin_of, rank_of, bin_off, sorted, clr, sc);
 }
 void launch_gather_colour(const int4* gtab, long long nbricks, const uint32_t* bin_off, const float4* pts,
                           const uint32_t* pclr, int olo, int ohi, int accum, uint32_t* out, cudaStream_t s) {
     if (nbricks <= 0) return;
-    k_gather_colour<<<(unsigned)nbricks, 128, 0, s>>>(gtab, bin_off, pts, pclr, olo, ohi, accum, out);
+    k_gather_colour<<<counted((unsigned)nbricks), 128, 0, s>>>(gtab, bin_off, pts, pclr, olo, ohi, accum, out);
 }
 void launch_gather_colour_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                                 const uint32_t* clr, int ax, int ay, int accum, uint32_t* out, cudaStream_t s) {
     if (nbricks <= 0) return;
-    k_gather_colour_lists<<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, clr, ax, ay, accum, out);
+    k_gather_colour_lists<<<counted((unsigned)nbricks), 256, 0, s>>>(t, linked, off, clr, ax, ay, accum, out);
 }
 void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* scmap, const AtlasNode* amap, int used,
                        int ax, int ay, long long n, int* bad, cudaStream_t s) {
-    k_push_check<<<blocks_for(std::max(n, 1ll), 256), 256, 0, s>>>(t, lg, scmap, amap, used, ax, ay, n, bad);
+    k_push_check<<<counted(blocks_for(std::max(n, 1ll), 256)), 256, 0, s>>>(t, lg, scmap, amap, used, ax, ay, n, bad);
 }
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    int4* gtab, void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
-    k_gather_prep<<<blocks_for(nbricks * 32, kPrepThreads), kPrepThreads, 0, s>>>(
+    k_gather_prep<<<counted(blocks_for(nbricks * 32, kPrepThreads)), kPrepThreads, 0, s>>>(
         t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay, gp.long_min, gp.order, gtab);
     const unsigned nb = (unsigned)nbricks;
     if (gp.min_blocks == 8) {
         if (gp.dtype == 3)
-            k_gather<float, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
+            k_gather<float, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
         else if (gp.dtype == 100)
-            k_gather<__half, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
+            k_gather<__half, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
         else
-            k_gather<__nv_bfloat16, 8><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
+            k_gather<__nv_bfloat16, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
                                                                     (__nv_bfloat16*)interior);
     } else {
         if (gp.dtype == 3)
-            k_gather<float, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
+            k_gather<float, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
         else if (gp.dtype == 100)
-            k_gather<__half, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
+            k_gather<__half, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
         else
-            k_gather<__nv_bfloat16, 10><<<nb, kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
+            k_gather<__nv_bfloat16, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
                                                                      (__nv_bfloat16*)interior);
     }
 }
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                        const uint32_t* scmap, uint32_t* cnt, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_count<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, cnt);
+    k_list_count<<<counted(gs_blocks(p.n, 128)), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, cnt);
 }
 void launch_list_fill(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
                       const uint32_t* scmap, const uint32_t* off, uint32_t* cursor, float* out3, ClrSrc clr,
                       uint32_t* out_clr, cudaStream_t s) {
     if (p.n <= 0) return;
-    k_list_fill<<<gs_blocks(p.n, 128), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, off, cursor, out3, clr,
+    k_list_fill<<<counted(gs_blocks(p.n, 128)), 128, 0, s>>>(t, lg, p, trans, R, q, scmap, off, cursor, out3, clr,
                                                    clr.base ? out_clr : nullptr);
 }
 void launch_gather_lists(const TreeView& t, const int* linked, long long nbricks, const uint32_t* off,
                          const float* pts3, const GatherParams& gp, void* interior, cudaStream_t s) {
     if (nbricks <= 0) return;
     if (gp.dtype == 3)
-        k_gather_lists<float><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp, (float*)interior);
+        k_gather_lists<float><<<counted((unsigned)nbricks), 256, 0, s>>>(t, linked, off, pts3, gp, (float*)interior);
     else if (gp.dtype == 100)
-        k_gather_lists<__half><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp, (__half*)interior);
+        k_gather_lists<__half><<<counted((unsigned)nbricks), 256, 0, s>>>(t, linked, off, pts3, gp, (__half*)interior);
     else
-        k_gather_lists<__nv_bfloat16><<<(unsigned)nbricks, 256, 0, s>>>(t, linked, off, pts3, gp,
+        k_gather_lists<__nv_bfloat16><<<counted((unsigned)nbricks), 256, 0, s>>>(t, linked, off, pts3, gp,
                                                                        (__nv_bfloat16*)interior);
 }
 

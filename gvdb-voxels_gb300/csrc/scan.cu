@@ -12,6 +12,8 @@
 
 namespace gbvdb {
 
+thread_local long long tl_kernels = 0;
+
 namespace {
 constexpr int kThreads = 1024;
 constexpr int kItems = 4;
@@ -204,16 +206,16 @@ static void scan_exclusive(ScanIn in, uint32_t* out, long long n, void* tmp, cud
     }
     long long t = ntiles(n);
     if (t == 1) {
-        k_tile_scan<kKind><<<1, kThreads, 0, s>>>(in, n, nullptr, out);
+        k_tile_scan<kKind><<<counted(1), kThreads, 0, s>>>(in, n, nullptr, out);
         return;
     }
     uint32_t* sums = reinterpret_cast<uint32_t*>(tmp);
     uint32_t* offs = sums + t;
     char* rest = reinterpret_cast<char*>(offs + t + 1);
     rest = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(rest) + 255) & ~uintptr_t(255));
-    k_tile_sums<kKind><<<(unsigned)t, kThreads, 0, s>>>(in, n, sums);
+    k_tile_sums<kKind><<<counted((unsigned)t), kThreads, 0, s>>>(in, n, sums);
     scan_exclusive<0>(ScanIn{sums, nullptr}, offs, t, rest, s);
-    k_tile_scan<kKind><<<(unsigned)t, kThreads, 0, s>>>(in, n, offs, out);
+    k_tile_scan<kKind><<<counted((unsigned)t), kThreads, 0, s>>>(in, n, offs, out);
 }
 
 void scan_exclusive_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
@@ -241,7 +243,7 @@ unsigned long long* sort_keys_u64(unsigned long long* keys, unsigned long long* 
                                   cudaStream_t s) {
     if (n <= 1) return keys;
     if (n <= kSortSmall) {
-        k_sort_small<<<1, 1024, 0, s>>>(keys, (int)n);
+        k_sort_small<<<counted(1), 1024, 0, s>>>(keys, (int)n);
         return keys;
     }
     const long long t = sort_tiles(n), h = 256 * t;
@@ -251,9 +253,9 @@ unsigned long long* sort_keys_u64(unsigned long long* keys, unsigned long long* 
     rest = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(rest) + 255) & ~uintptr_t(255));
     unsigned long long *src = keys, *dst = alt;
     for (int shift = 0; shift < bits; shift += 8) {
-        k_digit_hist<<<(unsigned)t, kSortThreads, 0, s>>>(src, n, shift, hist);
+        k_digit_hist<<<counted((unsigned)t), kSortThreads, 0, s>>>(src, n, shift, hist);
         scan_exclusive_u32(hist, offs, h, rest, s);
-        k_digit_scatter<<<(unsigned)t, kSortThreads, 0, s>>>(src, dst, n, shift, offs);
+        k_digit_scatter<<<counted((unsigned)t), kSortThreads, 0, s>>>(src, dst, n, shift, offs);
         unsigned long long* x = src;
         src = dst;
         dst = x;

@@ -844,7 +844,7 @@ inline unsigned grid_stride_blocks(long long n, int t) {
 void launch_bbox(PointSrc p, float3 orig, int* out6, cudaStream_t s) {
     // at most 4 blocks per SM: each block ends with six same-address atomics
     const unsigned b = std::min<unsigned>(grid_stride_blocks(p.n, 512), 152u * 4u);
-    k_bbox<<<b, 512, 0, s>>>(p, orig, out6);
+    k_bbox<<<counted(b), 512, 0, s>>>(p, orig, out6);
 }
 void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, const KeyDomains& dom,
                        uint32_t* bitmap, const KeySets& ks, int* err, cudaStream_t s) {
@@ -852,7 +852,7 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
     for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
     size_t smem = !ks.keys.tab && nwords <= 8192 ? (size_t)nwords * 4 : 0;
     unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-    k_keys_pass1<<<blocks, 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, ks.keys, err);
+    k_keys_pass1<<<counted(blocks), 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, ks.keys, err);
 }
 long long touch_dirs_words(const KeyDomains& dom) {
     return (long long)(dom.d[0].dim[0] + 2) * (dom.d[0].dim[1] + 2) * (dom.d[0].dim[2] + 2);
@@ -869,13 +869,13 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
     if (ks.touched.tab) {
         // sparse form: the per-point walk into the touched table, parents level by level,
         // then every touched position resolved in one pass
-        k_touch_box<<<grid_stride_blocks(p.n, 256), 256, 0, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
+        k_touch_box<<<counted(grid_stride_blocks(p.n, 256)), 256, 0, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom,
                                                                  nullptr, 0, ks.touched, err);
         const unsigned long long cap = ks.touched.mask + 1;
         for (int lev = 1; lev < depth; lev++)
-            k_touch_up_hashed<<<grid_stride_blocks((long long)cap, 256), 256, 0, s>>>(ks.touched, dom.d[lev - 1],
+            k_touch_up_hashed<<<counted(grid_stride_blocks((long long)cap, 256)), 256, 0, s>>>(ks.touched, dom.d[lev - 1],
                                                                                       dom.d[lev], t.lgres[lev], err);
-        k_resolve_hashed<<<grid_stride_blocks((long long)cap, 256), 256, 0, s>>>(t, lg, depth, dom, ks.touched, ks.keys,
+        k_resolve_hashed<<<counted(grid_stride_blocks((long long)cap, 256)), 256, 0, s>>>(t, lg, depth, dom, ks.touched, ks.keys,
                                                                                  markers, err);
         return;
     }
@@ -900,21 +900,21 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
                 PointSrc q = p;
                 q.stride = p.stride * 64;
                 q.n = (p.n + 63) / 64;
-                touch<<<grid_stride_blocks((q.n + 3) / 4, 64), 64, 0, s>>>(q, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
+                touch<<<counted(grid_stride_blocks((q.n + 3) / 4, 64)), 64, 0, s>>>(q, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
                                                                             dirs, err);
             }
-            touch<<<grid_stride_blocks((p.n + 3) / 4, 256), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
+            touch<<<counted(grid_stride_blocks((p.n + 3) / 4, 256)), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
                                                                           dirs, err);
         }
         const long long nw = (dom.d[0].nbits + 31) >> 5;
-        k_touch_from_dirs<<<blocks_for(nw * 32, 128), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
+        k_touch_from_dirs<<<counted(blocks_for(nw * 32, 128)), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
     } else {
         // the points touch level 0 (its bits start at bit 0); the upper levels follow from it
         long long nwords = (dom.d[0].bitbase + dom.d[0].nbits + 31) >> 5;
         size_t smem = nwords <= kTouchSmemWords ? (size_t)nwords * 4 : 0;
         // fewer, fuller blocks when each one flushes a shared bitmap
         unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-        k_touch_box<<<blocks, 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords,
+        k_touch_box<<<counted(blocks), 256, smem, s>>>(t, p, orig, radius, hi_mul, depth, rlo, rhi, dom, touched, nwords,
                                               KeyHash{nullptr, 0}, err);
     }
     for (int lev = 1; lev < depth; lev++) {
@@ -922,72 +922,72 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
         const long long pnw = (dom.d[lev].nbits + 31) >> 5;
         const size_t smem = pnw <= kTouchSmemWords ? (size_t)pnw * 4 : 0;
         // 1024 threads per block: fewer blocks flushing the parent words
-        k_touch_up<<<blocks_for(nw * 32, 1024), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
+        k_touch_up<<<counted(blocks_for(nw * 32, 1024)), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
     }
     const long long nw_all = (dom.d[depth - 1].bitbase + dom.d[depth - 1].nbits + 31) >> 5;
-    k_resolve_touched<<<blocks_for(nw_all * 32, 128), 128, 0, s>>>(t, lg, depth, dom, touched, bitmap, markers);
+    k_resolve_touched<<<counted(blocks_for(nw_all * 32, 128)), 128, 0, s>>>(t, lg, depth, dom, touched, bitmap, markers);
 }
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s) {
     if (n <= 0) return;
-    k_build_leaf_grid<<<blocks_for(n, 256), 256, 0, s>>>(t, n, cells, make_int3(lo[0], lo[1], lo[2]),
+    k_build_leaf_grid<<<counted(blocks_for(n, 256)), 256, 0, s>>>(t, n, cells, make_int3(lo[0], lo[1], lo[2]),
                                                          make_int3(dim[0], dim[1], dim[2]), lgrange0);
 }
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
     if (nwords <= 0) return;
-    k_alloc_nodes<<<blocks_for(nwords * 32, 256), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
+    k_alloc_nodes<<<counted(blocks_for(nwords * 32, 256)), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
 }
 void launch_hash_compact(const KeyHash& h, unsigned long long* out, unsigned int* count, cudaStream_t s) {
-    k_hash_compact<<<grid_stride_blocks((long long)(h.mask + 1), 256), 256, 0, s>>>(h, out, count);
+    k_hash_compact<<<counted(grid_stride_blocks((long long)(h.mask + 1), 256)), 256, 0, s>>>(h, out, count);
 }
 void launch_key_bounds(const unsigned long long* sorted, const unsigned int* n, const KeyDomains& dom, int depth,
                        unsigned int* at, cudaStream_t s) {
-    k_key_bounds<<<1, 32, 0, s>>>(sorted, n, dom, depth, at);
+    k_key_bounds<<<counted(1), 32, 0, s>>>(sorted, n, dom, depth, at);
 }
 void launch_alloc_nodes_sorted(const unsigned long long* sorted, long long first, long long count, int lev,
                                int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
     if (count <= 0) return;
-    k_alloc_nodes_sorted<<<blocks_for(count, 256), 256, 0, s>>>(sorted, first, count, lev, lgrange, d, base, nodes);
+    k_alloc_nodes_sorted<<<counted(blocks_for(count, 256)), 256, 0, s>>>(sorted, first, count, lev, lgrange, d, base, nodes);
 }
-void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<1, 1, 0, s>>>(dst, v); }
+void launch_write_node(Node* dst, const Node& v, cudaStream_t s) { k_write_node<<<counted(1), 1, 0, s>>>(dst, v); }
 void launch_link(const TreeView& t, int lev, long long count, int* tag, long long* slot_of, cudaStream_t s) {
     if (count <= 0) return;
     long long nslots = t.ncnt[lev + 1] << (3 * t.lgres[lev + 1]);
     cudaMemsetAsync(tag, 0xFF, (size_t)nslots * sizeof(int), s);
-    k_link_claim<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
-    k_link_write<<<blocks_for(count, 256), 256, 0, s>>>(t, lev, count, tag, slot_of);
+    k_link_claim<<<counted(blocks_for(count, 256)), 256, 0, s>>>(t, lev, count, tag, slot_of);
+    k_link_write<<<counted(blocks_for(count, 256)), 256, 0, s>>>(t, lev, count, tag, slot_of);
 }
 void launch_apply_markers(Node* leaves, long long n, const int* markers, cudaStream_t s) {
     if (n <= 0) return;
-    k_apply_markers<<<blocks_for(n, 256), 256, 0, s>>>(leaves, n, markers);
+    k_apply_markers<<<counted(blocks_for(n, 256)), 256, 0, s>>>(leaves, n, markers);
 }
 void launch_delink_leaf(const TreeView& t, long long n, cudaStream_t s) {
     if (n <= 0) return;
-    k_delink_leaf<<<blocks_for(n, 256), 256, 0, s>>>(t, n);
+    k_delink_leaf<<<counted(blocks_for(n, 256)), 256, 0, s>>>(t, n);
 }
 void launch_delink_upper(const TreeView& t, int lev, long long n, cudaStream_t s) {
     if (n <= 0) return;
-    k_delink_upper<<<blocks_for(n, 128), 128, 0, s>>>(t, lev, n);
+    k_delink_upper<<<counted(blocks_for(n, 128)), 128, 0, s>>>(t, lev, n);
 }
 void launch_stage_counts(const uint32_t* pscan, const CountStage& st, uint32_t* out, cudaStream_t s) {
-    k_stage_counts<<<1, 32, 0, s>>>(pscan, st, out);
+    k_stage_counts<<<counted(1), 32, 0, s>>>(pscan, st, out);
 }
 void launch_incr_setup(const Node* leaves, long long n, int* markers, int accum, int* err, unsigned long long* kept,
                        int* bbox6, cudaStream_t s) {
-    k_incr_setup<<<blocks_for(std::max(n, 1ll), 256), 256, 0, s>>>(leaves, n, markers, accum, err, kept, bbox6);
+    k_incr_setup<<<counted(blocks_for(std::max(n, 1ll), 256)), 256, 0, s>>>(leaves, n, markers, accum, err, kept, bbox6);
 }
 void launch_count_markers(const int* markers, long long n, unsigned long long* out, cudaStream_t s) {
     if (n <= 0) return;
-    k_count_markers<<<grid_stride_blocks(n, 256), 256, 0, s>>>(markers, n, out);
+    k_count_markers<<<counted(grid_stride_blocks(n, 256)), 256, 0, s>>>(markers, n, out);
 }
 void launch_count_flags(const Node* nodes, long long n, unsigned long long* out, cudaStream_t s) {
     if (n <= 0) return;
-    k_count_flags<<<grid_stride_blocks(n, 256), 256, 0, s>>>(nodes, n, out);
+    k_count_flags<<<counted(grid_stride_blocks(n, 256)), 256, 0, s>>>(nodes, n, out);
 }
 void launch_leaf_bounds(const Node* leaves, long long n, int lgrange0, int* out6, cudaStream_t s) {
     if (n <= 0) return;
-    k_leaf_bounds<<<1, 1024, 0, s>>>(leaves, n, lgrange0, out6);
+    k_leaf_bounds<<<counted(1), 1024, 0, s>>>(leaves, n, lgrange0, out6);
 }
 
 }  // namespace gbvdb
