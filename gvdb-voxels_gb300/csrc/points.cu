@@ -753,6 +753,50 @@ __global__ void __launch_bounds__(kPrepThreads) k_gather_prep(TreeView t, LeafGr
     if (lane < 28) gtab[pos * 32 + lane] = e;
 }
 
+// Runs of home bins that can hold a point near enough to a brick to matter for
+// cutoffs T <= 16 and T <= 25 (scatter form): the brick's own 64 bins, and of each of
+// the 26 neighbours the layers of subcells next to the brick (local coordinate 0
+// toward a neighbour on the + side; 3, or 2 and 3, toward one on the - side; all four
+// along an axis where it is level with the brick), cut into runs of consecutive bin
+// indices (bin = z*16 + y*4 + x).  A point homed farther out is at least 5 voxels from
+// every voxel of the brick on some axis toward the + side (the brick's last voxel is at
+// 15, the second layer starts at 20), and more than 4 (one layer) or 8 (two layers)
+// toward the - side, so its d^2 >= 25 (> 16 with one layer) >= T.  Entry: direction
+// (dx+1) + 3 (dy+1) + 9 (dz+1) | first bin << 8 | bins << 16.  One layer: 87 runs,
+// 216 bins; two: 115 runs, 343 bins (of the neighbourhood's 1,728).
+constexpr int kLayerRunsMax = 115;
+struct LayerRunTable {
+    uint32_t e[kLayerRunsMax];
+    int n;
+};
+constexpr LayerRunTable make_layer_run_table(int minus_layers) {
+    LayerRunTable t{};
+    int n = 0;
+    for (int d = 0; d < 27; d++) {
+        const int dd[3] = {d % 3 - 1, (d / 3) % 3 - 1, d / 9 - 1};
+        int run0 = -1, prev = -2;
+        for (int b = 0; b <= 64; b++) {
+            bool in = b < 64;
+            for (int a = 0; a < 3 && in; a++) {
+                const int c = (b >> (2 * a)) & 3;
+                in = dd[a] == 0 || (dd[a] > 0 ? c == 0 : c >= 4 - minus_layers);
+            }
+            if (in && b == prev + 1) {
+                prev = b;
+                continue;
+            }
+            if (run0 >= 0) t.e[n++] = (uint32_t)d | ((uint32_t)run0 << 8) | ((uint32_t)(prev - run0 + 1) << 16);
+            run0 = in ? b : -1;
+            prev = in ? b : -2;
+        }
+    }
+    t.n = n;
+    return t;
+}
+static __device__ const LayerRunTable kLayerRuns16 = make_layer_run_table(1);
+static __device__ const LayerRunTable kLayerRuns25 = make_layer_run_table(2);
+static_assert(make_layer_run_table(1).n == 87 && make_layer_run_table(2).n == 115, "layer run counts");
+
 // One block per linked leaf.  Setup: the brick's record from k_gather_prep (the
 // ranks of the 3x3x3 neighbour bricks and their point ranges in the home-binned
 // array, a brick's 64 bins being contiguous; the origin and the atlas slot).
@@ -760,7 +804,9 @@ __global__ void __launch_bounds__(kPrepThreads) k_gather_prep(TreeView t, LeafGr
 // neighbourhood (either form is exact; the choice only affects speed):
 //
 // scatter (sparse bricks): every thread loads one neighbourhood point at a time
-//   (all loads in flight together) and derives its reach in this brick (member
+//   (with a cutoff T <= 25 only the points homed in the neighbours' subcell layers
+//   next to the brick, kLayerRuns16/25; all loads in flight together) and derives
+//   its reach in this brick (member
 //   subcells cut to the cutoff box); each warp then walks its live points: the
 //   reach's voxel columns 32 at a time, each lane one column, z two at a time
 //   over the part of the cutoff sphere above the group's nearest column, min d^2
@@ -791,6 +837,9 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
     __shared__ int nlive;
     __shared__ int next_sc;  // gather form: next subcell to search
     __shared__ int pslot[27];  // fused apron: slot of the neighbour at each direction, -1: none / no push
+    // scatter form with T <= 25: the layer runs' first points and exclusive prefix (kLayerRuns16/25)
+    __shared__ uint32_t lr_beg[kLayerRunsMax];
+    __shared__ uint32_t lr_pre[128];
 
     const int4* rec = gtab + (size_t)blockIdx.x * 32;  // this brick's setup (k_gather_prep)
     const int4 head = __ldg(rec + 27);
@@ -838,16 +887,67 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
         // (its columns row-major, 32 per group, a lane per column; z walked two at
         // a time over the group's reach) with shared atomicMin.
         float4* live_pts = reinterpret_cast<float4*>(scratch);
-        for (uint32_t cbase = 0; cbase < ncand; cbase += kLive) {
+        // cutoff T <= 25: the candidates are the points of the layer runs (kLayerRuns16/25)
+        // instead of all 27 neighbours' points
+        const bool layered = gp.tbits <= 0x41C80000u;  // 25.0f
+        const LayerRunTable& runs = gp.tbits <= 0x41800000u ? kLayerRuns16 : kLayerRuns25;  // 16.0f
+        const int nruns = runs.n;
+        uint32_t nsc = ncand;
+        if (layered) {
+            if (threadIdx.x < nruns) {
+                const uint32_t e = runs.e[threadIdx.x];
+                const int r = nrank[e & 0xFF];
+                uint32_t b = 0, c = 0;
+                if (r >= 0) {
+                    const size_t b0 = (size_t)r * 64 + ((e >> 8) & 0xFF);
+                    b = __ldg(bin_off + b0);
+                    c = __ldg(bin_off + b0 + (e >> 16)) - b;
+                }
+                lr_beg[threadIdx.x] = b;
+                lr_pre[threadIdx.x] = c;  // the count, replaced by the prefix below
+            }
+            __syncthreads();
+            if (warp == 0) {  // exclusive prefix of the runs' counts, four per lane
+                uint32_t c[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) c[i] = 4 * lane + i < nruns ? lr_pre[4 * lane + i] : 0u;
+                const uint32_t sum = c[0] + c[1] + c[2] + c[3];
+                uint32_t incl = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                __syncwarp();
+                const uint32_t ex = incl - sum;
+                lr_pre[4 * lane] = ex;
+                lr_pre[4 * lane + 1] = ex + c[0];
+                lr_pre[4 * lane + 2] = ex + c[0] + c[1];
+                lr_pre[4 * lane + 3] = ex + c[0] + c[1] + c[2];
+            }
+            __syncthreads();
+            nsc = lr_pre[nruns];
+        }
+        for (uint32_t cbase = 0; cbase < nsc; cbase += kLive) {
             if (threadIdx.x == 0) nlive = 0;
             __syncthreads();
-            const uint32_t cend = min(ncand, cbase + (uint32_t)kLive);
+            const uint32_t cend = min(nsc, cbase + (uint32_t)kLive);
             for (uint32_t idx = cbase + threadIdx.x; idx < cend; idx += blockDim.x) {
-                int nb = 0;  // neighbour holding point idx: last nb with nb_pre[nb] <= idx
+                uint32_t src;
+                if (layered) {
+                    int k = 0;  // run holding candidate idx: last k with lr_pre[k] <= idx
 #pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (nb + step < 27 && nb_pre[nb + step] <= idx) nb += step;
-                const float4 q = pts[nb_beg[nb] + (idx - nb_pre[nb])];
+                    for (int step = 64; step > 0; step >>= 1)
+                        if (k + step < nruns && lr_pre[k + step] <= idx) k += step;
+                    src = lr_beg[k] + (idx - lr_pre[k]);
+                } else {
+                    int nb = 0;  // neighbour holding point idx: last nb with nb_pre[nb] <= idx
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (nb + step < 27 && nb_pre[nb + step] <= idx) nb += step;
+                    src = nb_beg[nb] + (idx - nb_pre[nb]);
+                }
+                const float4 q = pts[src];
                 const int pk = __float_as_int(q.w);
                 const float pw[3] = {q.x, q.y, q.z};
                 const int org[3] = {ox, oy, oz};
