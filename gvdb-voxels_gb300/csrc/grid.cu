@@ -902,7 +902,7 @@ struct gbvdb_grid_s {
             at = key_pass(D, kd, bits, (long long)at[(size_t)D] + 1024, 4 * n + 1024, [&](const KeySets& ks) {
                 launch_keys_box(t, lgv, p, orig, radius, 2, D, rlo, rhi, kd, touched_bits(),
                                 ptr<uint32_t>(bitmap), nullptr, ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd),
-                                ks, stream);
+                                ks, ncnt[0], stream);
                 check_launch("keys_extra");
             });
             if (allocate_counted(D, kd, at) > 0) {
@@ -1008,7 +1008,7 @@ struct gbvdb_grid_s {
             // (the sparse form may run the pass again: its count starts from zero each time)
             if (hashed) check(cudaMemsetAsync(kept, 0, 8, stream), "kept clear");
             launch_keys_box(t, lgv, p, orig, radius, 1, D, rlo, rhi, kd, touched_bits(), ptr<uint32_t>(bitmap),
-                            ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, stream);
+                            ptr<int>(markers), ptr<int>(misc) + 8, hashed ? nullptr : touch_dirs_buf(kd), ks, nleaf, stream);
             check_launch("keys_incr");
             launch_count_markers(ptr<int>(markers), nleaf, kept, stream);
             check_launch("count_markers");

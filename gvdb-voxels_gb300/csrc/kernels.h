@@ -103,12 +103,13 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
                        uint32_t* bitmap, const KeySets& ks, int* err, cudaStream_t s);
 // touched: scratch bitmap with the layout of `bitmap`, cleared by the caller; dirs (or null):
 // scratch of touch_dirs_words(dom) words for the direction-set form (boxes within one node
-// of the home node), cleared by the launcher
+// of the home node), cleared by the launcher; home_hint: an estimate of the home leaf
+// positions (the leaf count), which picks how the direction sets become touched bits
 long long touch_dirs_words(const KeyDomains& dom);
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
                      uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, const KeySets& ks,
-                     cudaStream_t s);
+                     long long home_hint, cudaStream_t s);
 // the key-count readback staged for one copy (k_stage_counts): prefix words of levels
 // [0, nlev) and the total (words[nlev]), the error flag, the kept-leaf count and the point
 // bounds (both optional)

@@ -450,6 +450,32 @@ __global__ void k_touch_from_dirs(KeyDomain d, DirDomain dd, const uint32_t* __r
     if (b == 0) touched[(d.bitbase >> 5) + w] = mask;
 }
 
+// The same bits from the other side, for key domains much larger than the set of home
+// positions (sparse clouds): a thread per entry of the direction table (a coalesced
+// read); a non-zero entry sets, for each direction in its mask, the bit of the position
+// at that direction (atomicOr into the touched words, cleared before the pass).  The gather
+// form above visits 27 entries for every position of the domain, most of them empty there.
+__global__ void k_touch_dirs_scatter(KeyDomain d, DirDomain dd, const uint32_t* __restrict__ dirs, long long nent,
+                                     uint32_t* touched) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nent; e += stride) {
+        uint32_t m = __ldg(dirs + e);
+        if (!m) continue;
+        const int hz = (int)(e % dd.dim[2]);
+        const long long q = e / dd.dim[2];
+        const int hy = (int)(q % dd.dim[1]), hx = (int)(q / dd.dim[1]);
+        while (m) {  // the entry's home position, domain coordinates h - 1, plus each direction
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const int px = hx - 1 + (k % 3 - 1), py = hy - 1 + ((k / 3) % 3 - 1), pz = hz - 1 + (k / 9 - 1);
+            if ((unsigned)px >= (unsigned)d.dim[0] || (unsigned)py >= (unsigned)d.dim[1] || (unsigned)pz >= (unsigned)d.dim[2])
+                continue;
+            const long long li = ((long long)px * d.dim[1] + py) * d.dim[2] + pz;
+            atomicOr(touched + (d.bitbase >> 5) + (li >> 5), 1u << (li & 31));
+        }
+    }
+}
+
 // Box positions of level lev from those of lev-1: every touched position's parent.  For
 // one box, trunc(b / R_lev) * R_lev .. trunc(e / R_lev) * R_lev is the set of parents
 // of trunc(b / R_lev-1) * R_lev-1 .. trunc(e / R_lev-1) * R_lev-1 once both are clipped
@@ -861,7 +887,7 @@ long long touch_dirs_words(const KeyDomains& dom) {
 void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 orig, float radius, int hi_mul,
                      int depth, int root_lo[3], int root_hi[3], const KeyDomains& dom, uint32_t* touched,
                      uint32_t* bitmap, int* markers, int* err, uint32_t* dirs, const KeySets& ks,
-                     cudaStream_t s) {
+                     long long home_hint, cudaStream_t s) {
     int3 rlo = make_int3(root_lo[0], root_lo[1], root_lo[2]);
     int3 rhi = make_int3(root_hi[0], root_hi[1], root_hi[2]);
     const float hr = hi_mul == 2 ? 2.0f * radius : radius;
@@ -906,8 +932,13 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
             touch<<<counted(grid_stride_blocks((p.n + 3) / 4, 256)), 256, 0, s>>>(p, orig, radius, hr, t.lgrange[0], rlo, rhi, dd,
                                                                           dirs, err);
         }
-        const long long nw = (dom.d[0].nbits + 31) >> 5;
-        k_touch_from_dirs<<<counted(blocks_for(nw * 32, 128)), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
+        if (dom.d[0].nbits > 8 * std::max(home_hint, 1ll)) {  // sparse domain: from the non-zero entries
+            const long long nent = touch_dirs_words(dom);
+            k_touch_dirs_scatter<<<counted(grid_stride_blocks(nent, 256)), 256, 0, s>>>(dom.d[0], dd, dirs, nent, touched);
+        } else {
+            const long long nw = (dom.d[0].nbits + 31) >> 5;
+            k_touch_from_dirs<<<counted(blocks_for(nw * 32, 128)), 128, 0, s>>>(dom.d[0], dd, dirs, touched);
+        }
     } else {
         // the points touch level 0 (its bits start at bit 0); the upper levels follow from it
         long long nwords = (dom.d[0].bitbase + dom.d[0].nbits + 31) >> 5;
