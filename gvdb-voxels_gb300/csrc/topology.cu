@@ -148,14 +148,16 @@ __device__ __forceinline__ void key_coords(const KeyDomain& d, long long li, int
 }
 
 // gvdbCalcBrickId (PT.cuh:352-382): key of every level below the root for every
-// point whose coordinates are all >= 0 (bits collected per block in shared memory
-// when the bitmap fits, as for the box keys below)
+// point whose coordinates are all >= 0.  Bits are collected per block in shared memory
+// for the words [sw0, nwords) of the bitmap when those fit (8,192 words at most): the whole
+// bitmap (sw0 = 0), or, when the leaf level is too large, the levels above it (sw0 = their
+// first word), whose few words every point of the cloud would otherwise test in L2.
 __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom, TreeView tv, uint32_t* bm,
-                             long long nwords, KeyHash kh, int* err) {
+                             long long nwords, long long sw0, KeyHash kh, int* err) {
     extern __shared__ uint32_t sbm[];
-    const bool use_smem = kh.tab == nullptr && nwords <= 8192;
+    const bool use_smem = kh.tab == nullptr && nwords - sw0 <= 8192;
     if (use_smem) {
-        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) sbm[k] = 0;
+        for (long long k = threadIdx.x; k < nwords - sw0; k += blockDim.x) sbm[k] = 0;
         __syncthreads();
     }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n; i += (long long)gridDim.x * blockDim.x) {
@@ -169,9 +171,9 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
             if (b < 0) { atomicOr(err, 1); continue; }
             if (kh.tab) {
                 hash_insert(kh, (unsigned long long)b, err);
-            } else if (use_smem) {
+            } else if (use_smem && (b >> 5) >= sw0) {
                 uint32_t bit = 1u << (b & 31);
-                if (!(sbm[b >> 5] & bit)) atomicOr(&sbm[b >> 5], bit);
+                if (!(sbm[(b >> 5) - sw0] & bit)) atomicOr(&sbm[(b >> 5) - sw0], bit);
             } else {
                 set_bit(bm, b);
             }
@@ -179,9 +181,9 @@ __global__ void k_keys_pass1(PointSrc p, float3 orig, int depth, KeyDomains dom,
     }
     if (use_smem) {
         __syncthreads();
-        for (long long k = threadIdx.x; k < nwords; k += blockDim.x) {
+        for (long long k = threadIdx.x; k < nwords - sw0; k += blockDim.x) {
             uint32_t v = sbm[k];
-            if (v && (__ldcg(bm + k) & v) != v) atomicOr(bm + k, v);
+            if (v && (__ldcg(bm + sw0 + k) & v) != v) atomicOr(bm + sw0 + k, v);
         }
     }
 }
@@ -876,9 +878,13 @@ void launch_keys_pass1(const TreeView& t, PointSrc p, float3 orig, int depth, co
                        uint32_t* bitmap, const KeySets& ks, int* err, cudaStream_t s) {
     long long nwords = 0;
     for (int lev = 0; lev < depth; lev++) nwords = std::max(nwords, (dom.d[lev].bitbase + dom.d[lev].nbits + 31) >> 5);
-    size_t smem = !ks.keys.tab && nwords <= 8192 ? (size_t)nwords * 4 : 0;
+    // the words staged in shared memory: all, else those of the levels above the leaves
+    // (level bit bases are multiples of 32)
+    long long w0 = 0;
+    if (nwords > 8192 && depth > 1) w0 = dom.d[1].bitbase >> 5;
+    size_t smem = !ks.keys.tab && nwords - w0 <= 8192 ? (size_t)(nwords - w0) * 4 : 0;
     unsigned blocks = smem ? std::min<unsigned>(grid_stride_blocks(p.n, 256), 152u * 4u) : grid_stride_blocks(p.n, 256);
-    k_keys_pass1<<<counted(blocks), 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, ks.keys, err);
+    k_keys_pass1<<<counted(blocks), 256, smem, s>>>(p, orig, depth, dom, t, bitmap, nwords, w0, ks.keys, err);
 }
 long long touch_dirs_words(const KeyDomains& dom) {
     return (long long)(dom.d[0].dim[0] + 2) * (dom.d[0].dim[1] + 2) * (dom.d[0].dim[2] + 2);
