@@ -494,11 +494,13 @@ __global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_
         for (long long k = threadIdx.x; k < pnw; k += blockDim.x) sbm[k] = 0;
         __syncthreads();
     }
-    // one thread per bit of the child level (a warp per bitmap word)
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = g >> 5, w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
-    const int b = (int)(g & 31);
-    if (w < nw && ((touched[w0 + w] >> b) & 1u)) {
+    // a lane per bit of the child level, warps striding over its bitmap words (the grid
+    // is capped, so that few blocks clear and flush the parent copy in shared memory)
+    const long long w0 = child.bitbase >> 5, nw = (child.nbits + 31) >> 5;
+    const int b = (int)(threadIdx.x & 31);
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
+        if (!((touched[w0 + w] >> b) & 1u)) continue;
         const long long li = w * 32 + b;
         const int rz = (int)(li % child.dim[2]);
         const long long q = li / child.dim[2];
@@ -525,35 +527,39 @@ __global__ void k_touch_up(KeyDomain child, KeyDomain parent, int lgres, uint32_
 }
 
 // a warp per touched-bitmap word of levels [0, depth) (their words follow each other:
-// each level's bitbase is word aligned), a lane per bit: getPosParent(pos, lev) for every
-// touched position; missing -> key bit, reachable leaf -> marker
-__global__ void k_resolve_touched(TreeView t, LeafGrid lg, int depth, KeyDomains dom,
+// each level's bitbase is word aligned; warps stride over the nw_all words, the grid
+// capped, so that the empty words of a sparse domain cost a load each), a lane per bit:
+// getPosParent(pos, lev) for every touched position; missing -> key bit, reachable
+// leaf -> marker
+__global__ void k_resolve_touched(TreeView t, LeafGrid lg, int depth, KeyDomains dom, long long nw_all,
                                   const uint32_t* __restrict__ touched, uint32_t* keys, int* markers) {
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long wg = g >> 5;  // global word
-    int lev = -1;
-    for (int l = 0; l < depth; l++)
-        if (wg >= (dom.d[l].bitbase >> 5) && wg < (dom.d[l].bitbase >> 5) + ((dom.d[l].nbits + 31) >> 5)) lev = l;
-    if (lev < 0) return;  // whole warps leave together (blockDim is a multiple of 32)
-    const KeyDomain& d = dom.d[lev];
-    const long long w0 = d.bitbase >> 5, w = wg - w0;
-    const int b = (int)(g & 31);
-    const uint32_t bits = touched[w0 + w];
-    bool miss = false;
-    if ((bits >> b) & 1u) {
-        const int lgr = t.lgrange[lev];
-        const long long li = w * 32 + b;
-        const int rz = (int)(li % d.dim[2]);
-        const long long q = li / d.dim[2];
-        const int ry = (int)(q % d.dim[1]);
-        const int rx = (int)(q / d.dim[1]);
-        const int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
-        const long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
-        if (pid < 0) miss = true;
-        else if (lev == 0 && markers) markers[pid] = 1;
+    const int b = (int)(threadIdx.x & 31);
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long wg = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wg < nw_all; wg += wstride) {
+        const uint32_t bits = touched[wg];
+        if (!bits) continue;  // (the whole warp: one word per warp)
+        int lev = -1;
+        for (int l = 0; l < depth; l++)
+            if (wg >= (dom.d[l].bitbase >> 5) && wg < (dom.d[l].bitbase >> 5) + ((dom.d[l].nbits + 31) >> 5)) lev = l;
+        if (lev < 0) continue;
+        const KeyDomain& d = dom.d[lev];
+        const long long w0 = d.bitbase >> 5, w = wg - w0;
+        bool miss = false;
+        if ((bits >> b) & 1u) {
+            const int lgr = t.lgrange[lev];
+            const long long li = w * 32 + b;
+            const int rz = (int)(li % d.dim[2]);
+            const long long q = li / d.dim[2];
+            const int ry = (int)(q % d.dim[1]);
+            const int rx = (int)(q / d.dim[1]);
+            const int px = (d.lo[0] + rx) << lgr, py = (d.lo[1] + ry) << lgr, pz = (d.lo[2] + rz) << lgr;
+            const long long pid = (lev == 0) ? lookup_leaf(lg, t, px, py, pz) : get_pos_parent(t, px, py, pz, lev);
+            if (pid < 0) miss = true;
+            else if (lev == 0 && markers) markers[pid] = 1;
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, miss);
+        if (b == 0 && m) keys[w0 + w] = m;  // each word has one owner warp
     }
-    const uint32_t m = __ballot_sync(0xFFFFFFFFu, miss);
-    if (b == 0 && m) keys[w0 + w] = m;  // each word has one owner warp
 }
 
 // k_touch_up over the sparse form: a thread per table slot; the level-(lev-1)
@@ -959,10 +965,12 @@ void launch_keys_box(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 o
         const long long pnw = (dom.d[lev].nbits + 31) >> 5;
         const size_t smem = pnw <= kTouchSmemWords ? (size_t)pnw * 4 : 0;
         // 1024 threads per block: fewer blocks flushing the parent words
-        k_touch_up<<<counted(blocks_for(nw * 32, 1024)), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
+        const unsigned blocks = std::min<unsigned>(blocks_for(nw * 32, 1024), 152u * 2u);
+        k_touch_up<<<counted(blocks), 1024, smem, s>>>(dom.d[lev - 1], dom.d[lev], t.lgres[lev], touched, err);
     }
     const long long nw_all = (dom.d[depth - 1].bitbase + dom.d[depth - 1].nbits + 31) >> 5;
-    k_resolve_touched<<<counted(blocks_for(nw_all * 32, 128)), 128, 0, s>>>(t, lg, depth, dom, touched, bitmap, markers);
+    k_resolve_touched<<<counted(std::min<unsigned>(blocks_for(nw_all * 32, 128), 152u * 16u)), 128, 0, s>>>(
+        t, lg, depth, dom, nw_all, touched, bitmap, markers);
 }
 void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const int lo[3], const int dim[3],
                             int lgrange0, cudaStream_t s) {
