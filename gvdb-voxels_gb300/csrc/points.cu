@@ -505,6 +505,9 @@ __constant__ float kRcp16[17] = {0.0f,       1.0f,       0.5f,       1.0f / 3,  
                                  1.0f / 6,   1.0f / 7,   0.125f,     1.0f / 9,  0.1f,      1.0f / 11,
                                  1.0f / 12,  1.0f / 13,  1.0f / 14,  1.0f / 15, 0.0625f};
 constexpr int kQueue = 64;  // per-warp point queue of the gather form (SoA x, y, z)
+// scatter form: reaches of cutoffs below this radius (boxes of at most 4 voxels a side)
+// are walked with the entries' columns packed across the warp
+constexpr float kPackedReach = 2.0f;
 constexpr int kLive = 256;  // live points per batch of the scatter form
 constexpr int kScratch = kLive * 16 > (kGatherThreads / 32) * 3 * kQueue * 4 ? kLive * 16
                                                                               : (kGatherThreads / 32) * 3 * kQueue * 4;
@@ -822,7 +825,7 @@ static_assert(make_layer_run_table(1).n == 87 && make_layer_run_table(2).n == 11
 // kMinB blocks per SM, from the tuning table (10 or 8).  10 (48 registers; the 20.9 KiB
 // of shared memory per block allows 10): measured 0.774 ms on the fluid frame against
 // 0.787 at 9 and 0.798 at 8
-template <typename T, int kMinB>
+template <typename T, int kMinB, bool kPackedWalk>
 __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __restrict__ gtab,
                                                            const uint32_t* __restrict__ bin_off,
                                                            const float4* __restrict__ pts,
@@ -971,6 +974,60 @@ __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __
             __syncthreads();
             const int nl = nlive;
             const float rc2 = __fmul_rn(gp.rcut, gp.rcut);
+            if constexpr (kPackedWalk) {
+                // small reaches (a few columns each): a warp takes 32 entries at a time and
+                // lays their columns out in one list, a lane per (entry, column) item, so that
+                // lanes are not left idle by entries of fewer than 32 columns; each lane walks
+                // z over its own column's cut of the cutoff sphere
+                for (int e0 = warp * 32; e0 < nl; e0 += kGatherThreads) {
+                    const int e = e0 + lane;
+                    float4 L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    int ncol = 0, nx = 1;
+                    if (e < nl) {
+                        L = live_pts[e];
+                        const int bx = __float_as_int(L.w);
+                        nx = ((bx >> 4) & 15) - (bx & 15) + 1;
+                        ncol = nx * (((bx >> 12) & 15) - ((bx >> 8) & 15) + 1);
+                    }
+                    const float rnx = __frcp_rn((float)nx);  // rounded 1 / nx, as kRcp16
+                    int incl = ncol;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    const int pre = incl - ncol, total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+                    for (int t0 = 0; t0 < total; t0 += 32) {
+                        const int t = t0 + lane;
+                        int j = 0;  // entry of item t: the last lane with pre <= t
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1) {
+                            const int pj = __shfl_sync(0xFFFFFFFFu, pre, j + step);
+                            if (pj <= t) j += step;
+                        }
+                        const float jx = __shfl_sync(0xFFFFFFFFu, L.x, j), jy = __shfl_sync(0xFFFFFFFFu, L.y, j);
+                        const float jz = __shfl_sync(0xFFFFFFFFu, L.z, j);
+                        const int bx = __shfl_sync(0xFFFFFFFFu, __float_as_int(L.w), j);
+                        const int jnx = __shfl_sync(0xFFFFFFFFu, nx, j);
+                        const float jr = __shfl_sync(0xFFFFFFFFu, rnx, j);
+                        const int k = t - __shfl_sync(0xFFFFFFFFu, pre, j);
+                        const int ry = (int)__fmul_rn((float)k + 0.5f, jr);  // k / nx, as in the walk below
+                        const int x = (bx & 15) + (k - ry * jnx), y = ((bx >> 8) & 15) + ry;
+                        const float dx = fsub(jx, (float)(ox + x)), dy = fsub(jy, (float)(oy + y));
+                        const float dxy = __fmaf_rn(dy, dy, __fmul_rn(dx, dx));
+                        if (!(t < total && __float_as_uint(dxy) < gp.tbits)) continue;
+                        const float zr = sqrt_approx(fsub(rc2, dxy));  // rcut's margin covers its error
+                        const float lz = fsub(jz, (float)oz);
+                        const int za = max((bx >> 16) & 15, (int)ceilf(lz - zr)), zb = min((bx >> 20) & 15, (int)floorf(lz + zr));
+                        uint32_t* col = tile + (za << 8) + (y << 4) + x;
+                        float fz = (float)(oz + za);  // integer-valued: steps of 1 are exact
+                        for (int z = za; z <= zb; z++, col += 256, fz += 1.0f) {
+                            const float dz = fsub(jz, fz);
+                            atomicMin(col, __float_as_uint(__fmaf_rn(dz, dz, dxy)));
+                        }
+                    }
+                }
+            } else
             // warps take the live entries in turn; a warp covers all of its entry's
             // reach (rows in groups of 4), so an entry is decoded once, not once per
             // warp, and warps may update the same voxel: shared atomicMin
@@ -1587,6 +1644,16 @@ void launch_push_check(const TreeView& t, const LeafGrid& lg, const uint32_t* sc
                        int ax, int ay, long long n, int* bad, cudaStream_t s) {
     k_push_check<<<counted(blocks_for(std::max(n, 1ll), 256)), 256, 0, s>>>(t, lg, scmap, amap, used, ax, ay, n, bad);
 }
+// the gather of one storage type and residency; the packed walk for cutoff radii below
+// kPackedReach (a kernel of its own, so that the other keeps its code)
+template <typename T, int kMinB>
+void launch_gather_kernel(unsigned nb, const int4* gtab, const uint32_t* bin_off, const float4* pts, const int4* offs,
+                          int noffs, const GatherParams& gp, void* interior, cudaStream_t s) {
+    if (gp.rcut < kPackedReach)
+        k_gather<T, kMinB, true><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (T*)interior);
+    else
+        k_gather<T, kMinB, false><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (T*)interior);
+}
 void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, long long nbricks, const uint32_t* scmap,
                    const uint32_t* bin_off, const float4* pts, const int4* offs, int noffs, const GatherParams& gp,
                    int4* gtab, void* interior, cudaStream_t s) {
@@ -1595,21 +1662,13 @@ void launch_gather(const TreeView& t, const LeafGrid& lg, const int* linked, lon
         t, lg, linked, nbricks, scmap, bin_off, gp.ax, gp.ay, gp.long_min, gp.order, gtab);
     const unsigned nb = (unsigned)nbricks;
     if (gp.min_blocks == 8) {
-        if (gp.dtype == 3)
-            k_gather<float, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
-        else if (gp.dtype == 100)
-            k_gather<__half, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
-        else
-            k_gather<__nv_bfloat16, 8><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
-                                                                    (__nv_bfloat16*)interior);
+        if (gp.dtype == 3) launch_gather_kernel<float, 8>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
+        else if (gp.dtype == 100) launch_gather_kernel<__half, 8>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
+        else launch_gather_kernel<__nv_bfloat16, 8>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
     } else {
-        if (gp.dtype == 3)
-            k_gather<float, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (float*)interior);
-        else if (gp.dtype == 100)
-            k_gather<__half, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp, (__half*)interior);
-        else
-            k_gather<__nv_bfloat16, 10><<<counted(nb), kGatherThreads, 0, s>>>(gtab, bin_off, pts, offs, noffs, gp,
-                                                                     (__nv_bfloat16*)interior);
+        if (gp.dtype == 3) launch_gather_kernel<float, 10>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
+        else if (gp.dtype == 100) launch_gather_kernel<__half, 10>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
+        else launch_gather_kernel<__nv_bfloat16, 10>(nb, gtab, bin_off, pts, offs, noffs, gp, interior, s);
     }
 }
 void launch_list_count(const TreeView& t, const LeafGrid& lg, PointSrc p, float3 trans, float R, Quant q,
