@@ -886,9 +886,21 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 500.0, 2000.0])
     ap.add_argument("--fused-apron", type=int, default=1, choices=[0, 1],
                     help="gathers write the neighbours' apron voxels (1) or UpdateApron copies them all (0)")
+    ap.add_argument("--surface-only", action="store_true",
+                    help="only the surface workload (3 warm-up and --steps timed frames per storage type; "
+                         "one JSON line with its times, for profiling that workload alone)")
     args = ap.parse_args()
     if args.impl == "reference":
         return bench_reference(args)
+    if args.surface_only:
+        import torch
+
+        import build_lib
+
+        torch.cuda.set_device(0)
+        build_lib.build()
+        print(json.dumps({"surface": bench_surface(args, steps=args.steps)}), flush=True)
+        return 0
     return bench_ours(args)
 
 
