@@ -667,16 +667,17 @@ __device__ __forceinline__ Node key_node(int lev, int lgrange, const KeyDomain& 
 // (SetupNode, VG.cpp:2512-2524) at pool index base + rank
 __global__ void k_alloc_nodes(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ prefix, long long word0,
                               long long nwords, int lev, int lgrange, KeyDomain d, long long base, Node* nodes) {
-    // a lane per bit: rank = the word's prefix + the set bits below this one
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = g >> 5;
-    if (w >= nwords) return;
-    const int b = (int)(g & 31);
-    const uint32_t bits = bm[word0 + w];
-    if (!((bits >> b) & 1u)) return;
-    const long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0] + __popc(bits & ((1u << b) - 1u));
-    const long long li = (word0 + w) * 32 + b - d.bitbase;  // bitbase is word aligned
-    nodes[base + rank] = key_node(lev, lgrange, d, li, base + rank);
+    // a lane per bit, warps striding over the words (the grid is capped: a sparse level's
+    // empty words cost a load each): rank = the word's prefix + the set bits below this one
+    const int b = (int)(threadIdx.x & 31);
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += wstride) {
+        const uint32_t bits = bm[word0 + w];
+        if (!((bits >> b) & 1u)) continue;
+        const long long rank = (long long)prefix[word0 + w] - (long long)prefix[word0] + __popc(bits & ((1u << b) - 1u));
+        const long long li = (word0 + w) * 32 + b - d.bitbase;  // bitbase is word aligned
+        nodes[base + rank] = key_node(lev, lgrange, d, li, base + rank);
+    }
 }
 
 // the sparse form's allocation: a thread per sorted key of the level
@@ -981,7 +982,8 @@ void launch_build_leaf_grid(const TreeView& t, long long n, int* cells, const in
 void launch_alloc_nodes(const uint32_t* bm, const uint32_t* prefix, long long word0, long long nwords,
                         int lev, int lgrange, const KeyDomain& d, long long base, Node* nodes, cudaStream_t s) {
     if (nwords <= 0) return;
-    k_alloc_nodes<<<counted(blocks_for(nwords * 32, 256)), 256, 0, s>>>(bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
+    k_alloc_nodes<<<counted(std::min<unsigned>(blocks_for(nwords * 32, 256), 152u * 8u)), 256, 0, s>>>(
+        bm, prefix, word0, nwords, lev, lgrange, d, base, nodes);
 }
 void launch_hash_compact(const KeyHash& h, unsigned long long* out, unsigned int* count, cudaStream_t s) {
     k_hash_compact<<<counted(grid_stride_blocks((long long)(h.mask + 1), 256)), 256, 0, s>>>(h, out, count);
