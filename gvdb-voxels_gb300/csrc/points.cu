@@ -822,9 +822,11 @@ static_assert(make_layer_run_table(1).n == 87 && make_layer_run_table(2).n == 11
 //   Skipped points cannot lower any voxel's minimum, so the result is exact.
 //
 // One coalesced write of the brick from the tile at the end.
-// kMinB blocks per SM, from the tuning table (10 or 8).  10 (48 registers; the 20.9 KiB
+// kMinB blocks per SM, from the tuning table (10 or 8).  10 (48 registers; the 21.4 KiB
 // of shared memory per block allows 10): measured 0.774 ms on the fluid frame against
-// 0.787 at 9 and 0.798 at 8
+// 0.787 at 9 and 0.798 at 8.  kPackedWalk: the scatter form's walk for cutoff radii
+// below kPackedReach (columns of 32 entries packed across the warp), a kernel of its
+// own so that the walk for larger reaches keeps its code.
 template <typename T, int kMinB, bool kPackedWalk>
 __global__ void __launch_bounds__(kGatherThreads, kMinB) k_gather(const int4* __restrict__ gtab,
                                                            const uint32_t* __restrict__ bin_off,
